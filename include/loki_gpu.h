@@ -1,0 +1,234 @@
+/*
+ * loki_gpu.h - C ABI of the GB300 electron Monte Carlo backend.
+ *
+ * The backend replaces the numerical core of LoKI-MC's BoltzmannMC engine
+ * (Code/LoKI-MC/Sources/BoltzmannMC.C, Code/LoKI-MC/Headers/BoltzmannMC.h).
+ * The reference has no foreign-function interface: the engine is a template
+ * parameter of Setup<T> and Output<T> (Code/LoKI-MC/Sources/lokimc.C:14-41,
+ * 78-80). Each entry point below names the reference routine or data it
+ * stands in for; a C++ adapter class (BoltzmannMCGPU)
+ * calls them from the reference's host code.
+ *
+ * Conventions: plain C types, host pointers with explicit sizes, int status
+ * returns (LGPU_OK = 0). A context owns all device memory; no pointer passed
+ * in is retained after a call returns. One host thread per context.
+ */
+#ifndef LOKI_GPU_H
+#define LOKI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference's failures call Message::error
+ * (Code/LoKI-MC/Sources/Message.C:6-16), which logs and exits; the host maps
+ * a non-zero status onto it. */
+#define LGPU_OK 0
+#define LGPU_ERR_BAD_ARG 1
+#define LGPU_ERR_OOM 2
+#define LGPU_ERR_ENERGY_ABOVE_TABLE 3 /* BoltzmannMC.C:1426-1430 */
+#define LGPU_ERR_TIMEOUT 4
+#define LGPU_ERR_CUDA 5
+#define LGPU_ERR_STATE 6              /* call out of order */
+#define LGPU_ERR_OVERFLOW 7           /* a device buffer or bounded loop ran out */
+#define LGPU_ERR_NO_DEVICE 8
+
+typedef struct lgpu_ctx lgpu_ctx;
+
+/* Numerical settings of one context: the electronKinetics.numericsMC keys the
+ * reference reads in its constructor (BoltzmannMC.h:262-376) plus the device
+ * and seed. Collision-count limits are given as in the setup file, i.e. in
+ * multiples of nElectrons (BoltzmannMC.h:295-303). */
+typedef struct lgpu_config {
+  int device;
+  uint64_t seed;
+  double n_electrons;               /* nElectrons */
+  int n_interp;                     /* nInterpPoints (default 1e4) */
+  int gas_temperature_effect;       /* 0 false, 1 true, 2 smartActivation */
+  int sharing;                      /* ionizationOperatorType: 0 equalSharing, 1 oneTakesAll, 2 usingSDCS, 3 randomUniform */
+  double init_temp_ratio;           /* initialElecTempOverGasTemp (default 0.01) */
+  double min_coll_before_ss;        /* minCollisionsBeforeSteadyState (x nElectrons) */
+  double max_coll_before_ss;        /* maxCollisionsBeforeSteadyState (x nElectrons) */
+  double max_coll_after_ss;         /* maxCollisionsAfterSteadyState (x nElectrons) */
+  double req_integration_points;    /* nIntegrationPoints (default 200) */
+  double req_ss_times;              /* nIntegratedSSTimes */
+  double req_abs_time;              /* integratedAbsoluteTime */
+  int errors_checked;               /* relError present */
+  double req_err_mean_energy, req_err_flux_v, req_err_flux_d, req_err_bulk_v, req_err_bulk_d, req_err_power;
+  int n_energy_cells, n_cos_cells, n_radial_cells, n_axial_cells, n_phases;
+  double sync_x;                    /* synchronizationTimeXMaxCollisionFrequency */
+  int sync_oversampling;            /* synchronizationOverSampling */
+  double max_seconds;               /* wall-clock cap of one solve (<= 0: none) */
+  long long max_sync_steps;         /* interval cap of one solve (<= 0: none) */
+} lgpu_config;
+
+/* Fills the reference's defaults (BoltzmannMC.h:50-76). */
+void lgpu_config_default(lgpu_config* cfg);
+
+/* One Monte Carlo process, flattened as BoltzmannMC::allocateEvaluateVariablesFirstTime
+ * does (BoltzmannMC.C:29-271): every non-Effective collision once, a reversible
+ * one followed immediately by its superelastic copy. */
+typedef struct lgpu_process {
+  int type;             /* 0 conservative, 1 ionization, 2 attachment (GeneralDefinitions.h:34-36) */
+  int is_super;         /* superelastic copy of the process before it */
+  int is_elastic;       /* Elastic collision (power bookkeeping) */
+  int sampler;          /* 0 isotropic, 1 forward, 2 bornDipole, 3 surendra, 4 coulombScreen, 5 momentumConservationIonization */
+  double sampler_p0, sampler_p1;
+  double superw;        /* g_target / g_product (superelastic), else 0 */
+  double emin, emax;    /* energyMinLimits / energyMaxLimits (eV) */
+  double rel_dens;      /* relDensities */
+  double mass;          /* targetMasses (kg) */
+  double eloss;         /* energyLosses (eV), negative for superelastic */
+  double wparam;        /* wParameters (eV) */
+  int raw_len;          /* threshold-clipped raw cross section (crossSectionEnergies/Values) */
+  const double* raw_e;
+  const double* raw_v;
+} lgpu_process;
+
+typedef struct lgpu_gas {
+  int first, last;      /* firstProcessIndexPerGas / lastProcessIndexPerGas */
+  double fraction;      /* gasFractions */
+} lgpu_gas;
+
+/* Working conditions of one job (WorkingConditions.h:55-132). */
+typedef struct lgpu_conditions {
+  double gas_density;            /* m^-3 */
+  double gas_temperature;        /* K */
+  double reduced_field_td;       /* E/N (Td) */
+  double field_angle_deg;        /* elecFieldAngle */
+  double excitation_freq_hz;     /* excitationFrequency */
+  double reduced_mag_field_hx;   /* B/N (Hx) */
+} lgpu_conditions;
+
+/* Results of one solve (BoltzmannMC.C:1484-1649 and the public members that
+ * Output.h reads). */
+typedef struct lgpu_result {
+  double mean_energy, mean_energy_err;
+  double flux_v[3], flux_v_err[3];
+  double flux_d[9], flux_d_err[9];
+  double bulk_v[3], bulk_v_err[3];
+  double bulk_d[9], bulk_d_err[9];
+  double power_field, power_growth, power_balance_rel_err;
+  double ss_time, final_time;
+  double trial_freq;
+  double max_eedf_energy;
+  double real_collisions, null_collisions;     /* totalCollisionCounter, nullCollisionCounter */
+  double coll_at_ss, null_at_ss;               /* collisionCounterAtSS, nullCollisionCounterAtSS */
+  long long integration_points;                /* nIntegrationPoints */
+  long long sampling_points;                   /* nSamplingPoints */
+  long long first_integration_index;
+  long long sync_steps;
+  double elapsed;                              /* seconds */
+  int capped;                                  /* stopped by max_seconds / max_sync_steps */
+} lgpu_result;
+
+/* Progress report of lgpu_advance. */
+typedef struct lgpu_step_report {
+  double time;                /* absolute simulation time (s) */
+  double trial_freq;          /* trialCollisionFrequency */
+  double max_energy;          /* largest electron energy (eV) */
+  double mean_energy;         /* ensemble mean at the last sample (eV) */
+  double real_collisions;     /* cumulative */
+  double null_collisions;     /* cumulative */
+  long long sync_steps;       /* cumulative */
+} lgpu_step_report;
+
+/* Device-time accounting of the main advance kernel (CUDA events on the
+ * context's stream). */
+typedef struct lgpu_timing {
+  double advance_ms;          /* summed duration of the main advance launches */
+  long long advance_launches;
+  double electron_steps;      /* electrons advanced by those launches */
+  long long kernel_launches;  /* every kernel this context launched */
+  double h2d_bytes;           /* host-to-device bytes copied by this context */
+  double d2h_bytes;           /* device-to-host bytes copied by this context */
+} lgpu_timing;
+
+/* Context lifetime (replaces `new BoltzmannMC(setup)`, BoltzmannMC.h:244-380). */
+int lgpu_create(const lgpu_config* cfg, lgpu_ctx** out);
+int lgpu_destroy(lgpu_ctx* ctx);
+/* Last error message of the context (empty when none). Returns the length. */
+int lgpu_last_error(const lgpu_ctx* ctx, char* buf, size_t size);
+/* The context's CUDA stream (a cudaStream_t), for callers that order work around it. */
+void* lgpu_stream(lgpu_ctx* ctx);
+
+/* Process set: the per-process arrays of BoltzmannMC.C:29-271 plus
+ * energyMaxElastic (BoltzmannMC.C:157-159). Uploads the raw tables once. */
+int lgpu_set_processes(lgpu_ctx* ctx, const lgpu_process* procs, int n_procs, const lgpu_gas* gases, int n_gases,
+                       double energy_max_elastic);
+
+/* Field and gas state of the next job (BoltzmannMC.C:428-489): E vector from
+ * E/N and the angle, sqrt(2) for AC, cyclotron frequency from B/N. */
+int lgpu_set_conditions(lgpu_ctx* ctx, const lgpu_conditions* cond);
+
+/* Start ensemble (BoltzmannMC.C:491-516): positions zero, Maxwellian
+ * velocities at initialElecTempOverGasTemp * Tg, first tables at twice the
+ * largest energy, trial frequency at their maximum. Resets every tally. */
+int lgpu_init_ensemble(lgpu_ctx* ctx);
+
+/* n synchronisation intervals of the plain method (BoltzmannMC.C:617-688),
+ * each followed by an ensemble sample; no steady-state logic. */
+int lgpu_advance(lgpu_ctx* ctx, int n_intervals, lgpu_step_report* report);
+
+/* The whole evaluateEEDF loop (BoltzmannMC.C:299-426): stepping, sampling,
+ * steady-state detection, error control and the time averages. */
+int lgpu_solve(lgpu_ctx* ctx, lgpu_result* result);
+
+/* Per-process MC results after a solve: collisionCounters, averagedRateCoeffs
+ * (BoltzmannMC.C:1627-1638), averagedPowerGain/LossProcesses
+ * (BoltzmannMC.C:1640-1649). Any pointer may be NULL; each has n_procs entries. */
+int lgpu_get_process_results(lgpu_ctx* ctx, unsigned long long* counts, double* rate, double* power_gain,
+                             double* power_loss, int n_procs);
+
+/* Time-averaged distributions after a solve (BoltzmannMC.C:1574-1605,
+ * 1728-1741). Sizes follow the config; NULL skips an output.
+ * eedf_cells/eedf/efadf/esadf: n_energy_cells; eadf: n_energy_cells x n_cos_cells;
+ * evdf: n_radial_cells x n_axial_cells (row-major), radial/axial cell centres;
+ * eedf_periodic: n_phases x n_energy_cells. */
+int lgpu_get_distributions(lgpu_ctx* ctx, double* eedf_cells, double* eedf, double* efadf, double* esadf,
+                           double* eadf, double* evdf, double* radial_cells, double* axial_cells,
+                           double* eedf_periodic);
+
+/* Sampled time series (BoltzmannMC.h:124-175). which: 0 samplingTimes,
+ * 1 meanEnergies, 2 meanPositions (x3), 3 meanVelocities (x3),
+ * 4 fluxDiffusionCoeffs (x9), 5 positionCovariances (x9), 6 bulkVelocities (x3),
+ * 7 bulkDiffusionCoeffs (x9). Returns the number of rows written (<= max_rows),
+ * or a negative status. */
+long long lgpu_get_series(lgpu_ctx* ctx, int which, double* out, long long max_rows);
+
+int lgpu_get_timing(lgpu_ctx* ctx, lgpu_timing* timing);
+
+/* ---- parity entry points: the production device functions on given inputs ---- */
+
+/* Rebuilds the tables at a given maximum energy (BoltzmannMC.C:561-615) and
+ * optionally returns them: grid/nu_tot/nu_max [M] in FP64, sig/cum [M*P] as the
+ * FP32 values the kernels use. Any output may be NULL. */
+int lgpu_build_tables(lgpu_ctx* ctx, double max_energy, double* nu_tot, double* nu_max, float* sig, float* cum);
+
+/* Overrides the field the kernels use (the reference harness sets
+ * electricField, excitationFrequency, reducedMagField and cyclotronFrequency
+ * directly): E in V/m (amplitude), f in Hz, B/N in Hx (only compared with
+ * zero), cyclotron frequency in rad/s. */
+int lgpu_set_field_raw(lgpu_ctx* ctx, const double e_field[3], double freq_hz, double red_mag_hx,
+                       double cyclotron);
+
+/* n free flights (BoltzmannMC.C:804-905): start time t (s, absolute), length
+ * dt, position and velocity [n x 3]. Outputs position, velocity, energy and
+ * field energy gain. */
+int lgpu_replay_flights(lgpu_ctx* ctx, int n, const double* t, const double* dt, const double* pos,
+                        const double* vel, double* pos_out, double* vel_out, double* energy_out, double* gain_out);
+
+/* n collision events (BoltzmannMC.C:907-1280) driven by recorded uniforms
+ * (u_stride per event, used in order). out: n x 11 = chosen process (-1
+ * null), velocity (3), energy, energy change, change / incident energy,
+ * secondary velocity (3), secondary energy. used: uniforms consumed. */
+int lgpu_replay_collisions(lgpu_ctx* ctx, int n, const double* nu_trial, const double* vel, const double* energy,
+                           const double* uniforms, int u_stride, double* out, int* used);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

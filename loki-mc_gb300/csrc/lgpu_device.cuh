@@ -1,0 +1,505 @@
+// lgpu_device.cuh - per-electron device physics of the electron Monte Carlo
+// path: counter-based random numbers, closed-form free flights, the
+// null-collision test and process choice on interpolated tables, and the
+// collision kinematics. Everything here runs in FP32; the FP64 parts of the
+// method (absolute time, phase origin, position origin, tallies) live in the
+// host runtime and the reduction kernels.
+//
+// Each function names the reference routine whose physics it implements
+// (paths relative to the reference's Code/ directory).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lgpu_types.h"
+
+namespace lgpu {
+
+// Constant.h:6-8
+constexpr double kQe = 1.6021766208e-19;
+constexpr double kMe = 9.10938356e-31;
+constexpr double kKb = 1.38064852e-23;
+constexpr float kTwoPiF = 6.28318530717958647692f;
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon et al., SC'11): counter (4 x u32) and key (2 x u32)
+// give four independent 32-bit words.
+struct Philox {
+  uint4 ctr;
+  uint2 key;
+  __device__ __forceinline__ static uint4 round(uint4 c, uint2 k) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    return make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  __device__ __forceinline__ uint4 next() {
+    uint4 c = ctr;
+    uint2 k = key;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      c = round(c, k);
+      k.x += 0x9E3779B9u;
+      k.y += 0xBB67AE85u;
+    }
+    c = round(c, k);
+    ctr.w += 1u;  // the per-electron event counter lives in the last word
+    return c;
+  }
+};
+
+// Uniform in (0, 1]: 24-bit lattice (k + 1) * 2^-24.
+__device__ __forceinline__ float u01_oc(uint32_t x) { return (float)((x >> 8) + 1u) * 5.9604644775390625e-8f; }
+// Uniform in (0, 1): 23-bit lattice (k + 0.5) * 2^-23.
+__device__ __forceinline__ float u01_oo(uint32_t x) { return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-7f; }
+
+// A stream of uniforms for one electron: four words per Philox call, used in
+// order. Counter = (electron id, interval index low, interval index high,
+// event word); key = the run seed.
+struct PhiloxStream {
+  Philox ph;
+  uint4 buf;
+  int left;
+  __device__ __forceinline__ void init(uint32_t electron, uint64_t interval, uint64_t seed, uint32_t salt) {
+    ph.ctr = make_uint4(electron, (uint32_t)interval, (uint32_t)(interval >> 32) ^ (salt << 16), 0u);
+    ph.key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    left = 0;
+  }
+  __device__ __forceinline__ uint32_t word() {
+    if (left == 0) {
+      buf = ph.next();
+      left = 4;
+    }
+    uint32_t w = buf.x;
+    buf.x = buf.y;
+    buf.y = buf.z;
+    buf.z = buf.w;
+    --left;
+    return w;
+  }
+  // (0,1] for choices and samplers whose reference draw allows one
+  __device__ __forceinline__ float oc() { return u01_oc(word()); }
+  // (0,1) for the free-flight exponential (reference excludes 0 and 1)
+  __device__ __forceinline__ float oo() { return u01_oo(word()); }
+  // [0,1]-semantics draws take the (0,1] lattice
+  __device__ __forceinline__ float cc() { return u01_oc(word()); }
+};
+
+// Replay of recorded uniforms (parity tests): values are taken in order.
+struct ReplayStream {
+  const double* u;
+  int n, pos;
+  __device__ __forceinline__ float take() { return pos < n ? (float)u[pos++] : (pos++, 0.5f); }
+  __device__ __forceinline__ float oc() { return take(); }
+  __device__ __forceinline__ float oo() { return take(); }
+  __device__ __forceinline__ float cc() { return take(); }
+};
+
+// ------------------------------------------------------------ free flight
+
+// Closed-form free flight (BoltzmannMC.C:804-905). `phi0` is the phase
+// w*t (AC, AC+B) or W*t (resonance) at the flight start, reduced to [0, 2pi)
+// by the caller in FP64. Position is an FP32 offset. Returns nothing; the
+// caller recomputes the energy from the new velocity.
+__device__ __forceinline__ void free_flight(const FieldF& f, float phi0, float dt, float3& p, float3& v) {
+  switch (f.mode) {
+    case kFieldDC: {
+      // x += v dt + a dt^2/2 ; v += a dt
+      const float hdt2 = 0.5f * dt * dt;
+      p.x += v.x * dt + f.ax * hdt2;
+      p.y += v.y * dt + f.ay * hdt2;
+      p.z += v.z * dt + f.az * hdt2;
+      v.x += f.ax * dt;
+      v.y += f.ay * dt;
+      v.z += f.az * dt;
+      break;
+    }
+    case kFieldAC: {
+      // harmonic E(t) = E cos(w t): BoltzmannMC.C:816-831
+      const float w = f.w;
+      float sPhi, cPhi, sPh, cPh;
+      sincosf(phi0, &sPhi, &cPhi);
+      const float wdt = w * dt;
+      sincosf(phi0 + wdt, &sPh, &cPh);
+      const float k = f.e_me / w;  // e/(m w)
+      const float aux1 = k / w * (cPh + wdt * sPhi - cPhi);
+      const float aux2 = k * (sPhi - sPh);
+      p.x += v.x * dt + f.Ex * aux1;
+      p.y += v.y * dt;
+      p.z += v.z * dt + f.Ez * aux1;
+      v.x += f.Ex * aux2;
+      v.z += f.Ez * aux2;
+      break;
+    }
+    case kFieldB: {
+      // DC E in the x-z plane, B along z: BoltzmannMC.C:835-849
+      const float W = f.W;
+      const float Wdt = W * dt;
+      float sW, cW;
+      sincosf(Wdt, &sW, &cW);
+      const float sh = sinf(0.5f * Wdt);
+      const float cWm1 = -2.0f * sh * sh;  // cos(W dt) - 1 without cancellation
+      const float sW_W = sW / W;
+      const float aux2 = cWm1 / W;
+      const float vEx = f.e_me * f.Ex / W;
+      const float az = f.e_me * f.Ez;
+      const float vx0 = v.x, vy0 = v.y, vz0 = v.z;
+      p.x += vx0 * sW_W + (vy0 + vEx) * aux2;
+      p.y += -vx0 * aux2 + vy0 * sW_W + vEx * (sW_W - dt);
+      p.z += vz0 * dt - 0.5f * az * dt * dt;
+      v.x = vx0 * cW - vy0 * sW - vEx * sW;
+      v.y = vx0 * sW + vy0 * cW + vEx * cWm1;
+      v.z = vz0 - az * dt;
+      break;
+    }
+    case kFieldECR: {
+      // w == W (cyclotron resonance): BoltzmannMC.C:850-872
+      const float W = f.W;
+      float sPhi, cPhi, sW, cW, sPh, cPh;
+      sincosf(phi0, &sPhi, &cPhi);
+      const float Wdt = W * dt;
+      sincosf(Wdt, &sW, &cW);
+      sincosf(phi0 + Wdt, &sPh, &cPh);
+      const float cOpp = cosf(phi0 - Wdt);
+      const float sh = sinf(0.5f * Wdt);
+      const float cWm1 = -2.0f * sh * sh;
+      const float k = f.e_me / W;
+      const float vEx = k * f.Ex, vEz = k * f.Ez;
+      const float sW_W = sW / W, cWm1_W = cWm1 / W, cPh_W = cPh / W;
+      const float vx0 = v.x, vy0 = v.y, vz0 = v.z;
+      p.x += vx0 * sW_W + vy0 * cWm1_W - 0.25f * vEx * (cPh_W - cOpp / W + 2.0f * dt * sPh);
+      p.y += -vx0 * cWm1_W + vy0 * sW_W + 0.5f * vEx * (dt * cPh_W - 2.0f * cWm1_W * sPhi - cPhi * sW_W);
+      p.z += vz0 * dt + vEz * (cPh_W - cPhi / W + dt * sPhi);
+      v.x = vx0 * cW - vy0 * sW - 0.5f * vEx * (Wdt * cPh + cPhi * sW);
+      v.y = vx0 * sW + vy0 * cW - 0.5f * vEx * (Wdt * cW * sPhi + (Wdt * cPhi - sPhi) * sW);
+      v.z = vz0 + vEz * (sPhi - sPh);
+      break;
+    }
+    default: {
+      // general AC E + DC B: BoltzmannMC.C:873-897
+      const float w = f.w, W = f.W;
+      float sPhi, cPhi, sw, cw, sPh, cPh, sW, cW;
+      sincosf(phi0, &sPhi, &cPhi);
+      const float wdt = w * dt;
+      sincosf(wdt, &sw, &cw);
+      sincosf(phi0 + wdt, &sPh, &cPh);
+      const float Wdt = W * dt;
+      sincosf(Wdt, &sW, &cW);
+      const float sh = sinf(0.5f * Wdt);
+      const float cWm1 = -2.0f * sh * sh;
+      const float w2 = w * w, W2 = W * W, d = w2 - W2;
+      const float vEx = f.e_me / W * f.Ex;
+      const float vEz = f.e_me / w * f.Ez;
+      const float vEx_d = vEx / d;
+      const float WvEx_d = W * vEx_d;
+      const float sW_W = sW / W, cWm1_W = cWm1 / W;
+      const float wsPhi = w * sPhi;
+      const float vx0 = v.x, vy0 = v.y, vz0 = v.z;
+      p.x += vx0 * sW_W + vy0 * cWm1_W + WvEx_d * (cPhi * (cw - cW) + (wsPhi * sW_W - sPhi * sw));
+      p.y += -vx0 * cWm1_W + vy0 * sW_W - vEx_d / w * ((W2 + w2 * cW - w2) * sPhi + W2 * (w * cPhi * sW_W - sPh));
+      p.z += vz0 * dt + vEz * ((cPh - cPhi) / w + dt * sPhi);
+      v.x = vx0 * cW - vy0 * sW + WvEx_d * w * (cW * sPhi - sPh + cPhi / w * W * sW);
+      v.y = vx0 * sW + vy0 * cW + vEx_d * W2 * (cPh - cPhi * cW + wsPhi * sW_W);
+      v.z = vz0 + vEz * (sPhi - sPh);
+      break;
+    }
+  }
+}
+
+// ------------------------------------------------------------ kinematics
+
+// Spherical angles without trigonometry (MathFunctions.C:143-163).
+struct Sph {
+  float speed, sT, cT, sP, cP;
+};
+__device__ __forceinline__ Sph cart2sph(float3 v) {
+  Sph s;
+  const float xy2 = v.x * v.x + v.y * v.y;
+  const float nxy = sqrtf(xy2);
+  s.speed = sqrtf(xy2 + v.z * v.z);
+  const float inv = 1.0f / s.speed;
+  s.sT = nxy * inv;
+  s.cT = v.z * inv;
+  if (nxy != 0.0f) {
+    const float ixy = 1.0f / nxy;
+    s.sP = v.y * ixy;
+    s.cP = v.x * ixy;
+  } else {
+    s.sP = 1.0f;
+    s.cP = 0.0f;
+  }
+  return s;
+}
+
+// Rotation of the scattering angles into the laboratory frame
+// (Yousfi 1994; MathFunctions.C:129-141).
+__device__ __forceinline__ float3 euler(float sChi, float cChi, float sEta, float cEta, const Sph& s) {
+  const float sCsE = sChi * sEta;
+  const float aux = sChi * cEta * s.cT + cChi * s.sT;
+  return make_float3(-sCsE * s.sP + aux * s.cP, sCsE * s.cP + aux * s.sP, -sChi * cEta * s.sT + cChi * s.cT);
+}
+
+// cos(chi) samplers (AngularScatteringFunctions.h:27-74).
+template <class Rng>
+__device__ __forceinline__ float sample_cos_chi(const ProcF& pr, float energy, float energy_after, Rng& rng) {
+  switch (pr.sampler) {
+    case kSamplerForward:
+      return 1.0f;
+    case kSamplerBornDipole: {
+      // Vialetto 2021, eq. 25
+      const float s = sqrtf(energy_after) + sqrtf(energy);
+      const float ratio = pr.eloss / (s * s);
+      const float r2 = ratio * ratio;
+      return 1.0f + 2.0f * r2 / (1.0f - r2) * (1.0f - powf(r2, -rng.cc()));
+    }
+    case kSamplerSurendra: {
+      // Vahedi 1995, eq. 9: (2 + e - 2 (1+e)^U) / e, written with expm1/log1p
+      const float u = rng.cc();
+      return (energy - 2.0f * expm1f(u * log1pf(energy))) / energy;
+    }
+    case kSamplerCoulombScreen: {
+      // Hagelaar 2000, eqs. 21-23
+      const float eps = (pr.sp0 == 0.0f) ? energy : energy_after;
+      const float sp = pr.sp1 / eps;
+      const float R = rng.cc();
+      return (sp + 1.0f - (2.0f * sp + 1.0f) * R) / (sp + 1.0f - R);
+    }
+    default:  // isotropic
+      return 1.0f - 2.0f * rng.cc();
+  }
+}
+
+// Result of one collision event.
+struct CollResult {
+  int chosen;         // process id, -1 null
+  float dE;           // energy change (eV) of the incident electron
+  int ionized;        // a secondary was created
+  float3 ej_v;        // secondary velocity
+};
+
+__device__ __forceinline__ float energy_of(float3 v, float half_me_over_e) {
+  return (v.x * v.x + v.y * v.y + v.z * v.z) * half_me_over_e;
+}
+
+// Collision kinematics of the chosen process (BoltzmannMC.C:1115-1280).
+// `tv` is the target velocity (zero for a cold gas). Returns false when the
+// event turns into a null collision (energy below the threshold after
+// interpolation, BoltzmannMC.C:1137-1140, 1169-1172, 1202-1205).
+template <class Rng>
+__device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr, bool thermal, float3 tv, float3& v,
+                                                float& energy, Rng& rng, CollResult& out) {
+  const float incident = energy;
+  if (pr.type == kConservative) {
+    if (thermal) {
+      // centre-of-mass kinematics with a moving target (BoltzmannMC.C:1125-1158)
+      const float3 rel = make_float3(v.x - tv.x, v.y - tv.y, v.z - tv.z);
+      const Sph s = cart2sph(rel);
+      const float relE = 0.5f * pr.red_mass * s.speed * s.speed * c.inv_qe;
+      const float relEA = relE - pr.eloss;
+      if (relEA <= 0.0f) return false;
+      const float cChi = sample_cos_chi(pr, relE, relEA, rng);
+      const float sChi = sqrtf(fmaxf(0.0f, 1.0f - cChi * cChi));
+      float sEta, cEta;
+      sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
+      const float3 ver = euler(sChi, cChi, sEta, cEta, s);
+      const float sa = sqrtf(fmaxf(0.0f, s.speed * s.speed - 2.0f / pr.red_mass * pr.eloss * c.qe));
+      const float inv_tot = 1.0f / (c.me + pr.mass);
+      const float fa = pr.mass * inv_tot;
+      v.x = fa * (sa * ver.x) + (c.me * v.x + pr.mass * tv.x) * inv_tot;
+      v.y = fa * (sa * ver.y) + (c.me * v.y + pr.mass * tv.y) * inv_tot;
+      v.z = fa * (sa * ver.z) + (c.me * v.z + pr.mass * tv.z) * inv_tot;
+    } else {
+      // target at rest (BoltzmannMC.C:1160-1187)
+      const Sph s = cart2sph(v);
+      const float eA = incident - pr.eloss;
+      if (eA <= 0.0f) return false;
+      const float cChi = sample_cos_chi(pr, incident, eA, rng);
+      const float sChi = sqrtf(fmaxf(0.0f, 1.0f - cChi * cChi));
+      float sEta, cEta;
+      sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
+      const float3 ver = euler(sChi, cChi, sEta, cEta, s);
+      const float sp = sqrtf(fmaxf(0.0f, (s.speed * s.speed - c.two_qe_over_me * pr.eloss) *
+                                             (1.0f - pr.mass_factor * (1.0f - cChi))));
+      v = make_float3(sp * ver.x, sp * ver.y, sp * ver.z);
+    }
+    energy = energy_of(v, c.half_me_over_e);
+    out.dE = energy - incident;
+    out.ionized = 0;
+    return true;
+  }
+  if (pr.type == kIonization) {
+    // BoltzmannMC.C:1195-1272
+    const float thr = pr.eloss;
+    if (incident < thr) return false;
+    const Sph s = cart2sph(v);
+    const float net = incident - thr;
+    float ej;
+    if (c.sharing == kSharingSDCS) {
+      ej = pr.wparam * tanf(rng.cc() * atanf(net / (2.0f * pr.wparam)));
+    } else if (c.sharing == kSharingRandom) {
+      ej = rng.cc() * net;
+    } else {
+      ej = c.sharing_factor * net;
+    }
+    const float scat = net - ej;
+    float cChiS, sChiS, cChiE, sChiE, sEtaS, cEtaS, sEtaE, cEtaE;
+    if (pr.sampler == kSamplerMomentumConservation) {
+      cChiS = sqrtf(scat / net);
+      sChiS = sqrtf(fmaxf(0.0f, 1.0f - cChiS * cChiS));
+      sincosf(kTwoPiF * rng.oc(), &sEtaS, &cEtaS);
+      cChiE = sqrtf(ej / net);
+      sChiE = sqrtf(fmaxf(0.0f, 1.0f - cChiE * cChiE));
+      sEtaE = -sEtaS;
+      cEtaE = -cEtaS;
+    } else {
+      cChiS = sample_cos_chi(pr, incident, scat, rng);
+      sChiS = sqrtf(fmaxf(0.0f, 1.0f - cChiS * cChiS));
+      sincosf(kTwoPiF * rng.oc(), &sEtaS, &cEtaS);
+      cChiE = sample_cos_chi(pr, incident, ej, rng);
+      sChiE = sqrtf(fmaxf(0.0f, 1.0f - cChiE * cChiE));
+      sincosf(kTwoPiF * rng.oc(), &sEtaE, &cEtaE);
+    }
+    const float3 vs = euler(sChiS, cChiS, sEtaS, cEtaS, s);
+    const float3 ve = euler(sChiE, cChiE, sEtaE, cEtaE, s);
+    const float ss = sqrtf(c.two_qe_over_me * scat), se = sqrtf(c.two_qe_over_me * ej);
+    v = make_float3(ss * vs.x, ss * vs.y, ss * vs.z);
+    out.ej_v = make_float3(se * ve.x, se * ve.y, se * ve.z);
+    energy = scat;
+    out.dE = -thr;
+    out.ionized = 1;
+    return true;
+  }
+  // attachment (BoltzmannMC.C:1274-1280)
+  out.dE = -incident;
+  out.ionized = 0;
+  return true;
+}
+
+// Row weights of the linear interpolation between table rows
+// (BoltzmannMC.C:1036-1047).
+__device__ __forceinline__ void row_weights(float eos, int M, int& i1, float& w1, float& w2) {
+  i1 = (int)fminf(eos, (float)(M - 1));
+  const int i2 = min(i1 + 1, M - 1);
+  w1 = (float)i2 - eos;
+  if (w1 < 0.0f) w1 = 0.0f;
+  w2 = 1.0f - w1;
+}
+
+// Process choice for a cold gas (BoltzmannMC.C:1033-1097): null test on the
+// interpolated total frequency, bisection over the interpolated cumulative
+// sums, backward skip of zero-rate processes. Returns -1 for null.
+template <class Rng>
+__device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, float energy, float speed, Rng& rng) {
+  const float r = nu_trial * rng.oc();
+  int i1;
+  float w1, w2;
+  row_weights(energy * t.inv_step, t.M, i1, w1, w2);
+  const float2 nt = __ldg(&t.nu_pair[i1]);
+  if (r > w1 * nt.x + w2 * nt.y) return -1;
+  const float rcs = r * t.inv_N / speed;
+  const float2* cum = t.cum_pair + (size_t)i1 * t.P;
+  int L = 0, R = t.P - 1, chosen = -1;
+  while (L != R) {
+    const int m = (L + R) >> 1;
+    const float2 c2 = __ldg(&cum[m]);
+    const float tvl = w1 * c2.x + w2 * c2.y;
+    if (rcs < tvl) R = m;
+    else if (rcs > tvl) L = m + 1;
+    else { chosen = m; break; }
+  }
+  if (L == R) chosen = L;
+  const float2* sig = t.sig_pair + (size_t)i1 * t.P;
+  while (chosen > 0) {
+    const float2 s2 = __ldg(&sig[chosen]);
+    if (!(w1 * s2.x == 0.0f && w2 * s2.y == 0.0f)) break;
+    --chosen;
+  }
+  return chosen;
+}
+
+// Process choice with thermal targets, gas by gas (BoltzmannMC.C:916-1031):
+// Maxwellian target velocity from three normals (Box-Muller on four
+// uniforms, MathFunctions.C:54-59), 0/1 row weights, per-gas bisection.
+template <class Rng>
+__device__ __forceinline__ int choose_thermal(const TablesF& t, const GasF* gases, int G, float nu_trial, float3 v,
+                                              Rng& rng, float3& tv, float inv_qe) {
+  float n0, n1, n2;
+  {
+    const float r1 = rng.oc(), r2 = rng.oc(), r3 = rng.oc(), r4 = rng.oc();
+    const float a = sqrtf(-2.0f * __logf(r1));
+    float sb, cb;
+    sincosf(kTwoPiF * r2, &sb, &cb);
+    n0 = a * cb;
+    n1 = a * sb;
+    n2 = sqrtf(-2.0f * __logf(r3)) * cosf(kTwoPiF * r4);
+  }
+  const float rcs = nu_trial * rng.oc() * t.inv_N;
+  float prev = 0.0f;
+  int chosen = -1;
+  for (int g = 0; g < G && chosen == -1; ++g) {
+    const GasF gs = gases[g];
+    if (gs.fraction == 0.0f) continue;
+    int L = gs.first, R = gs.last;
+    tv = make_float3(n0 * gs.thermal_sd, n1 * gs.thermal_sd, n2 * gs.thermal_sd);
+    const float rx = v.x - tv.x, ry = v.y - tv.y, rz = v.z - tv.z;
+    const float rs = sqrtf(rx * rx + ry * ry + rz * rz);
+    const float reos = 0.5f * gs.red_mass * rs * rs * inv_qe * t.inv_step;
+    int i1 = (int)fminf(reos, (float)(t.M - 1));
+    const int i2 = min(i1 + 1, t.M - 1);
+    // BoltzmannMC.C:959-967: the weight is 0 or 1
+    const float w1 = ((float)i2 - reos < 0.0f) ? 0.0f : 1.0f;
+    const float w2 = 1.0f - w1;
+    const float2* cum = t.cum_pair + (size_t)i1 * t.P;
+    float ref = 0.0f;
+    if (L > 0) {
+      const float2 c2 = __ldg(&cum[L - 1]);
+      ref = w1 * c2.x + w2 * c2.y;
+    }
+    const float2 cr = __ldg(&cum[R]);
+    const float lim = prev + (w1 * cr.x + w2 * cr.y - ref) * rs;
+    if (rcs > lim) {
+      prev = lim;
+      continue;
+    }
+    while (L != R) {
+      const int m = (L + R) >> 1;
+      const float2 c2 = __ldg(&cum[m]);
+      const float tvl = prev + (w1 * c2.x + w2 * c2.y - ref) * rs;
+      if (rcs < tvl) R = m;
+      else if (rcs > tvl) L = m + 1;
+      else { chosen = m; break; }
+    }
+    if (L == R) chosen = L;
+    const float2* sig = t.sig_pair + (size_t)i1 * t.P;
+    while (chosen > 0) {
+      const float2 s2 = __ldg(&sig[chosen]);
+      if (!(w1 * s2.x == 0.0f && w2 * s2.y == 0.0f)) break;
+      --chosen;
+    }
+  }
+  return chosen;
+}
+
+// One collision event at the end of a free flight (BoltzmannMC.C:907-1113).
+template <class Rng>
+__device__ __forceinline__ void collide(const Consts& c, const TablesF& t, const ProcF* procs, const GasF* gases,
+                                        float nu_trial, float3& v, float& energy, Rng& rng, CollResult& out) {
+  out.chosen = -1;
+  out.dE = 0.0f;
+  out.ionized = 0;
+  const bool thermal = (c.gas_temp == kGasTempTrue) || (c.gas_temp == kGasTempSmart && energy < c.smart_energy);
+  float3 tv = make_float3(0.f, 0.f, 0.f);
+  int ch;
+  if (thermal) {
+    ch = choose_thermal(t, gases, c.G, nu_trial, v, rng, tv, c.inv_qe);
+  } else {
+    const float speed = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    ch = choose_cold(t, nu_trial, energy, speed, rng);
+  }
+  if (ch < 0) return;
+  const ProcF pr = procs[ch];
+  if (!apply_collision(c, pr, thermal, tv, v, energy, rng, out)) return;
+  out.chosen = ch;
+}
+
+}  // namespace lgpu

@@ -1,0 +1,619 @@
+// lgpu_kernels.cu - sm_103a kernels of the electron Monte Carlo path.
+//
+//   k_advance       free flights + collisions of every electron up to the
+//                   synchronisation time (BoltzmannMC.C:617-688, 804-1280)
+//   k_init          Maxwellian start ensemble (BoltzmannMC.C:491-508)
+//   k_build_tables  FP64 interpolated tables -> FP32 row pairs
+//                   (BoltzmannMC.C:561-615)
+//   k_sample        ensemble moments and maximum energy (BoltzmannMC.C:1410-1446)
+//   k_hist          EEDF / EADF / EVDF tallies (BoltzmannMC.C:1550-1571)
+//   k_pop_*         population control after ionization and attachment
+//                   (BoltzmannMC.C:1282-1408)
+//   k_replay_*      the same device functions on given inputs (parity tests)
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
+#include "lgpu_device.cuh"
+#include "lgpu_kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace lgpu {
+
+namespace {
+
+__device__ __forceinline__ void atomic_max_energy(unsigned int* bits, float e) {
+  // energies are >= 0, so the IEEE bit pattern orders like the value
+  atomicMax(bits, __float_as_uint(fmaxf(e, 0.0f)));
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Warp-aggregated append: one atomic per warp for the lanes that call it.
+__device__ __forceinline__ int append_slot(int* counter) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+  base = g.shfl(base, 0);
+  return base + (int)g.thread_rank();
+}
+
+constexpr int kAdvanceThreads = 256;
+
+// ---------------------------------------------------------------- advance
+template <int MODE>
+__global__ void __launch_bounds__(kAdvanceThreads) k_advance(AdvanceArgs a) {
+  __shared__ unsigned int s_count[kMaxProcesses];
+  __shared__ float s_gain[kMaxProcesses];
+  __shared__ float s_loss[kMaxProcesses];
+  __shared__ ProcF s_proc[kMaxProcesses];
+  __shared__ GasF s_gas[kMaxGases];
+  __shared__ double s_red[kAdvanceThreads / 32];
+  __shared__ unsigned long long s_redn[kAdvanceThreads / 32];
+  __shared__ unsigned long long s_redr[kAdvanceThreads / 32];
+
+  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
+    s_count[p] = 0u;
+    s_gain[p] = 0.0f;
+    s_loss[p] = 0.0f;
+    s_proc[p] = a.procs[p];
+  }
+  if (threadIdx.x < a.c.G) s_gas[threadIdx.x] = a.gases[threadIdx.x];
+  __syncthreads();
+
+  FieldF field = a.field;
+  field.mode = MODE;
+  const float T = a.dt_sync;
+  const float nu = a.nu;
+  const float inv_nu = 1.0f / nu;
+  const float hme = a.c.half_me_over_e;
+
+  float gain_sum = 0.0f;
+  unsigned int null_n = 0, real_n = 0;
+  float e_max = 0.0f;
+
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) {
+    const int slot = a.list ? a.list[i] : i;
+    float4 A = a.state[2 * slot];
+    float4 B = a.state[2 * slot + 1];
+    if (B.w == 0.0f) {
+      float3 p = make_float3(A.x - a.shift.x, A.y - a.shift.y, A.z - a.shift.z);
+      float3 v = make_float3(B.x, B.y, B.z);
+      float s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
+      float t = 0.0f;
+      if (a.list) {
+        t = a.pend_t[slot];
+        a.pend_t[slot] = -1.0f;
+      }
+      PhiloxStream rng;
+      rng.init((uint32_t)slot, a.interval, a.seed, a.salt);
+      float energy = energy_of(v, hme);
+      bool dead = false, done = false;
+      for (int guard = 0; guard < (1 << 20); ++guard) {
+        if (s < 0.0f) s = -__logf(rng.oo());
+        const float tau = s * inv_nu;
+        const float phi = a.phi0 + a.phase_rate * t;
+        if (t + tau > T) {
+          // partial flight to the synchronisation time (BoltzmannMC.C:657-663)
+          const float dt = T - t;
+          free_flight(field, phi, dt, p, v);
+          s = fmaxf(s - nu * dt, 0.0f);
+          const float e1 = energy_of(v, hme);
+          gain_sum += e1 - energy;
+          energy = e1;
+          done = true;
+          break;
+        }
+        free_flight(field, phi, tau, p, v);
+        t += tau;
+        {
+          const float e1 = energy_of(v, hme);
+          gain_sum += e1 - energy;
+          energy = e1;
+        }
+        CollResult cr;
+        collide(a.c, a.t, s_proc, s_gas, nu, v, energy, rng, cr);
+        if (cr.chosen < 0) {
+          ++null_n;
+        } else {
+          ++real_n;
+          atomicAdd(&s_count[cr.chosen], 1u);
+          if (cr.dE >= 0.0f) atomicAdd(&s_gain[cr.chosen], cr.dE);
+          else atomicAdd(&s_loss[cr.chosen], cr.dE);
+          const int ptype = s_proc[cr.chosen].type;
+          if (ptype == kIonization) {
+            const int k = append_slot(a.sec_count);
+            if (k < a.sec_cap) {
+              a.sec[2 * k] = make_float4(p.x, p.y, p.z, t);
+              a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, energy_of(cr.ej_v, hme));
+            } else {
+              atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
+            }
+          } else if (ptype == kAttachment) {
+            const int k = append_slot(a.att_count);
+            a.att_list[k] = slot;
+            dead = true;
+            done = true;
+            break;
+          }
+        }
+        s = -__logf(rng.oo());  // next free flight (BoltzmannMC.C:670)
+      }
+      if (!done) atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+      a.state[2 * slot] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
+      a.state[2 * slot + 1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
+      if (!dead) e_max = energy;
+    }
+  }
+
+  // block reductions -> global tallies
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double g = warp_sum((double)gain_sum);
+  unsigned long long nn = warp_sum_u64((unsigned long long)null_n);
+  unsigned long long nr = warp_sum_u64((unsigned long long)real_n);
+  float em = warp_max(e_max);
+  if (lane == 0) {
+    s_red[wid] = g;
+    s_redn[wid] = nn;
+    s_redr[wid] = nr;
+    if (em > 0.0f) atomic_max_energy(a.max_energy_bits, em);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double gs = 0.0;
+    unsigned long long ns = 0, rs = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      gs += s_red[w];
+      ns += s_redn[w];
+      rs += s_redr[w];
+    }
+    if (gs != 0.0) atomicAdd(a.field_gain, gs);
+    if (ns) atomicAdd(a.null_count, ns);
+    if (rs) atomicAdd(a.real_count, rs);
+  }
+  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
+    if (s_count[p]) {
+      atomicAdd(&a.proc_count[p], (unsigned long long)s_count[p]);
+      if (s_gain[p] != 0.0f) atomicAdd(&a.proc_gain[p], (double)s_gain[p]);
+      if (s_loss[p] != 0.0f) atomicAdd(&a.proc_loss[p], (double)s_loss[p]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ init
+__global__ void k_init(InitArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float e = 0.0f;
+  if (i < a.n) {
+    PhiloxStream rng;
+    rng.init((uint32_t)i, 0xFFFFFFFFFFFFull, a.seed, 0x7u);
+    // three normals from four uniforms (Box-Muller, MathFunctions.C:54-59)
+    const float r1 = rng.oc(), r2 = rng.oc(), r3 = rng.oc(), r4 = rng.oc();
+    const float aa = sqrtf(-2.0f * logf(r1));
+    float sb, cb;
+    sincosf(kTwoPiF * r2, &sb, &cb);
+    const float3 v = make_float3(aa * cb * a.sd, aa * sb * a.sd, sqrtf(-2.0f * logf(r3)) * cosf(kTwoPiF * r4) * a.sd);
+    a.state[2 * i] = make_float4(0.f, 0.f, 0.f, -1.0f);
+    a.state[2 * i + 1] = make_float4(v.x, v.y, v.z, 0.0f);
+    e = energy_of(v, a.half_me_over_e);
+  }
+  e = warp_max(e);
+  if ((threadIdx.x & 31) == 0 && e > 0.0f) atomic_max_energy(a.max_energy_bits, e);
+}
+
+// --------------------------------------------------------------- tables
+// Linear interpolation of the raw table (the bracketing index by bisection,
+// largest i with x_i <= x clamped to n-2, then y_i + (x-x_i)/(x_{i+1}-x_i)*(y_{i+1}-y_i)),
+// with explicit round-to-nearest operations so no FMA contraction happens.
+__device__ double interp_raw(const double* xs, const double* ys, int n, double x) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (hi + lo) >> 1;
+    if (xs[mid] > x) hi = mid; else lo = mid;
+  }
+  const double dx = __dsub_rn(xs[lo + 1], xs[lo]);
+  return __dadd_rn(ys[lo], __dmul_rn(__ddiv_rn(__dsub_rn(x, xs[lo]), dx), __dsub_rn(ys[lo + 1], ys[lo])));
+}
+
+__global__ void k_build_tables(TableBuildArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.M) return;
+  const int P = a.P;
+  const double energy = __dmul_rn((double)i, a.step);
+  double cur = 0.0;
+  for (int p = 0; p < P; ++p) {
+    double value = 0.0;
+    if (a.is_super[p]) {
+      if (energy > a.emin[p] && energy <= a.emax[p]) {
+        const double thr = a.emin[p - 1];
+        const double sg = interp_raw(a.raw_e + a.raw_off[p - 1], a.raw_v + a.raw_off[p - 1], a.raw_len[p - 1],
+                                     __dadd_rn(energy, thr));
+        value = __dmul_rn(__dmul_rn(__dmul_rn(a.superw[p], __dadd_rn(1.0, __ddiv_rn(thr, energy))), sg), a.rel_dens[p]);
+      }
+    } else if (energy >= a.emin[p] && energy <= a.emax[p]) {
+      value = __dmul_rn(interp_raw(a.raw_e + a.raw_off[p], a.raw_v + a.raw_off[p], a.raw_len[p], energy), a.rel_dens[p]);
+    }
+    cur = __dadd_rn(cur, value);
+    const size_t k = (size_t)i * P + p;
+    if (a.sig64) a.sig64[k] = value;
+    if (a.cum64) a.cum64[k] = cur;
+    const float vf = (float)value, cf = (float)cur;
+    a.sig_pair[k].x = vf;
+    a.cum_pair[k].x = cf;
+    if (i > 0) {
+      a.sig_pair[k - P].y = vf;
+      a.cum_pair[k - P].y = cf;
+    }
+    if (i == a.M - 1) {
+      a.sig_pair[k].y = vf;
+      a.cum_pair[k].y = cf;
+    }
+  }
+  const double kq = 1.6021766208e-19, km = 9.10938356e-31;
+  const double nu = __dmul_rn(cur, __dmul_rn(a.N, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(energy, 2.0), kq), km))));
+  a.nu_tot[i] = nu;
+  a.nu_pair[i].x = (float)nu;
+  if (i > 0) a.nu_pair[i - 1].y = (float)nu;
+  if (i == a.M - 1) a.nu_pair[i].y = (float)nu;
+}
+
+// running maximum of nu_tot (single block)
+__global__ void k_prefix_max(const double* nu_tot, double* nu_max, int M) {
+  __shared__ double s_part[1024];
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int chunk = (M + nt - 1) / nt;
+  const int b = t * chunk, e = min(M, b + chunk);
+  double m = 0.0;
+  for (int i = b; i < e; ++i) m = fmax(nu_tot[i], m);
+  s_part[t] = m;
+  __syncthreads();
+  if (t == 0) {
+    double run = 0.0;
+    for (int k = 0; k < nt; ++k) {
+      const double v = s_part[k];
+      s_part[k] = run;  // exclusive prefix max
+      run = fmax(run, v);
+    }
+  }
+  __syncthreads();
+  double run = s_part[t];
+  for (int i = b; i < e; ++i) {
+    run = fmax(nu_tot[i], run);
+    nu_max[i] = run;
+  }
+}
+
+// ---------------------------------------------------------------- sample
+constexpr int kSampleThreads = 256;
+
+__global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
+  __shared__ double s_m[kSampleThreads / 32][kMoments];
+  // per-thread partial sums in FP32 (a handful of electrons each), FP64 from
+  // the warp reduction on
+  float m[kMoments];
+#pragma unroll
+  for (int k = 0; k < kMoments; ++k) m[k] = 0.0f;
+  float e_max = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+    const float4 A = a.state[2 * i];
+    const float4 B = a.state[2 * i + 1];
+    const float e = (B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e;
+    e_max = fmaxf(e_max, e);
+    const float x = A.x, y = A.y, z = A.z, vx = B.x, vy = B.y, vz = B.z;
+    m[0] += e;
+    m[1] += x; m[2] += y; m[3] += z;
+    m[4] += vx; m[5] += vy; m[6] += vz;
+    m[7] += x * x; m[8] += x * y; m[9] += x * z; m[10] += y * y; m[11] += y * z; m[12] += z * z;
+    m[13] += x * vx; m[14] += x * vy; m[15] += x * vz;
+    m[16] += y * vx; m[17] += y * vy; m[18] += y * vz;
+    m[19] += z * vx; m[20] += z * vy; m[21] += z * vz;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kMoments; ++k) {
+    const double w = warp_sum((double)m[k]);
+    if (lane == 0) s_m[wid][k] = w;
+  }
+  e_max = warp_max(e_max);
+  if (lane == 0 && e_max > 0.0f) atomic_max_energy(a.max_energy_bits, e_max);
+  __syncthreads();
+  if (threadIdx.x < kMoments) {
+    double s = 0.0;
+    for (int w = 0; w < kSampleThreads / 32; ++w) s += s_m[w][threadIdx.x];
+    atomicAdd(&a.moments[threadIdx.x], s);
+  }
+}
+
+// ------------------------------------------------------------- histograms
+constexpr int kHistThreads = 512;
+constexpr int kMaxEedfCells = 4096;
+
+__global__ void __launch_bounds__(kHistThreads) k_hist(HistArgs a) {
+  __shared__ unsigned int s_h[kMaxEedfCells];
+  for (int c = threadIdx.x; c < a.n_e_cells; c += blockDim.x) s_h[c] = 0u;
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+    const float4 B = a.state[2 * i + 1];
+    const float v2xy = B.x * B.x + B.y * B.y;
+    const float v2 = v2xy + B.z * B.z;
+    const float e = v2 * a.half_me_over_e;
+    // MathFunctions.C:61-81: cell = (x - x0) / step, counted when below the cell count
+    const int c = (int)(e * a.inv_e_step);
+    if (c < a.n_e_cells) atomicAdd(&s_h[c], 1u);
+    if (a.cylindrical) {
+      const float speed = sqrtf(v2);
+      const float cosang = B.z / speed;
+      // MathFunctions.C:106-127
+      const int cx = c;
+      const int cy = (int)((cosang + 1.0f) * (0.5f * (float)a.n_cos));
+      if (cx < a.n_e_cells && cx >= 0 && cy < a.n_cos && cy >= 0) atomicAdd(&a.eadf[(size_t)cx * a.n_cos + cy], 1.0);
+      const float vr = sqrtf(v2xy);
+      const int rx = (int)(vr * a.inv_rad_step);
+      const int ry = (int)((B.z + a.max_speed) * a.inv_ax_step);
+      if (rx < a.n_rad && rx >= 0 && ry < a.n_ax && ry >= 0) atomicAdd(&a.evdf[(size_t)rx * a.n_ax + ry], 1.0);
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < a.n_e_cells; c += blockDim.x) {
+    const unsigned int h = s_h[c];
+    if (h) {
+      atomicAdd(&a.eedf[c], (double)h);
+      if (a.eedf_periodic_row) atomicAdd(&a.eedf_periodic_row[c], (double)h);
+    }
+  }
+}
+
+// ------------------------------------------------------- population control
+__device__ __forceinline__ uint32_t pop_word(uint32_t idx, uint64_t interval, uint64_t seed, uint32_t salt,
+                                             uint32_t draw) {
+  Philox ph;
+  ph.ctr = make_uint4(idx, (uint32_t)interval, (uint32_t)(interval >> 32) ^ (salt << 16), 0x80000000u | draw);
+  ph.key = make_uint2((uint32_t)(seed ^ 0xA5A5A5A5u), (uint32_t)(seed >> 32));
+  return ph.next().x;
+}
+
+// uniform integer in [0, n) from a 32-bit word (n < 2^31)
+__device__ __forceinline__ int uniform_index(uint32_t w, int n) {
+  return (int)(((unsigned long long)w * (unsigned long long)n) >> 32);
+}
+
+// A slot that must still be advanced from time t0 to the synchronisation
+// time. pend_t[slot] holds the start time (NaN or negative: not pending); a
+// slot enters the list once even when it is refilled twice in one round.
+__device__ __forceinline__ void mark_pending(const PopArgs& a, int slot, float t0) {
+  const float old = atomicExch(&a.pend_t[slot], t0);
+  if (!(old >= 0.0f)) {
+    const int k = append_slot(a.pend_count);
+    a.pend_list[k] = slot;
+  }
+}
+
+// (1) attached slots take secondaries, last secondary first (BoltzmannMC.C:1344-1359)
+__global__ void k_pop_fill(PopArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = min(a.n_att, a.n_sec);
+  if (j >= k) return;
+  const int slot = a.att_list[j];
+  const int sidx = a.n_sec - 1 - j;
+  const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
+  a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
+  a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
+  mark_pending(a, slot, S0.w);
+}
+
+// (2) remaining attached slots clone a random surviving electron
+// (BoltzmannMC.C:1360-1376); the energy-growth term gains its energy.
+__global__ void k_pop_clone(PopArgs a) {
+  const int j = a.n_sec + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n_att) return;
+  const int dest = a.att_list[j];
+  int src = -1;
+  for (uint32_t d = 0; d < 4096u; ++d) {
+    const int r = uniform_index(pop_word((uint32_t)j, a.interval, a.seed, a.salt, d), a.n_electrons);
+    if (a.state[2 * r + 1].w == 0.0f) {
+      src = r;
+      break;
+    }
+  }
+  if (src < 0) {
+    atomicExch(a.error_flag, 1);
+    return;
+  }
+  const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
+  a.state[2 * dest] = A;
+  a.state[2 * dest + 1] = B;
+  atomicAdd(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
+  const float t0 = a.pend_t[src];
+  if (t0 >= 0.0f) mark_pending(a, dest, t0);
+}
+
+// (3) excess secondaries: remove a uniformly random subset of size m from the
+// pool of n_electrons slots + m unplaced secondaries, the outcome of the
+// reference's sequential uniform removal (BoltzmannMC.C:1379-1407).
+__global__ void k_pop_claim(PopArgs a) {
+  const int m = a.n_sec - a.n_att;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int pool = a.n_electrons + m;
+  for (uint32_t d = 0; d < 4096u; ++d) {
+    const int r = uniform_index(pop_word((uint32_t)j, a.interval, a.seed, a.salt ^ 0x55u, d), pool);
+    const unsigned int bit = 1u << (r & 31);
+    const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
+    if (!(old & bit)) {
+      a.removed[j] = r;
+      return;
+    }
+  }
+  a.removed[j] = -1;
+  atomicExch(a.error_flag, 1);
+}
+
+__global__ void k_pop_pair(PopArgs a) {
+  const int m = a.n_sec - a.n_att;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int r = a.removed[j];
+  if (r >= 0 && r < a.n_electrons) {
+    const int q = atomicAdd(&a.pair_counts[0], 1);
+    a.pair_slot[q] = r;
+  } else if (r >= a.n_electrons) {
+    // a removed secondary: its energy leaves the ensemble
+    const int sidx = r - a.n_electrons;
+    atomicAdd(a.growth, -(double)a.sec[2 * sidx + 1].w);
+  }
+  // secondary j survives when its pool bit was not claimed
+  const int b = a.n_electrons + j;
+  if (!(a.claim[b >> 5] & (1u << (b & 31)))) {
+    const int q = atomicAdd(&a.pair_counts[1], 1);
+    a.pair_sec[q] = j;
+  }
+}
+
+__global__ void k_pop_place(PopArgs a) {
+  const int m = a.n_sec - a.n_att;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < min(a.pair_counts[0], a.pair_counts[1])) {
+    const int slot = a.pair_slot[q];
+    const int sidx = a.pair_sec[q];
+    const float4 B = a.state[2 * slot + 1];
+    atomicAdd(a.growth, -(double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
+    const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
+    a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
+    a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
+    mark_pending(a, slot, S0.w);
+  }
+}
+
+__global__ void k_pop_unclaim(PopArgs a) {
+  const int m = a.n_sec - a.n_att;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int r = a.removed[j];
+  if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
+}
+
+// --------------------------------------------------------------- replay
+__global__ void k_replay_flight(ReplayFlightArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  float3 p = make_float3((float)a.pos[3 * i], (float)a.pos[3 * i + 1], (float)a.pos[3 * i + 2]);
+  float3 v = make_float3((float)a.vel[3 * i], (float)a.vel[3 * i + 1], (float)a.vel[3 * i + 2]);
+  const float e0 = energy_of(v, a.half_me_over_e);
+  free_flight(a.field, (float)a.phi0[i], (float)a.dt[i], p, v);
+  const float e1 = energy_of(v, a.half_me_over_e);
+  a.pos_out[3 * i] = p.x;
+  a.pos_out[3 * i + 1] = p.y;
+  a.pos_out[3 * i + 2] = p.z;
+  a.vel_out[3 * i] = v.x;
+  a.vel_out[3 * i + 1] = v.y;
+  a.vel_out[3 * i + 2] = v.z;
+  a.energy_out[i] = e1;
+  a.gain_out[i] = e1 - e0;
+}
+
+__global__ void k_replay_collide(ReplayCollArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  ReplayStream rng;
+  rng.u = a.u + (size_t)i * a.u_stride;
+  rng.n = a.u_stride;
+  rng.pos = 0;
+  float3 v = make_float3((float)a.vel[3 * i], (float)a.vel[3 * i + 1], (float)a.vel[3 * i + 2]);
+  float energy = (float)a.energy[i];
+  CollResult cr;
+  cr.ej_v = make_float3(0.f, 0.f, 0.f);
+  collide(a.c, a.t, a.procs, a.gases, (float)a.nu[i], v, energy, rng, cr);
+  double* o = a.out + (size_t)i * 11;
+  o[0] = cr.chosen;
+  o[1] = v.x;
+  o[2] = v.y;
+  o[3] = v.z;
+  o[4] = energy;
+  o[5] = cr.chosen >= 0 ? cr.dE : 0.0;
+  o[6] = cr.chosen >= 0 ? (double)cr.dE / a.energy[i] : 0.0;
+  const bool ion = cr.chosen >= 0 && cr.ionized;
+  o[7] = ion ? cr.ej_v.x : 0.0;
+  o[8] = ion ? cr.ej_v.y : 0.0;
+  o[9] = ion ? cr.ej_v.z : 0.0;
+  o[10] = ion ? (double)energy_of(cr.ej_v, a.c.half_me_over_e) : 0.0;
+  a.used[i] = rng.pos;
+}
+
+inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; }
+
+}  // namespace
+
+void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const int grid = blocks_for(a.n, kAdvanceThreads);
+  switch (a.field.mode) {
+    case kFieldDC: k_advance<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+    case kFieldAC: k_advance<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+    case kFieldB: k_advance<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+    case kFieldECR: k_advance<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+    default: k_advance<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+  }
+}
+
+void launch_init(const InitArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  k_init<<<blocks_for(a.n, 256), 256, 0, s>>>(a);
+}
+
+void launch_build_tables(const TableBuildArgs& a, cudaStream_t s) {
+  k_build_tables<<<blocks_for(a.M, 128), 128, 0, s>>>(a);
+  k_prefix_max<<<1, 1024, 0, s>>>(a.nu_tot, a.nu_max, a.M);
+}
+
+void launch_sample(const SampleArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const int grid = min(blocks_for(a.n, kSampleThreads), 152 * 4);
+  k_sample<<<grid, kSampleThreads, 0, s>>>(a);
+}
+
+void launch_hist(const HistArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const int grid = min(blocks_for(a.n, kHistThreads), 152 * 2);
+  k_hist<<<grid, kHistThreads, 0, s>>>(a);
+}
+
+void launch_pop_control(const PopArgs& a, cudaStream_t s) {
+  const int k = a.n_att < a.n_sec ? a.n_att : a.n_sec;
+  if (k > 0) k_pop_fill<<<blocks_for(k, 128), 128, 0, s>>>(a);
+  if (a.n_att > a.n_sec) k_pop_clone<<<blocks_for(a.n_att - a.n_sec, 128), 128, 0, s>>>(a);
+  const int m = a.n_sec - a.n_att;
+  if (m > 0) {
+    const int g = blocks_for(m, 128);
+    k_pop_claim<<<g, 128, 0, s>>>(a);
+    k_pop_pair<<<g, 128, 0, s>>>(a);
+    k_pop_place<<<g, 128, 0, s>>>(a);
+    k_pop_unclaim<<<g, 128, 0, s>>>(a);
+  }
+}
+
+void launch_replay_flight(const ReplayFlightArgs& a, cudaStream_t s) {
+  if (a.n > 0) k_replay_flight<<<blocks_for(a.n, 128), 128, 0, s>>>(a);
+}
+
+void launch_replay_collide(const ReplayCollArgs& a, cudaStream_t s) {
+  if (a.n > 0) k_replay_collide<<<blocks_for(a.n, 128), 128, 0, s>>>(a);
+}
+
+}  // namespace lgpu

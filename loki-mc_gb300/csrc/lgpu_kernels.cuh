@@ -1,0 +1,173 @@
+// lgpu_kernels.cuh - launch interface of the electron Monte Carlo kernels
+// (implemented in lgpu_kernels.cu, called by the host runtime).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lgpu_types.h"
+
+namespace lgpu {
+
+constexpr int kMaxProcesses = 512;
+constexpr int kMaxGases = 16;
+constexpr int kMoments = 22;  // sum e, r(3), v(3), r r^T (6 unique), r v^T (9)
+
+// Arguments of one advance launch: every listed electron is pushed from its
+// start time to the end of the synchronisation interval, colliding on the way.
+struct AdvanceArgs {
+  float4* state;            // [2*cap]: (x, y, z, s) and (vx, vy, vz, dead flag)
+  int n;                    // electrons to advance (list length when `list` is set)
+  const int* list;          // optional slot list (pending electrons)
+  float* pend_t;            // start time of each pending slot (s, from the interval start); reset on use
+  float dt_sync;            // interval length (s)
+  float phi0;               // phase at the interval start (rad), FP64-reduced on the host
+  float phase_rate;         // w (AC, AC+B) or W (resonance)
+  float nu;                 // trial collision frequency (1/s)
+  uint64_t seed;
+  uint64_t interval;        // synchronisation interval index (RNG counter)
+  uint32_t salt;            // distinguishes the main pass from pending rounds
+  float3 shift;             // origin shift subtracted from every position on load
+  FieldF field;
+  Consts c;
+  TablesF t;
+  const ProcF* procs;
+  const GasF* gases;
+  int P;
+  // outputs
+  float4* sec;              // [2*sec_cap]: (x, y, z, t_c), (vx, vy, vz, energy)
+  int* sec_count;
+  int sec_cap;
+  int* att_list;
+  int* att_count;
+  unsigned long long* proc_count;  // [P]
+  double* proc_gain;               // [P]
+  double* proc_loss;               // [P]
+  unsigned long long* null_count;
+  unsigned long long* real_count;
+  double* field_gain;
+  unsigned int* max_energy_bits;   // float bits of the largest final energy
+  int* error_flag;                 // 2: secondary buffer full, 3: collision budget exhausted
+};
+
+void launch_advance(const AdvanceArgs& a, cudaStream_t s);
+
+struct InitArgs {
+  float4* state;
+  int n;
+  float sd;                 // sqrt(k T_e / m)
+  uint64_t seed;
+  float half_me_over_e;
+  unsigned int* max_energy_bits;
+};
+void launch_init(const InitArgs& a, cudaStream_t s);
+
+// Table build on the device in FP64 (BoltzmannMC.C:561-615).
+struct TableBuildArgs {
+  int M, P;
+  double step, N;
+  const int* is_super;
+  const double* superw;
+  const double* emin;
+  const double* emax;
+  const double* rel_dens;
+  const int* raw_off;
+  const int* raw_len;
+  const double* raw_e;
+  const double* raw_v;
+  float2* nu_pair;
+  float2* cum_pair;
+  float2* sig_pair;
+  double* nu_tot;     // FP64 total frequency per row
+  double* nu_max;     // FP64 running maximum
+  double* sig64;      // optional FP64 sigma*n [M*P] (tests), may be null
+  double* cum64;      // optional FP64 cumulative [M*P] (tests), may be null
+};
+void launch_build_tables(const TableBuildArgs& a, cudaStream_t s);
+
+// Ensemble sample: moment sums (FP64) and the largest energy.
+struct SampleArgs {
+  const float4* state;
+  int n;
+  float half_me_over_e;
+  double* moments;                 // [kMoments], accumulated (zeroed by the caller)
+  unsigned int* max_energy_bits;
+};
+void launch_sample(const SampleArgs& a, cudaStream_t s);
+
+// Distribution tallies of one sample (BoltzmannMC.C:1550-1571).
+struct HistArgs {
+  const float4* state;
+  int n;
+  float half_me_over_e;
+  int n_e_cells;
+  float inv_e_step;                // 1 / EEDF energy step
+  double* eedf;                    // [n_e_cells]
+  double* eedf_periodic_row;       // [n_e_cells] or null
+  int cylindrical;
+  int n_cos;                       // EADF: [n_e_cells x n_cos]
+  double* eadf;
+  int n_rad, n_ax;                 // EVDF: [n_rad x n_ax]
+  float inv_rad_step, inv_ax_step, max_speed;
+  double* evdf;
+};
+void launch_hist(const HistArgs& a, cudaStream_t s);
+
+// Population control (BoltzmannMC.C:1282-1408), in parallel.
+struct PopArgs {
+  float4* state;
+  int n_electrons;
+  float4* sec;                     // secondaries (x, y, z, t_c), (vx, vy, vz, energy)
+  int n_sec;
+  const int* att_list;
+  int n_att;
+  float* pend_t;                   // [cap] start time of pending slots (<0: not pending)
+  int* pend_list;                  // pending slot list
+  int* pend_count;
+  unsigned int* claim;             // bitmap over n_electrons + n_sec, all zero on entry and on exit
+  int* removed;                    // [n_sec] scratch
+  int* pair_slot;                  // [n_sec] scratch
+  int* pair_sec;                   // [n_sec] scratch
+  int* pair_counts;                // [2] scratch counters (zeroed by the caller)
+  double* growth;                  // energy growth accumulator (eV)
+  float half_me_over_e;
+  uint64_t seed, interval;
+  uint32_t salt;
+  int* error_flag;                 // set when a bounded retry loop gives up
+};
+void launch_pop_control(const PopArgs& a, cudaStream_t s);
+
+// Replay kernels for the parity tests: the production device functions
+// driven by given inputs and recorded uniforms.
+struct ReplayFlightArgs {
+  int n;
+  const double* phi0;     // phase at flight start (rad, already reduced)
+  const double* dt;
+  const double* pos;      // [n*3]
+  const double* vel;      // [n*3]
+  double* pos_out;
+  double* vel_out;
+  double* energy_out;
+  double* gain_out;
+  FieldF field;
+  float half_me_over_e;
+};
+void launch_replay_flight(const ReplayFlightArgs& a, cudaStream_t s);
+
+struct ReplayCollArgs {
+  int n;
+  const double* nu;
+  const double* vel;      // [n*3]
+  const double* energy;
+  const double* u;        // [n*u_stride]
+  int u_stride;
+  double* out;            // [n*11]: chosen, v(3), energy, dE, dE/E, ej v(3), ej energy
+  int* used;
+  Consts c;
+  TablesF t;
+  const ProcF* procs;
+  const GasF* gases;
+};
+void launch_replay_collide(const ReplayCollArgs& a, cudaStream_t s);
+
+}  // namespace lgpu

@@ -1,0 +1,288 @@
+"""ctypes binding of the C ABI in include/loki_gpu.h (libloki_gpu.so).
+
+Only plain C types cross the boundary. A missing library or a failing call
+raises; there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+LIB_NAME = "libloki_gpu.so"
+
+D = ctypes.c_double
+I = ctypes.c_int
+LL = ctypes.c_longlong
+U64 = ctypes.c_uint64
+P_ = ctypes.POINTER
+
+LGPU_OK = 0
+STATUS = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ENERGY_ABOVE_TABLE", 4: "TIMEOUT", 5: "CUDA_ERROR", 6: "STATE",
+          7: "OVERFLOW", 8: "NO_DEVICE"}
+
+EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_stream",
+            "lgpu_set_processes", "lgpu_set_conditions", "lgpu_init_ensemble", "lgpu_advance", "lgpu_solve",
+            "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_series", "lgpu_get_timing",
+            "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions")
+
+
+class LokiGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", I), ("seed", U64), ("n_electrons", D), ("n_interp", I), ("gas_temperature_effect", I),
+                ("sharing", I), ("init_temp_ratio", D), ("min_coll_before_ss", D), ("max_coll_before_ss", D),
+                ("max_coll_after_ss", D), ("req_integration_points", D), ("req_ss_times", D), ("req_abs_time", D),
+                ("errors_checked", I), ("req_err_mean_energy", D), ("req_err_flux_v", D), ("req_err_flux_d", D),
+                ("req_err_bulk_v", D), ("req_err_bulk_d", D), ("req_err_power", D), ("n_energy_cells", I),
+                ("n_cos_cells", I), ("n_radial_cells", I), ("n_axial_cells", I), ("n_phases", I), ("sync_x", D),
+                ("sync_oversampling", I), ("max_seconds", D), ("max_sync_steps", LL)]
+
+
+class Process(ctypes.Structure):
+    _fields_ = [("type", I), ("is_super", I), ("is_elastic", I), ("sampler", I), ("sampler_p0", D),
+                ("sampler_p1", D), ("superw", D), ("emin", D), ("emax", D), ("rel_dens", D), ("mass", D),
+                ("eloss", D), ("wparam", D), ("raw_len", I), ("raw_e", P_(D)), ("raw_v", P_(D))]
+
+
+class Gas(ctypes.Structure):
+    _fields_ = [("first", I), ("last", I), ("fraction", D)]
+
+
+class Conditions(ctypes.Structure):
+    _fields_ = [("gas_density", D), ("gas_temperature", D), ("reduced_field_td", D), ("field_angle_deg", D),
+                ("excitation_freq_hz", D), ("reduced_mag_field_hx", D)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("mean_energy", D), ("mean_energy_err", D), ("flux_v", D * 3), ("flux_v_err", D * 3),
+                ("flux_d", D * 9), ("flux_d_err", D * 9), ("bulk_v", D * 3), ("bulk_v_err", D * 3),
+                ("bulk_d", D * 9), ("bulk_d_err", D * 9), ("power_field", D), ("power_growth", D),
+                ("power_balance_rel_err", D), ("ss_time", D), ("final_time", D), ("trial_freq", D),
+                ("max_eedf_energy", D), ("real_collisions", D), ("null_collisions", D), ("coll_at_ss", D),
+                ("null_at_ss", D), ("integration_points", LL), ("sampling_points", LL),
+                ("first_integration_index", LL), ("sync_steps", LL), ("elapsed", D), ("capped", I)]
+
+
+class StepReport(ctypes.Structure):
+    _fields_ = [("time", D), ("trial_freq", D), ("max_energy", D), ("mean_energy", D), ("real_collisions", D),
+                ("null_collisions", D), ("sync_steps", LL)]
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("advance_ms", D), ("advance_launches", LL), ("electron_steps", D), ("kernel_launches", LL),
+                ("h2d_bytes", D), ("d2h_bytes", D)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return os.path.join(PKG_DIR, LIB_NAME)
+
+
+def load(path: str | None = None):
+    """Loads libloki_gpu.so (built by ``lokigpu.build``); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise LokiGpuError(8, f"{p} is missing: build it with __graft_entry__.build() or lokigpu.build.build()")
+    lib = ctypes.CDLL(p)
+    lib.lgpu_config_default.argtypes = [P_(Config)]
+    lib.lgpu_config_default.restype = None
+    lib.lgpu_create.argtypes = [P_(Config), P_(ctypes.c_void_p)]
+    lib.lgpu_destroy.argtypes = [ctypes.c_void_p]
+    lib.lgpu_last_error.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+    lib.lgpu_stream.argtypes = [ctypes.c_void_p]
+    lib.lgpu_stream.restype = ctypes.c_void_p
+    lib.lgpu_set_processes.argtypes = [ctypes.c_void_p, P_(Process), I, P_(Gas), I, D]
+    lib.lgpu_set_conditions.argtypes = [ctypes.c_void_p, P_(Conditions)]
+    lib.lgpu_init_ensemble.argtypes = [ctypes.c_void_p]
+    lib.lgpu_advance.argtypes = [ctypes.c_void_p, I, P_(StepReport)]
+    lib.lgpu_solve.argtypes = [ctypes.c_void_p, P_(Result)]
+    lib.lgpu_get_process_results.argtypes = [ctypes.c_void_p, P_(ctypes.c_ulonglong), P_(D), P_(D), P_(D), I]
+    lib.lgpu_get_distributions.argtypes = [ctypes.c_void_p] + [P_(D)] * 9
+    lib.lgpu_get_series.argtypes = [ctypes.c_void_p, I, P_(D), LL]
+    lib.lgpu_get_series.restype = LL
+    lib.lgpu_get_timing.argtypes = [ctypes.c_void_p, P_(Timing)]
+    lib.lgpu_build_tables.argtypes = [ctypes.c_void_p, D, P_(D), P_(D), P_(ctypes.c_float), P_(ctypes.c_float)]
+    lib.lgpu_set_field_raw.argtypes = [ctypes.c_void_p, P_(D), D, D, D]
+    lib.lgpu_replay_flights.argtypes = [ctypes.c_void_p, I] + [P_(D)] * 8
+    lib.lgpu_replay_collisions.argtypes = [ctypes.c_void_p, I, P_(D), P_(D), P_(D), P_(D), I, P_(D), P_(I)]
+    _lib = lib
+    return lib
+
+
+def dptr(a):
+    return None if a is None else a.ctypes.data_as(P_(D))
+
+
+def default_config(**kw) -> Config:
+    c = Config()
+    load().lgpu_config_default(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Context:
+    """Owns one lgpu_ctx (one swarm condition)."""
+
+    def __init__(self, cfg: Config):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        rc = self.lib.lgpu_create(ctypes.byref(cfg), ctypes.byref(self.h))
+        self.cfg = cfg
+        self._keep = []
+        self.check(rc)
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        self.lib.lgpu_last_error(self.h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def check(self, rc):
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+
+    def close(self):
+        if self.h:
+            self.lib.lgpu_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_processes(self, ps, gas_first, gas_last, gas_fraction):
+        """ps: a ProcessSet-like object (see synth.ProcessSet)."""
+        n = ps.n
+        arr = (Process * n)()
+        keep = []
+        for p in range(n):
+            q = arr[p]
+            q.type = int(ps.ptype[p])
+            q.is_super = int(ps.is_super[p])
+            q.is_elastic = int(ps.is_elastic[p])
+            q.sampler = int(ps.sampler[p])
+            q.sampler_p0 = float(ps.sampler_p0[p])
+            q.sampler_p1 = float(ps.sampler_p1[p])
+            q.superw = float(ps.superw[p])
+            q.emin = float(ps.emin[p])
+            q.emax = float(ps.emax[p])
+            q.rel_dens = float(ps.rel_dens[p])
+            q.mass = float(ps.mass[p])
+            q.eloss = float(ps.eloss[p])
+            q.wparam = float(ps.wparam[p])
+            e = np.ascontiguousarray(ps.raw_e[p], dtype=np.float64)
+            v = np.ascontiguousarray(ps.raw_v[p], dtype=np.float64)
+            keep += [e, v]
+            q.raw_len = len(e) if not ps.is_super[p] else 0
+            q.raw_e = dptr(e)
+            q.raw_v = dptr(v)
+        G = len(gas_first)
+        gs = (Gas * G)()
+        for g in range(G):
+            gs[g].first = int(gas_first[g])
+            gs[g].last = int(gas_last[g])
+            gs[g].fraction = float(gas_fraction[g])
+        self.check(self.lib.lgpu_set_processes(self.h, arr, n, gs, G, float(ps.energy_max_elastic)))
+        self.P = n
+
+    def set_conditions(self, N, Tg=300.0, red_field=0.0, angle=180.0, freq_hz=0.0, red_mag=0.0):
+        c = Conditions(N, Tg, red_field, angle, freq_hz, red_mag)
+        self.check(self.lib.lgpu_set_conditions(self.h, ctypes.byref(c)))
+
+    def init_ensemble(self):
+        self.check(self.lib.lgpu_init_ensemble(self.h))
+
+    def advance(self, n):
+        r = StepReport()
+        self.check(self.lib.lgpu_advance(self.h, int(n), ctypes.byref(r)))
+        return r
+
+    def solve(self) -> Result:
+        r = Result()
+        self.check(self.lib.lgpu_solve(self.h, ctypes.byref(r)))
+        return r
+
+    def process_results(self):
+        P = self.P
+        cnt = (ctypes.c_ulonglong * P)()
+        rate, gain, loss = np.zeros(P), np.zeros(P), np.zeros(P)
+        self.check(self.lib.lgpu_get_process_results(self.h, cnt, dptr(rate), dptr(gain), dptr(loss), P))
+        return np.array(cnt[:], dtype=np.uint64), rate, gain, loss
+
+    def distributions(self):
+        c = self.cfg
+        nEC, nCos, nR, nA, nPh = c.n_energy_cells, c.n_cos_cells, c.n_radial_cells, c.n_axial_cells, c.n_phases
+        out = dict(eedf_cells=np.zeros(nEC), eedf=np.zeros(nEC), efadf=np.zeros(nEC), esadf=np.zeros(nEC),
+                   eadf=np.zeros((nEC, nCos)), evdf=np.zeros((nR, nA)), radial_cells=np.zeros(nR),
+                   axial_cells=np.zeros(nA), eedf_periodic=np.zeros((nPh, nEC)))
+        self.check(self.lib.lgpu_get_distributions(self.h, *[dptr(out[k]) for k in (
+            "eedf_cells", "eedf", "efadf", "esadf", "eadf", "evdf", "radial_cells", "axial_cells", "eedf_periodic")]))
+        return out
+
+    def series(self, which, width):
+        n = self.lib.lgpu_get_series(self.h, which, None, 0)
+        rows = self.lib.lgpu_get_series(self.h, which, None, 1 << 40)
+        out = np.zeros(rows * width)
+        got = self.lib.lgpu_get_series(self.h, which, dptr(out), rows)
+        if got < 0:
+            self.check(-got)
+        del n
+        return out.reshape(rows, width) if width > 1 else out
+
+    def timing(self) -> Timing:
+        t = Timing()
+        self.check(self.lib.lgpu_get_timing(self.h, ctypes.byref(t)))
+        return t
+
+    def stream(self) -> int:
+        return self.lib.lgpu_stream(self.h) or 0
+
+    def build_tables(self, max_energy, M, P):
+        nu_tot, nu_max = np.zeros(M), np.zeros(M)
+        sig = np.zeros(M * P, np.float32)
+        cum = np.zeros(M * P, np.float32)
+        self.check(self.lib.lgpu_build_tables(self.h, float(max_energy), dptr(nu_tot), dptr(nu_max),
+                                              sig.ctypes.data_as(P_(ctypes.c_float)),
+                                              cum.ctypes.data_as(P_(ctypes.c_float))))
+        return nu_tot, nu_max, sig, cum
+
+    def set_field_raw(self, E, freq_hz, red_mag, cyclotron):
+        e = np.ascontiguousarray(E, dtype=np.float64)
+        self.check(self.lib.lgpu_set_field_raw(self.h, dptr(e), float(freq_hz), float(red_mag), float(cyclotron)))
+
+    def replay_flights(self, t, dt, pos, vel):
+        n = len(t)
+        t = np.ascontiguousarray(t, np.float64)
+        dt = np.ascontiguousarray(dt, np.float64)
+        pos = np.ascontiguousarray(pos, np.float64).reshape(n, 3)
+        vel = np.ascontiguousarray(vel, np.float64).reshape(n, 3)
+        po, vo, eo, go = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n), np.zeros(n)
+        self.check(self.lib.lgpu_replay_flights(self.h, n, dptr(t), dptr(dt), dptr(pos), dptr(vel), dptr(po),
+                                                dptr(vo), dptr(eo), dptr(go)))
+        return po, vo, eo, go
+
+    def replay_collisions(self, nu, vel, energy, uniforms):
+        n = len(nu)
+        nu = np.ascontiguousarray(nu, np.float64)
+        vel = np.ascontiguousarray(vel, np.float64).reshape(n, 3)
+        energy = np.ascontiguousarray(energy, np.float64)
+        u = np.ascontiguousarray(uniforms, np.float64).reshape(n, -1)
+        out = np.zeros((n, 11))
+        used = np.zeros(n, np.int32)
+        self.check(self.lib.lgpu_replay_collisions(self.h, n, dptr(nu), dptr(vel), dptr(energy), dptr(u), u.shape[1],
+                                                   dptr(out), used.ctypes.data_as(P_(I))))
+        return out, used

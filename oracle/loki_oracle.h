@@ -131,6 +131,7 @@ typedef struct lo_run_config {
   int cylindrical;                 /* angle == 180 */
   double max_seconds;              /* wall-clock cap (<=0: none); used to bound baseline samples */
   long long max_sync_steps;        /* cap on synchronisation intervals (<=0: none) */
+  long long mark_sync_step;        /* record collisions and wall time after this many intervals (<=0: none) */
 } lo_run_config;
 
 typedef struct lo_run_result {
@@ -145,6 +146,7 @@ typedef struct lo_run_result {
   double max_eedf_energy;
   double elapsed;
   long long sync_steps;
+  double mark_real_collisions, mark_null_collisions, mark_elapsed;
   int status;                      /* 0 ok, 1 energy above elastic table, 2 capped by time/steps */
 } lo_run_result;
 

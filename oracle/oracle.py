@@ -59,7 +59,8 @@ class RunConfig(ctypes.Structure):
                 ("errors_checked", I), ("req_err_energy", D), ("req_err_flux_v", D), ("req_err_flux_d", D),
                 ("req_err_bulk_v", D), ("req_err_bulk_d", D), ("req_err_power", D), ("n_energy_cells", I),
                 ("n_cos_cells", I), ("n_radial_cells", I), ("n_axial_cells", I), ("n_phases", I),
-                ("cylindrical", I), ("max_seconds", D), ("max_sync_steps", ctypes.c_longlong)]
+                ("cylindrical", I), ("max_seconds", D), ("max_sync_steps", ctypes.c_longlong),
+                ("mark_sync_step", ctypes.c_longlong)]
 
 
 class RunResult(ctypes.Structure):
@@ -69,7 +70,8 @@ class RunResult(ctypes.Structure):
                 ("coll_at_ss", D), ("null_at_ss", D), ("ss_time", D), ("final_time", D),
                 ("integration_points", D), ("trial_freq", D), ("power_field", D), ("power_growth", D),
                 ("power_balance_rel_err", D), ("max_eedf_energy", D), ("elapsed", D),
-                ("sync_steps", ctypes.c_longlong), ("status", I)]
+                ("sync_steps", ctypes.c_longlong), ("mark_real_collisions", D), ("mark_null_collisions", D),
+                ("mark_elapsed", D), ("status", I)]
 
 
 _lib = None
@@ -199,6 +201,7 @@ def default_run_config(n_electrons, **kw) -> RunConfig:
     c.cylindrical = 1
     c.max_seconds = 0
     c.max_sync_steps = 0
+    c.mark_sync_step = 0
     for k, v in kw.items():
         setattr(c, k, v)
     return c
