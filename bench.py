@@ -65,7 +65,7 @@ class ClockSampler:
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
@@ -189,6 +189,8 @@ def run_gpu_arm(args):
         ctx.set_conditions(N_GAS, T_GAS, E_N)
         return ctx
 
+    clocks = ClockSampler(local)
+    clocks.start()                         # sampled over the relaxation and the timed steps
     ctx = make_ctx(1000 + rank)
     ctx.init_ensemble()
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
@@ -201,8 +203,6 @@ def run_gpu_arm(args):
 
     r0 = ctx.advance(0)
     t0 = ctx.timing()
-    clocks = ClockSampler(local)
-    clocks.start()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -297,7 +297,7 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--electrons", type=int, default=N_ELECTRONS)

@@ -239,34 +239,47 @@ __device__ __forceinline__ float3 euler(float sChi, float cChi, float sEta, floa
   return make_float3(-sCsE * s.sP + aux * s.cP, sCsE * s.cP + aux * s.sP, -sChi * cEta * s.sT + cChi * s.cT);
 }
 
-// cos(chi) samplers (AngularScatteringFunctions.h:27-74).
+// cos(chi) samplers (AngularScatteringFunctions.h:27-74). Each returns
+// (cos chi, 1 - cos chi) with the second term formed without cancellation, so
+// that sin chi = sqrt((1-c)(1+c)) keeps FP32 accuracy for forward scattering.
 template <class Rng>
-__device__ __forceinline__ float sample_cos_chi(const ProcF& pr, float energy, float energy_after, Rng& rng) {
+__device__ __forceinline__ float2 sample_cos_chi(const ProcF& pr, float energy, float energy_after, Rng& rng) {
   switch (pr.sampler) {
     case kSamplerForward:
-      return 1.0f;
+      return make_float2(1.0f, 0.0f);
     case kSamplerBornDipole: {
-      // Vialetto 2021, eq. 25
+      // Vialetto 2021, eq. 25: 1 + 2 r2/(1-r2) (1 - r2^-U)
       const float s = sqrtf(energy_after) + sqrtf(energy);
       const float ratio = pr.eloss / (s * s);
       const float r2 = ratio * ratio;
-      return 1.0f + 2.0f * r2 / (1.0f - r2) * (1.0f - powf(r2, -rng.cc()));
+      const float u = rng.cc();
+      const float om = 2.0f * r2 / (1.0f - r2) * expm1f(-u * logf(r2));  // 1 - cos
+      return make_float2(1.0f - om, om);
     }
     case kSamplerSurendra: {
-      // Vahedi 1995, eq. 9: (2 + e - 2 (1+e)^U) / e, written with expm1/log1p
+      // Vahedi 1995, eq. 9: (2 + e - 2 (1+e)^U) / e ; 1 - cos = 2((1+e)^U - 1)/e
       const float u = rng.cc();
-      return (energy - 2.0f * expm1f(u * log1pf(energy))) / energy;
+      const float om = 2.0f * expm1f(u * log1pf(energy)) / energy;
+      return make_float2(1.0f - om, om);
     }
     case kSamplerCoulombScreen: {
-      // Hagelaar 2000, eqs. 21-23
+      // Hagelaar 2000, eqs. 21-23: (sp + 1 - (2 sp + 1) R) / (sp + 1 - R); 1 - cos = 2 sp R / (sp + 1 - R)
       const float eps = (pr.sp0 == 0.0f) ? energy : energy_after;
       const float sp = pr.sp1 / eps;
       const float R = rng.cc();
-      return (sp + 1.0f - (2.0f * sp + 1.0f) * R) / (sp + 1.0f - R);
+      const float den = sp + 1.0f - R;
+      const float om = 2.0f * sp * R / den;
+      return make_float2((sp + 1.0f - (2.0f * sp + 1.0f) * R) / den, om);
     }
-    default:  // isotropic
-      return 1.0f - 2.0f * rng.cc();
+    default: {  // isotropic: 1 - 2U
+      const float u = rng.cc();
+      return make_float2(1.0f - 2.0f * u, 2.0f * u);
+    }
   }
+}
+
+__device__ __forceinline__ float sin_from(float2 c) {
+  return sqrtf(fmaxf(0.0f, c.y * (2.0f - c.y)));
 }
 
 // Result of one collision event.
@@ -297,8 +310,8 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
       const float relE = 0.5f * pr.red_mass * s.speed * s.speed * c.inv_qe;
       const float relEA = relE - pr.eloss;
       if (relEA <= 0.0f) return false;
-      const float cChi = sample_cos_chi(pr, relE, relEA, rng);
-      const float sChi = sqrtf(fmaxf(0.0f, 1.0f - cChi * cChi));
+      const float2 cc = sample_cos_chi(pr, relE, relEA, rng);
+      const float cChi = cc.x, sChi = sin_from(cc);
       float sEta, cEta;
       sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
       const float3 ver = euler(sChi, cChi, sEta, cEta, s);
@@ -313,13 +326,13 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
       const Sph s = cart2sph(v);
       const float eA = incident - pr.eloss;
       if (eA <= 0.0f) return false;
-      const float cChi = sample_cos_chi(pr, incident, eA, rng);
-      const float sChi = sqrtf(fmaxf(0.0f, 1.0f - cChi * cChi));
+      const float2 cc = sample_cos_chi(pr, incident, eA, rng);
+      const float cChi = cc.x, sChi = sin_from(cc);
       float sEta, cEta;
       sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
       const float3 ver = euler(sChi, cChi, sEta, cEta, s);
       const float sp = sqrtf(fmaxf(0.0f, (s.speed * s.speed - c.two_qe_over_me * pr.eloss) *
-                                             (1.0f - pr.mass_factor * (1.0f - cChi))));
+                                             (1.0f - pr.mass_factor * cc.y)));
       v = make_float3(sp * ver.x, sp * ver.y, sp * ver.z);
     }
     energy = energy_of(v, c.half_me_over_e);
@@ -345,18 +358,20 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
     float cChiS, sChiS, cChiE, sChiE, sEtaS, cEtaS, sEtaE, cEtaE;
     if (pr.sampler == kSamplerMomentumConservation) {
       cChiS = sqrtf(scat / net);
-      sChiS = sqrtf(fmaxf(0.0f, 1.0f - cChiS * cChiS));
+      sChiS = sqrtf(ej / net);  // sqrt(1 - cos^2) with cos^2 = scat/net
       sincosf(kTwoPiF * rng.oc(), &sEtaS, &cEtaS);
       cChiE = sqrtf(ej / net);
-      sChiE = sqrtf(fmaxf(0.0f, 1.0f - cChiE * cChiE));
+      sChiE = sqrtf(scat / net);
       sEtaE = -sEtaS;
       cEtaE = -cEtaS;
     } else {
-      cChiS = sample_cos_chi(pr, incident, scat, rng);
-      sChiS = sqrtf(fmaxf(0.0f, 1.0f - cChiS * cChiS));
+      const float2 cs = sample_cos_chi(pr, incident, scat, rng);
+      cChiS = cs.x;
+      sChiS = sin_from(cs);
       sincosf(kTwoPiF * rng.oc(), &sEtaS, &cEtaS);
-      cChiE = sample_cos_chi(pr, incident, ej, rng);
-      sChiE = sqrtf(fmaxf(0.0f, 1.0f - cChiE * cChiE));
+      const float2 ce = sample_cos_chi(pr, incident, ej, rng);
+      cChiE = ce.x;
+      sChiE = sin_from(ce);
       sincosf(kTwoPiF * rng.oc(), &sEtaE, &cEtaE);
     }
     const float3 vs = euler(sChiS, cChiS, sEtaS, cEtaS, s);
