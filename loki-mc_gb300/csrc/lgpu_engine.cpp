@@ -48,7 +48,7 @@ struct DevScalars {
   int sec_count, att_count, pend_count, error_flag;
   int pair_counts[2];
   unsigned int max_energy_bits;
-  int pad;
+  int work_counter;
   unsigned long long null_count;
   unsigned long long real_count;
   double field_gain;
@@ -122,6 +122,7 @@ class Engine {
     if (cfg_.n_energy_cells < 1 || cfg_.n_energy_cells > 4096) return fail(LGPU_ERR_BAD_ARG, "nEnergyCells must be 1..4096");
     if (cfg_.sync_oversampling < 1) return fail(LGPU_ERR_BAD_ARG, "synchronizationOverSampling must be >= 1");
     LGPU_CU(cudaSetDevice(cfg_.device));
+    LGPU_CU(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, cfg_.device));
     LGPU_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     LGPU_CU(cudaEventCreate(&ev0_));
     LGPU_CU(cudaEventCreate(&ev1_));
@@ -573,6 +574,8 @@ class Engine {
     a.field_gain = &d_sc_->field_gain;
     a.max_energy_bits = &d_sc_->max_energy_bits;
     a.error_flag = &d_sc_->error_flag;
+    a.work_counter = &d_sc_->work_counter;
+    a.sm_count = sm_count_;
     LGPU_CU(cudaEventRecord(ev0_, stream_));
     launch_advance(a, stream_);
     LGPU_CU(cudaEventRecord(ev1_, stream_));
@@ -626,6 +629,7 @@ class Engine {
       const int npend = h_sc_->pend_count;
       LGPU_CU(cudaMemsetAsync(&d_sc_->sec_count, 0, 2 * sizeof(int), stream_));
       if (npend > 0) {
+        LGPU_CU(cudaMemsetAsync(&d_sc_->work_counter, 0, sizeof(int), stream_));
         AdvanceArgs b = a;
         b.n = npend;
         b.list = d_pend_list_;
@@ -1246,7 +1250,7 @@ class Engine {
   }
 
   // ------------------------------------------------------------ state
-  int N_ = 0, P_ = 0, M_ = 0, sec_cap_ = 0;
+  int N_ = 0, P_ = 0, M_ = 0, sec_cap_ = 0, sm_count_ = 1;
   size_t claim_words_ = 0;
   std::vector<lgpu_process> procs_;
   std::vector<lgpu_gas> gases_;

@@ -55,10 +55,19 @@ __device__ __forceinline__ int append_slot(int* counter) {
 }
 
 constexpr int kAdvanceThreads = 256;
+constexpr int kAdvanceBlocksPerSM = 4;
+constexpr int kChunk = 128;  // electrons a warp takes from the global work counter at a time
 
 // ---------------------------------------------------------------- advance
+// Every electron is flown and collided until the synchronisation time
+// (BoltzmannMC.C:617-688). Work distribution: a persistent grid; each warp
+// takes chunks of electrons from a global counter and every lane holds one
+// electron. A lane whose electron reaches the synchronisation time (or is
+// attached) writes it back and takes the next electron of the warp's chunk,
+// so the lanes of a warp stay busy although the number of collisions per
+// electron and interval is random (Poisson-distributed).
 template <int MODE>
-__global__ void __launch_bounds__(kAdvanceThreads) k_advance(AdvanceArgs a) {
+__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance(AdvanceArgs a) {
   __shared__ unsigned int s_count[kMaxProcesses];
   __shared__ float s_gain[kMaxProcesses];
   __shared__ float s_loss[kMaxProcesses];
@@ -83,88 +92,136 @@ __global__ void __launch_bounds__(kAdvanceThreads) k_advance(AdvanceArgs a) {
   const float nu = a.nu;
   const float inv_nu = 1.0f / nu;
   const float hme = a.c.half_me_over_e;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
 
   float gain_sum = 0.0f;
   unsigned int null_n = 0, real_n = 0;
   float e_max = 0.0f;
 
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n) {
-    const int slot = a.list ? a.list[i] : i;
-    float4 A = a.state[2 * slot];
-    float4 B = a.state[2 * slot + 1];
-    if (B.w == 0.0f) {
-      float3 p = make_float3(A.x - a.shift.x, A.y - a.shift.y, A.z - a.shift.z);
-      float3 v = make_float3(B.x, B.y, B.z);
-      float s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
-      float t = 0.0f;
-      if (a.list) {
-        t = a.pend_t[slot];
-        a.pend_t[slot] = -1.0f;
-      }
-      PhiloxStream rng;
-      rng.init((uint32_t)slot, a.interval, a.seed, a.salt);
-      float energy = energy_of(v, hme);
-      bool dead = false, done = false;
-      for (int guard = 0; guard < (1 << 20); ++guard) {
-        if (s < 0.0f) s = -__logf(rng.oo());
-        const float tau = s * inv_nu;
-        const float phi = a.phi0 + a.phase_rate * t;
-        if (t + tau > T) {
-          // partial flight to the synchronisation time (BoltzmannMC.C:657-663)
-          const float dt = T - t;
-          free_flight(field, phi, dt, p, v);
-          s = fmaxf(s - nu * dt, 0.0f);
-          const float e1 = energy_of(v, hme);
-          gain_sum += e1 - energy;
-          energy = e1;
-          done = true;
-          break;
-        }
-        free_flight(field, phi, tau, p, v);
-        t += tau;
-        {
-          const float e1 = energy_of(v, hme);
-          gain_sum += e1 - energy;
-          energy = e1;
-        }
-        CollResult cr;
-        collide(a.c, a.t, s_proc, s_gas, nu, v, energy, rng, cr);
-        if (cr.chosen < 0) {
-          ++null_n;
+  // warp-uniform chunk cursor
+  int next = 0, end = 0;
+  bool exhausted = false;
+  // per-lane electron
+  bool have = false;
+  int slot = 0;
+  float3 p = make_float3(0.f, 0.f, 0.f), v = make_float3(0.f, 0.f, 0.f);
+  float s = -1.0f, t = 0.0f, energy = 0.0f;
+  int events = 0;
+  PhiloxStream rng;
+
+  for (;;) {
+    // ---- refill lanes without an electron from the warp's chunk
+    const unsigned need = __ballot_sync(0xffffffffu, !have);
+    if (need) {
+      const int n_need = __popc(need);
+      const int r = __popc(need & lt_mask);
+      int idx = -1;
+      int avail = end - next;
+      int take = min(n_need, avail);
+      if (!have && r < take) idx = next + r;
+      next += take;
+      if (n_need > take && !exhausted) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.work_counter, kChunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.n) {
+          exhausted = true;
         } else {
-          ++real_n;
-          atomicAdd(&s_count[cr.chosen], 1u);
-          if (cr.dE >= 0.0f) atomicAdd(&s_gain[cr.chosen], cr.dE);
-          else atomicAdd(&s_loss[cr.chosen], cr.dE);
-          const int ptype = s_proc[cr.chosen].type;
-          if (ptype == kIonization) {
-            const int k = append_slot(a.sec_count);
-            if (k < a.sec_cap) {
-              a.sec[2 * k] = make_float4(p.x, p.y, p.z, t);
-              a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, energy_of(cr.ej_v, hme));
-            } else {
-              atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
-            }
-          } else if (ptype == kAttachment) {
-            const int k = append_slot(a.att_count);
-            a.att_list[k] = slot;
-            dead = true;
-            done = true;
-            break;
-          }
+          next = base;
+          end = min(base + kChunk, a.n);
+          const int r2 = r - take;
+          const int take2 = min(n_need - take, end - next);
+          if (!have && r2 >= 0 && r2 < take2) idx = next + r2;
+          next += take2;
         }
-        s = -__logf(rng.oo());  // next free flight (BoltzmannMC.C:670)
       }
-      if (!done) atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+      if (idx >= 0) {
+        slot = a.list ? a.list[idx] : idx;
+        const float4 A = a.state[2 * slot];
+        const float4 B = a.state[2 * slot + 1];
+        if (B.w == 0.0f) {
+          p = make_float3(A.x - a.shift.x, A.y - a.shift.y, A.z - a.shift.z);
+          v = make_float3(B.x, B.y, B.z);
+          s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
+          t = 0.0f;
+          if (a.list) {
+            t = a.pend_t[slot];
+            a.pend_t[slot] = -1.0f;
+          }
+          rng.init((uint32_t)slot, a.interval, a.seed, a.salt);
+          energy = energy_of(v, hme);
+          events = 0;
+          have = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (!have) continue;
+
+    // ---- one event of this lane's electron
+    if (s < 0.0f) s = -__logf(rng.oo());
+    const float tau = s * inv_nu;
+    const float phi = a.phi0 + a.phase_rate * t;
+    bool finished = false, dead = false;
+    if (t + tau > T) {
+      // partial flight to the synchronisation time (BoltzmannMC.C:657-663)
+      const float dt = T - t;
+      free_flight(field, phi, dt, p, v);
+      s = fmaxf(s - nu * dt, 0.0f);
+      const float e1 = energy_of(v, hme);
+      gain_sum += e1 - energy;
+      energy = e1;
+      finished = true;
+    } else {
+      free_flight(field, phi, tau, p, v);
+      t += tau;
+      const float e1 = energy_of(v, hme);
+      gain_sum += e1 - energy;
+      energy = e1;
+      CollResult cr;
+      collide(a.c, a.t, s_proc, s_gas, nu, v, energy, rng, cr);
+      if (cr.chosen < 0) {
+        ++null_n;
+      } else {
+        ++real_n;
+        atomicAdd(&s_count[cr.chosen], 1u);
+        if (cr.dE >= 0.0f) atomicAdd(&s_gain[cr.chosen], cr.dE);
+        else atomicAdd(&s_loss[cr.chosen], cr.dE);
+        const int ptype = s_proc[cr.chosen].type;
+        if (ptype == kIonization) {
+          const int k = append_slot(a.sec_count);
+          if (k < a.sec_cap) {
+            a.sec[2 * k] = make_float4(p.x, p.y, p.z, t);
+            a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, energy_of(cr.ej_v, hme));
+          } else {
+            atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
+          }
+        } else if (ptype == kAttachment) {
+          const int k = append_slot(a.att_count);
+          a.att_list[k] = slot;
+          dead = true;
+          finished = true;
+        }
+      }
+      s = -__logf(rng.oo());  // next free flight (BoltzmannMC.C:670)
+      if (++events >= (1 << 20) && !finished) {
+        atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+        finished = true;
+      }
+    }
+    if (finished) {
       a.state[2 * slot] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
       a.state[2 * slot + 1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
-      if (!dead) e_max = energy;
+      if (!dead) e_max = fmaxf(e_max, energy);
+      have = false;
     }
   }
 
   // block reductions -> global tallies
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double g = warp_sum((double)gain_sum);
   unsigned long long nn = warp_sum_u64((unsigned long long)null_n);
   unsigned long long nr = warp_sum_u64((unsigned long long)real_n);
@@ -188,11 +245,11 @@ __global__ void __launch_bounds__(kAdvanceThreads) k_advance(AdvanceArgs a) {
     if (ns) atomicAdd(a.null_count, ns);
     if (rs) atomicAdd(a.real_count, rs);
   }
-  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
-    if (s_count[p]) {
-      atomicAdd(&a.proc_count[p], (unsigned long long)s_count[p]);
-      if (s_gain[p] != 0.0f) atomicAdd(&a.proc_gain[p], (double)s_gain[p]);
-      if (s_loss[p] != 0.0f) atomicAdd(&a.proc_loss[p], (double)s_loss[p]);
+  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
+    if (s_count[q]) {
+      atomicAdd(&a.proc_count[q], (unsigned long long)s_count[q]);
+      if (s_gain[q] != 0.0f) atomicAdd(&a.proc_gain[q], (double)s_gain[q]);
+      if (s_loss[q] != 0.0f) atomicAdd(&a.proc_loss[q], (double)s_loss[q]);
     }
   }
 }
@@ -326,10 +383,13 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
     m[19] += z * vx; m[20] += z * vy; m[21] += z * vz;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // FP32 tree reduction inside the warp (32 partials), FP64 across warps and blocks
 #pragma unroll
   for (int k = 0; k < kMoments; ++k) {
-    const double w = warp_sum((double)m[k]);
-    if (lane == 0) s_m[wid][k] = w;
+    float w = m[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (lane == 0) s_m[wid][k] = (double)w;
   }
   e_max = warp_max(e_max);
   if (lane == 0 && e_max > 0.0f) atomic_max_energy(a.max_energy_bits, e_max);
@@ -397,6 +457,13 @@ __device__ __forceinline__ int uniform_index(uint32_t w, int n) {
 // A slot that must still be advanced from time t0 to the synchronisation
 // time. pend_t[slot] holds the start time (NaN or negative: not pending); a
 // slot enters the list once even when it is refilled twice in one round.
+// adds a per-thread energy to the growth accumulator with one atomic per warp
+__device__ __forceinline__ void add_growth(double* growth, double e) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  const double tot = cg::reduce(g, e, cg::plus<double>());
+  if (g.thread_rank() == 0) atomicAdd(growth, tot);
+}
+
 __device__ __forceinline__ void mark_pending(const PopArgs& a, int slot, float t0) {
   const float old = atomicExch(&a.pend_t[slot], t0);
   if (!(old >= 0.0f)) {
@@ -439,7 +506,7 @@ __global__ void k_pop_clone(PopArgs a) {
   const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
   a.state[2 * dest] = A;
   a.state[2 * dest + 1] = B;
-  atomicAdd(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
+  add_growth(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
   const float t0 = a.pend_t[src];
   if (t0 >= 0.0f) mark_pending(a, dest, t0);
 }
@@ -476,7 +543,7 @@ __global__ void k_pop_pair(PopArgs a) {
   } else if (r >= a.n_electrons) {
     // a removed secondary: its energy leaves the ensemble
     const int sidx = r - a.n_electrons;
-    atomicAdd(a.growth, -(double)a.sec[2 * sidx + 1].w);
+    add_growth(a.growth, -(double)a.sec[2 * sidx + 1].w);
   }
   // secondary j survives when its pool bit was not claimed
   const int b = a.n_electrons + j;
@@ -493,7 +560,7 @@ __global__ void k_pop_place(PopArgs a) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
     const float4 B = a.state[2 * slot + 1];
-    atomicAdd(a.growth, -(double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
+    add_growth(a.growth, -(double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
     const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
     a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
     a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
@@ -562,7 +629,10 @@ inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; 
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
-  const int grid = blocks_for(a.n, kAdvanceThreads);
+  // persistent grid: at most kAdvanceBlocksPerSM blocks per SM, fewer when
+  // the electrons do not fill them (one chunk per warp)
+  const int warps_needed = (a.n + kChunk - 1) / kChunk;
+  const int grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
   switch (a.field.mode) {
     case kFieldDC: k_advance<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
     case kFieldAC: k_advance<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;

@@ -48,6 +48,8 @@ struct AdvanceArgs {
   double* field_gain;
   unsigned int* max_energy_bits;   // float bits of the largest final energy
   int* error_flag;                 // 2: secondary buffer full, 3: collision budget exhausted
+  int* work_counter;               // chunk counter of the persistent grid (zero before the launch)
+  int sm_count;
 };
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);

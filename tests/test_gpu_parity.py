@@ -87,11 +87,17 @@ def _boundary_margin(pr, f, nu, vel, energy, u):
     return min(m1, m2)
 
 
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
 def test_collisions(gpu_case):
+    """The kernel reads its inputs (trial frequency, velocity, energy and the
+    recorded uniforms) as FP32; the oracle gets the same FP32-rounded values,
+    so the comparison measures the FP32 arithmetic of the kinematics alone."""
     name, g, ctx, ps = gpu_case
     sc = g["scalars_tab"]
     M = len(g["tab_grid"])
-    ctx.build_tables(sc[15], M, ps.n)
     pr = O.OracleProcs(gu.proc_arrays(g), M)
     pr.build_tables(O.make_fields(sc[0], sc[1]), sc[15])
     from lokigpu import capi
@@ -104,26 +110,28 @@ def test_collisions(gpu_case):
         c2.set_processes(ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
         c2.set_conditions(sc[0], sc[1], 100.0)
         c2.build_tables(sc[15], M, ps.n)
-        nu, vel, en, U = g[f"col{m}_nu"], g[f"col{m}_vel"], g[f"col{m}_energy"], g[f"col{m}_u"]
+        nu, vel, en, U = (_f32(g[f"col{m}_{k}"]) for k in ("nu", "vel", "energy", "u"))
         out, used = c2.replay_collisions(nu, vel, en, U)
         c2.close()
-        ref = g[f"col{m}_out"]
         f = O.make_fields(sc[0], sc[1], gas_temp_effect=int(gte), sharing=int(shr), sharing_factor=fac)
-        mismatch, unexplained = 0, 0
+        mismatch, unexplained, compared = 0, 0, 0
         for k in range(len(nu)):
-            if out[k][0] != ref[k][0]:
+            ref, ref_used, _ = O.collide(pr, f, nu[k], vel[k], en[k], U[k])
+            if out[k][0] != ref[0]:
                 mismatch += 1
                 if int(gte) == 0 and _boundary_margin(pr, f, nu[k], vel[k], en[k], U[k]) > 1e-5:
                     unexplained += 1
                 continue
-            if ref[k][0] < 0:
+            if ref[0] < 0:
                 continue
-            assert used[k] == g[f"col{m}_used"][k], (name, m, k)
-            vs = np.linalg.norm(ref[k][1:4])
-            assert np.linalg.norm(out[k][1:4] - ref[k][1:4]) <= 1e-5 * max(vs, 1.0), (name, m, k, out[k], ref[k])
-            assert abs(out[k][4] - ref[k][4]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
-            assert abs(out[k][5] - ref[k][5]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
-            es = np.linalg.norm(ref[k][7:10])
-            assert np.linalg.norm(out[k][7:10] - ref[k][7:10]) <= 1e-5 * max(es, 1.0), (name, m, k)
+            compared += 1
+            assert used[k] == ref_used, (name, m, k)
+            vs = np.linalg.norm(ref[1:4])
+            assert np.linalg.norm(out[k][1:4] - ref[1:4]) <= 1e-5 * max(vs, 1.0), (name, m, k, out[k], ref)
+            assert abs(out[k][4] - ref[4]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
+            assert abs(out[k][5] - ref[5]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
+            es = np.linalg.norm(ref[7:10])
+            assert np.linalg.norm(out[k][7:10] - ref[7:10]) <= 1e-5 * max(es, 1.0), (name, m, k)
+        assert compared > 100, (name, m, compared)
         assert mismatch <= 0.02 * len(nu), (name, m, mismatch)
         assert unexplained <= 2, (name, m, unexplained)
