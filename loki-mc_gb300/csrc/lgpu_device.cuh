@@ -240,47 +240,56 @@ __device__ __forceinline__ float3 euler(float sChi, float cChi, float sEta, floa
 }
 
 // cos(chi) samplers (AngularScatteringFunctions.h:27-74). Each returns
-// (cos chi, 1 - cos chi) with the second term formed without cancellation, so
-// that sin chi = sqrt((1-c)(1+c)) keeps FP32 accuracy for forward scattering.
+// (cos chi, 1 - cos chi, 1 + cos chi), the last two formed without
+// cancellation, so that sin chi = sqrt((1-c)(1+c)) keeps FP32 accuracy for
+// forward and backward scattering alike.
 template <class Rng>
-__device__ __forceinline__ float2 sample_cos_chi(const ProcF& pr, float energy, float energy_after, Rng& rng) {
+__device__ __forceinline__ float3 sample_cos_chi(const ProcF& pr, float energy, float energy_after, Rng& rng) {
   switch (pr.sampler) {
     case kSamplerForward:
-      return make_float2(1.0f, 0.0f);
+      return make_float3(1.0f, 0.0f, 2.0f);
     case kSamplerBornDipole: {
-      // Vialetto 2021, eq. 25: 1 + 2 r2/(1-r2) (1 - r2^-U)
+      // Vialetto 2021, eq. 25: c = 1 + 2 r2/(1-r2) (1 - r2^-U)
+      // 1 - c = 2 r2 (r2^-U - 1)/(1-r2), 1 + c = 2 (1 - r2^(1-U))/(1-r2)
       const float s = sqrtf(energy_after) + sqrtf(energy);
       const float ratio = pr.eloss / (s * s);
       const float r2 = ratio * ratio;
       const float u = rng.cc();
-      const float om = 2.0f * r2 / (1.0f - r2) * expm1f(-u * logf(r2));  // 1 - cos
-      return make_float2(1.0f - om, om);
+      const float lr = logf(r2);
+      const float inv = 1.0f / (1.0f - r2);
+      const float om = 2.0f * r2 * inv * expm1f(-u * lr);
+      const float op = -2.0f * inv * expm1f((1.0f - u) * lr);
+      return make_float3(1.0f - om, om, op);
     }
     case kSamplerSurendra: {
-      // Vahedi 1995, eq. 9: (2 + e - 2 (1+e)^U) / e ; 1 - cos = 2((1+e)^U - 1)/e
+      // Vahedi 1995, eq. 9: c = (2 + e - 2 (1+e)^U) / e
+      // 1 - c = 2((1+e)^U - 1)/e, 1 + c = -2 (1+e) ((1+e)^(U-1) - 1)/e
       const float u = rng.cc();
-      const float om = 2.0f * expm1f(u * log1pf(energy)) / energy;
-      return make_float2(1.0f - om, om);
+      const float l = log1pf(energy);
+      const float om = 2.0f * expm1f(u * l) / energy;
+      const float op = -2.0f * (1.0f + energy) * expm1f((u - 1.0f) * l) / energy;
+      return make_float3(1.0f - om, om, op);
     }
     case kSamplerCoulombScreen: {
-      // Hagelaar 2000, eqs. 21-23: (sp + 1 - (2 sp + 1) R) / (sp + 1 - R); 1 - cos = 2 sp R / (sp + 1 - R)
+      // Hagelaar 2000, eqs. 21-23: c = (sp + 1 - (2 sp + 1) R) / (sp + 1 - R)
+      // 1 - c = 2 sp R / d, 1 + c = 2 (sp + 1)(1 - R) / d, d = sp + (1 - R)
       const float eps = (pr.sp0 == 0.0f) ? energy : energy_after;
       const float sp = pr.sp1 / eps;
       const float R = rng.cc();
-      const float den = sp + 1.0f - R;
-      const float om = 2.0f * sp * R / den;
-      return make_float2((sp + 1.0f - (2.0f * sp + 1.0f) * R) / den, om);
+      const float omr = 1.0f - R;
+      const float inv = 1.0f / (sp + omr);
+      const float om = 2.0f * sp * R * inv;
+      const float op = 2.0f * (sp + 1.0f) * omr * inv;
+      return make_float3((sp + 1.0f - (2.0f * sp + 1.0f) * R) * inv, om, op);
     }
-    default: {  // isotropic: 1 - 2U
+    default: {  // isotropic: c = 1 - 2U
       const float u = rng.cc();
-      return make_float2(1.0f - 2.0f * u, 2.0f * u);
+      return make_float3(1.0f - 2.0f * u, 2.0f * u, 2.0f * (1.0f - u));
     }
   }
 }
 
-__device__ __forceinline__ float sin_from(float2 c) {
-  return sqrtf(fmaxf(0.0f, c.y * (2.0f - c.y)));
-}
+__device__ __forceinline__ float sin_from(float3 c) { return sqrtf(fmaxf(0.0f, c.y * c.z)); }
 
 // Result of one collision event.
 struct CollResult {
@@ -310,7 +319,7 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
       const float relE = 0.5f * pr.red_mass * s.speed * s.speed * c.inv_qe;
       const float relEA = relE - pr.eloss;
       if (relEA <= 0.0f) return false;
-      const float2 cc = sample_cos_chi(pr, relE, relEA, rng);
+      const float3 cc = sample_cos_chi(pr, relE, relEA, rng);
       const float cChi = cc.x, sChi = sin_from(cc);
       float sEta, cEta;
       sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
@@ -326,7 +335,7 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
       const Sph s = cart2sph(v);
       const float eA = incident - pr.eloss;
       if (eA <= 0.0f) return false;
-      const float2 cc = sample_cos_chi(pr, incident, eA, rng);
+      const float3 cc = sample_cos_chi(pr, incident, eA, rng);
       const float cChi = cc.x, sChi = sin_from(cc);
       float sEta, cEta;
       sincosf(kTwoPiF * rng.oc(), &sEta, &cEta);
@@ -365,11 +374,11 @@ __device__ __forceinline__ bool apply_collision(const Consts& c, const ProcF& pr
       sEtaE = -sEtaS;
       cEtaE = -cEtaS;
     } else {
-      const float2 cs = sample_cos_chi(pr, incident, scat, rng);
+      const float3 cs = sample_cos_chi(pr, incident, scat, rng);
       cChiS = cs.x;
       sChiS = sin_from(cs);
       sincosf(kTwoPiF * rng.oc(), &sEtaS, &cEtaS);
-      const float2 ce = sample_cos_chi(pr, incident, ej, rng);
+      const float3 ce = sample_cos_chi(pr, incident, ej, rng);
       cChiE = ce.x;
       sChiE = sin_from(ce);
       sincosf(kTwoPiF * rng.oc(), &sEtaE, &cEtaE);

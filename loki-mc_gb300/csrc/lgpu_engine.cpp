@@ -31,6 +31,7 @@ constexpr double kMeD = 9.10938356e-31;    // Constant.h:8
 constexpr double kKbD = 1.38064852e-23;    // Constant.h:6
 constexpr double kNonDef = -123456789.0;   // Constant.h:23
 constexpr double kPi = 3.14159265358979323846;
+constexpr uint32_t kGraphPopRounds = 2;  // population-control rounds inside the captured interval
 
 struct Kahan {
   double s = 0, c = 0;
@@ -53,6 +54,8 @@ struct DevScalars {
   unsigned long long real_count;
   double field_gain;
   double growth;
+  unsigned int sample_max_bits;
+  int pad2;
   double moments[kMoments];
 };
 
@@ -140,6 +143,9 @@ class Engine {
     LGPU_TRY(dalloc(&d_pair_sec_, (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_sc_, 1));
     LGPU_CU(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
+    LGPU_TRY(dalloc(&d_ctl_, 1));
+    LGPU_CU(cudaMallocHost((void**)&h_ctl_, sizeof(IntervalCtl)));
+    std::memset(h_ctl_, 0, sizeof(IntervalCtl));
     LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
     LGPU_CU(cudaMemsetAsync(d_pend_t_, 0xFF, (size_t)N_ * sizeof(float), stream_));  // NaN: not pending
     LGPU_CU(cudaMemsetAsync(d_sc_, 0, sizeof(DevScalars), stream_));
@@ -158,6 +164,11 @@ class Engine {
 
   void release() {
     if (stream_) cudaStreamSynchronize(stream_);
+    drop_graphs();
+    if (d_ctl_) cudaFree(d_ctl_);
+    if (h_ctl_) cudaFreeHost(h_ctl_);
+    d_ctl_ = nullptr;
+    h_ctl_ = nullptr;
     void* ptrs[] = {d_state_, d_pend_t_, d_pend_list_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
                     d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_cum_pair_, d_sig_pair_, d_procf_,
                     d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
@@ -453,6 +464,7 @@ class Engine {
   // ------------------------------------------------------------ ensemble
   int init_ensemble() {
     if (!have_procs_ || !have_cond_) return fail(LGPU_ERR_STATE, "set_processes and set_conditions come first");
+    drop_graphs();  // kernel arguments (field, constants, sizes) may have changed
     LGPU_TRY(upload_proc_consts());
     time_ = 0;
     ss_time_ = kNonDef;
@@ -528,33 +540,11 @@ class Engine {
     return sync("read_scalars");
   }
 
-  // one synchronisation interval (BoltzmannMC.C:617-688)
-  int step_interval() {
-    LGPU_TRY(check_max_frequency(cur_max_energy_));
-    const double dt_sync = cfg_.sync_x / nu_trial_;
-    double phi0 = 0.0, rate = 0.0;
-    if (field_.mode == kFieldAC || field_.mode == kFieldACB) {
-      phi0 = std::fmod(omega_ * time_, 2.0 * kPi);
-      rate = omega_;
-    } else if (field_.mode == kFieldECR) {
-      phi0 = std::fmod(omega_c_ * time_, 2.0 * kPi);
-      rate = omega_c_;
-    }
-    // reset per-interval counters (sec, att, pend, error, pairs, max energy)
-    LGPU_CU(cudaMemsetAsync(d_sc_, 0, offsetof(DevScalars, null_count), stream_));
+  AdvanceArgs advance_args() const {
     AdvanceArgs a{};
     a.state = d_state_;
-    a.n = N_;
-    a.list = nullptr;
     a.pend_t = d_pend_t_;
-    a.dt_sync = (float)dt_sync;
-    a.phi0 = (float)phi0;
-    a.phase_rate = (float)rate;
-    a.nu = (float)nu_trial_;
     a.seed = cfg_.seed;
-    a.interval = interval_;
-    a.salt = 0;
-    a.shift = make_float3((float)shift_[0], (float)shift_[1], (float)shift_[2]);
     a.field = field_;
     a.c = consts();
     a.t = tables();
@@ -576,16 +566,146 @@ class Engine {
     a.error_flag = &d_sc_->error_flag;
     a.work_counter = &d_sc_->work_counter;
     a.sm_count = sm_count_;
-    LGPU_CU(cudaEventRecord(ev0_, stream_));
+    a.ctl = d_ctl_;
+    return a;
+  }
+
+  PopArgs pop_args(uint32_t round) const {
+    PopArgs p{};
+    p.state = d_state_;
+    p.n_electrons = N_;
+    p.sec = d_sec_;
+    p.att_list = d_att_;
+    p.pend_t = d_pend_t_;
+    p.pend_list = d_pend_list_;
+    p.pend_count = &d_sc_->pend_count;
+    p.claim = d_claim_;
+    p.removed = d_removed_;
+    p.pair_slot = d_pair_slot_;
+    p.pair_sec = d_pair_sec_;
+    p.pair_counts = d_sc_->pair_counts;
+    p.growth = &d_sc_->growth;
+    p.half_me_over_e = (float)(0.5 * kMeD / kQeD);
+    p.seed = cfg_.seed;
+    p.salt = round;
+    p.error_flag = &d_sc_->error_flag;
+    p.n_sec_dev = &d_sc_->sec_count;
+    p.n_att_dev = &d_sc_->att_count;
+    p.ctl = d_ctl_;
+    p.grid_blocks = 2 * sm_count_;
+    return p;
+  }
+
+  // One population-control round and the advance of the electrons it left
+  // pending, with every count read on the device.
+  void enqueue_pop_round(uint32_t round) {
+    cudaMemsetAsync(&d_sc_->pend_count, 0, sizeof(int), stream_);
+    cudaMemsetAsync(d_sc_->pair_counts, 0, 2 * sizeof(int), stream_);
+    launch_pop_control(pop_args(round), stream_);
+    cudaMemsetAsync(&d_sc_->sec_count, 0, 2 * sizeof(int), stream_);  // sec_count, att_count
+    cudaMemsetAsync(&d_sc_->work_counter, 0, sizeof(int), stream_);
+    AdvanceArgs b = advance_args();
+    b.list = d_pend_list_;
+    b.n_dev = &d_sc_->pend_count;
+    b.salt = round;
+    b.grid_blocks = sm_count_;
+    launch_advance(b, stream_);
+    launches_ += 7;
+  }
+
+  // The device work of one interval: the advance of every electron, two
+  // population-control rounds (when the mixture ionizes or attaches), the
+  // ensemble sample and the scalar read-back. Captured once as a CUDA graph.
+  void enqueue_interval(bool sample) {
+    copy(d_ctl_, h_ctl_, sizeof(IntervalCtl), cudaMemcpyHostToDevice);
+    cudaMemsetAsync(d_sc_, 0, offsetof(DevScalars, null_count), stream_);
+    AdvanceArgs a = advance_args();
+    a.n = N_;
+    cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
     launch_advance(a, stream_);
-    LGPU_CU(cudaEventRecord(ev1_, stream_));
+    cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
     ++launches_;
+    if (have_ion_att_)
+      for (uint32_t r = 1; r <= kGraphPopRounds; ++r) enqueue_pop_round(r);
+    if (sample) enqueue_sample();
+    copy(h_sc_, d_sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost);
+  }
+
+  void enqueue_sample() {
+    cudaMemsetAsync(d_sc_->moments, 0, sizeof(double) * kMoments, stream_);
+    cudaMemsetAsync(&d_sc_->sample_max_bits, 0, sizeof(unsigned int), stream_);
+    SampleArgs s{};
+    s.state = d_state_;
+    s.n = N_;
+    s.half_me_over_e = (float)(0.5 * kMeD / kQeD);
+    s.moments = d_sc_->moments;
+    s.max_energy_bits = &d_sc_->sample_max_bits;
+    launch_sample(s, stream_);
+    ++launches_;
+  }
+
+  int graph_for(bool sample, cudaGraphExec_t* out) {
+    cudaGraphExec_t& ge = graph_[sample ? 1 : 0];
+    if (!ge) {
+      cudaGraph_t g;
+      const long long l0 = launches_;
+      LGPU_CU(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+      enqueue_interval(sample);
+      LGPU_CU(cudaStreamEndCapture(stream_, &g));
+      LGPU_CU(cudaGraphInstantiate(&ge, g, 0));
+      cudaGraphDestroy(g);
+      graph_launches_[sample ? 1 : 0] = launches_ - l0;
+      launches_ = l0;
+      h2d_bytes_ -= sizeof(IntervalCtl);
+      d2h_bytes_ -= sizeof(DevScalars);
+    }
+    *out = ge;
+    return LGPU_OK;
+  }
+
+  void drop_graphs() {
+    for (auto& g : graph_)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
+
+  // one synchronisation interval (BoltzmannMC.C:617-688); when `sample`, the
+  // ensemble moments at its end are in h_sc_ afterwards
+  int step_interval(bool sample) {
+    LGPU_TRY(check_max_frequency(cur_max_energy_));
+    const double dt_sync = cfg_.sync_x / nu_trial_;
+    double phi0 = 0.0, rate = 0.0;
+    if (field_.mode == kFieldAC || field_.mode == kFieldACB) {
+      phi0 = std::fmod(omega_ * time_, 2.0 * kPi);
+      rate = omega_;
+    } else if (field_.mode == kFieldECR) {
+      phi0 = std::fmod(omega_c_ * time_, 2.0 * kPi);
+      rate = omega_c_;
+    }
+    IntervalCtl& c = *h_ctl_;
+    c.dt_sync = (float)dt_sync;
+    c.phi0 = (float)phi0;
+    c.phase_rate = (float)rate;
+    c.nu = (float)nu_trial_;
+    c.inv_step = (float)(1.0 / step_);
+    c.shift_x = (float)shift_[0];
+    c.shift_y = (float)shift_[1];
+    c.shift_z = (float)shift_[2];
+    c.interval = interval_;
+    cudaGraphExec_t ge;
+    LGPU_TRY(graph_for(sample, &ge));
+    LGPU_CU(cudaGraphLaunch(ge, stream_));
+    launches_ += graph_launches_[sample ? 1 : 0];
+    h2d_bytes_ += sizeof(IntervalCtl);
+    d2h_bytes_ += sizeof(DevScalars);
     // the origin shift is now part of the stored offsets
     for (int k = 0; k < 3; ++k) {
       origin_[k] += (double)(float)shift_[k];
       shift_[k] = 0;
     }
-    LGPU_TRY(read_scalars());
+    LGPU_TRY(sync("interval"));
     {
       float ms = 0;
       LGPU_CU(cudaEventElapsedTime(&ms, ev0_, ev1_));
@@ -594,52 +714,22 @@ class Engine {
       adv_electron_steps_ += N_;
     }
     LGPU_TRY(check_device_errors());
-    // population control and pending rounds (BoltzmannMC.C:1282-1408)
-    for (int round = 1; have_ion_att_ && (h_sc_->sec_count > 0 || h_sc_->att_count > 0); ++round) {
+    // rounds beyond the captured ones (rare: secondaries of secondaries within
+    // one interval), then a fresh sample
+    bool extra = false;
+    for (uint32_t round = kGraphPopRounds + 1; have_ion_att_ && (h_sc_->sec_count > 0 || h_sc_->att_count > 0);
+         ++round) {
       if (round > 256) return fail(LGPU_ERR_OVERFLOW, "population control did not settle");
-      const int nS = h_sc_->sec_count, nA = h_sc_->att_count;
-      if (nS > sec_cap_) return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", nS, sec_cap_);
-      PopArgs p{};
-      p.state = d_state_;
-      p.n_electrons = N_;
-      p.sec = d_sec_;
-      p.n_sec = nS;
-      p.att_list = d_att_;
-      p.n_att = nA;
-      p.pend_t = d_pend_t_;
-      p.pend_list = d_pend_list_;
-      p.pend_count = &d_sc_->pend_count;
-      p.claim = d_claim_;
-      p.removed = d_removed_;
-      p.pair_slot = d_pair_slot_;
-      p.pair_sec = d_pair_sec_;
-      p.pair_counts = d_sc_->pair_counts;
-      p.growth = &d_sc_->growth;
-      p.half_me_over_e = (float)(0.5 * kMeD / kQeD);
-      p.seed = cfg_.seed;
-      p.interval = interval_;
-      p.salt = (uint32_t)round;
-      p.error_flag = &d_sc_->error_flag;
-      LGPU_CU(cudaMemsetAsync(&d_sc_->pend_count, 0, sizeof(int), stream_));
-      LGPU_CU(cudaMemsetAsync(d_sc_->pair_counts, 0, 2 * sizeof(int), stream_));
-      launch_pop_control(p, stream_);
-      launches_ += 6;
+      if (h_sc_->sec_count > sec_cap_)
+        return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", h_sc_->sec_count, sec_cap_);
+      enqueue_pop_round(round);
       LGPU_TRY(read_scalars());
       LGPU_TRY(check_device_errors());
-      const int npend = h_sc_->pend_count;
-      LGPU_CU(cudaMemsetAsync(&d_sc_->sec_count, 0, 2 * sizeof(int), stream_));
-      if (npend > 0) {
-        LGPU_CU(cudaMemsetAsync(&d_sc_->work_counter, 0, sizeof(int), stream_));
-        AdvanceArgs b = a;
-        b.n = npend;
-        b.list = d_pend_list_;
-        b.salt = (uint32_t)round;
-        b.shift = make_float3(0.f, 0.f, 0.f);
-        launch_advance(b, stream_);
-        ++launches_;
-      }
+      extra = true;
+    }
+    if (extra && sample) {
+      enqueue_sample();
       LGPU_TRY(read_scalars());
-      LGPU_TRY(check_device_errors());
     }
     {
       float f;
@@ -669,23 +759,20 @@ class Engine {
     return LGPU_OK;
   }
 
-  // calculateMeanDataForSwarmParams (BoltzmannMC.C:1410-1482)
+  // ensemble moments at t = 0 (BoltzmannMC.C:306-310), outside the interval graph
   int sample_moments() {
-    LGPU_CU(cudaMemsetAsync(d_sc_->moments, 0, sizeof(double) * kMoments, stream_));
-    LGPU_CU(cudaMemsetAsync(&d_sc_->max_energy_bits, 0, sizeof(unsigned int), stream_));
-    SampleArgs s{};
-    s.state = d_state_;
-    s.n = N_;
-    s.half_me_over_e = (float)(0.5 * kMeD / kQeD);
-    s.moments = d_sc_->moments;
-    s.max_energy_bits = &d_sc_->max_energy_bits;
-    launch_sample(s, stream_);
-    ++launches_;
+    enqueue_sample();
     LGPU_TRY(read_scalars());
+    return process_sample();
+  }
+
+  // calculateMeanDataForSwarmParams (BoltzmannMC.C:1410-1482) on the moment
+  // sums of the last sample (h_sc_)
+  int process_sample() {
     const double* S = h_sc_->moments;
     const double n = (double)N_;
     float fmax;
-    std::memcpy(&fmax, &h_sc_->max_energy_bits, 4);
+    std::memcpy(&fmax, &h_sc_->sample_max_bits, 4);
     cur_max_energy_ = fmax;
     max_elec_energy_ = std::fmax(max_elec_energy_, (double)fmax);
     if (max_elec_energy_ > emax_elastic_) {
@@ -954,11 +1041,12 @@ class Engine {
         capped = 1;
         break;
       }
-      LGPU_TRY(step_interval());
+      const bool sampling = (n_sync_ + 1) % cfg_.sync_oversampling == 0;
+      LGPU_TRY(step_interval(sampling));
       ++steps;
-      if (n_sync_ % cfg_.sync_oversampling == 0) {
+      if (sampling) {
         ++n_samp_;
-        LGPU_TRY(sample_moments());
+        LGPU_TRY(process_sample());
         int dec = (int)std::fmax(std::log((double)n_samp_) / std::log(2.0) - 11, 6);
         const long long between_ss = (long long)std::pow(2, dec);
         if (ss_time_ != kNonDef) {
@@ -1118,9 +1206,9 @@ class Engine {
   int advance(int n, lgpu_step_report* rep) {
     if (!initialized_) return fail(LGPU_ERR_STATE, "init_ensemble comes first");
     for (int i = 0; i < n; ++i) {
-      LGPU_TRY(step_interval());
+      LGPU_TRY(step_interval(true));
       ++n_samp_;
-      LGPU_TRY(sample_moments());
+      LGPU_TRY(process_sample());
     }
     if (rep) {
       LGPU_TRY(read_counters());
@@ -1296,6 +1384,10 @@ class Engine {
   int *d_removed_ = nullptr, *d_pair_slot_ = nullptr, *d_pair_sec_ = nullptr;
   DevScalars* d_sc_ = nullptr;
   DevScalars* h_sc_ = nullptr;
+  IntervalCtl* d_ctl_ = nullptr;
+  IntervalCtl* h_ctl_ = nullptr;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  long long graph_launches_[2] = {0, 0};
   float2 *d_nu_pair_ = nullptr, *d_cum_pair_ = nullptr, *d_sig_pair_ = nullptr;
   double *d_nu_tot_ = nullptr, *d_nu_max_ = nullptr;
   ProcF* d_procf_ = nullptr;

@@ -88,8 +88,21 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
 
   FieldF field = a.field;
   field.mode = MODE;
-  const float T = a.dt_sync;
-  const float nu = a.nu;
+  float T = a.dt_sync, nu = a.nu, phi0 = a.phi0, phase_rate = a.phase_rate;
+  float3 shift = a.shift;
+  uint64_t interval = a.interval;
+  TablesF tab = a.t;
+  if (a.ctl) {
+    const IntervalCtl c = *a.ctl;
+    T = c.dt_sync;
+    nu = c.nu;
+    phi0 = c.phi0;
+    phase_rate = c.phase_rate;
+    shift = make_float3(c.shift_x, c.shift_y, c.shift_z);
+    interval = c.interval;
+    tab.inv_step = c.inv_step;
+  }
+  const int n_el = a.n_dev ? *a.n_dev : a.n;
   const float inv_nu = 1.0f / nu;
   const float hme = a.c.half_me_over_e;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -125,11 +138,11 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
         int base = 0;
         if (lane == 0) base = atomicAdd(a.work_counter, kChunk);
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= a.n) {
+        if (base >= n_el) {
           exhausted = true;
         } else {
           next = base;
-          end = min(base + kChunk, a.n);
+          end = min(base + kChunk, n_el);
           const int r2 = r - take;
           const int take2 = min(n_need - take, end - next);
           if (!have && r2 >= 0 && r2 < take2) idx = next + r2;
@@ -141,7 +154,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
         const float4 A = a.state[2 * slot];
         const float4 B = a.state[2 * slot + 1];
         if (B.w == 0.0f) {
-          p = make_float3(A.x - a.shift.x, A.y - a.shift.y, A.z - a.shift.z);
+          p = make_float3(A.x - shift.x, A.y - shift.y, A.z - shift.z);
           v = make_float3(B.x, B.y, B.z);
           s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
           t = 0.0f;
@@ -149,7 +162,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
             t = a.pend_t[slot];
             a.pend_t[slot] = -1.0f;
           }
-          rng.init((uint32_t)slot, a.interval, a.seed, a.salt);
+          rng.init((uint32_t)slot, interval, a.seed, a.salt);
           energy = energy_of(v, hme);
           events = 0;
           have = true;
@@ -165,7 +178,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
     // ---- one event of this lane's electron
     if (s < 0.0f) s = -__logf(rng.oo());
     const float tau = s * inv_nu;
-    const float phi = a.phi0 + a.phase_rate * t;
+    const float phi = phi0 + phase_rate * t;
     bool finished = false, dead = false;
     if (t + tau > T) {
       // partial flight to the synchronisation time (BoltzmannMC.C:657-663)
@@ -183,7 +196,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
       gain_sum += e1 - energy;
       energy = e1;
       CollResult cr;
-      collide(a.c, a.t, s_proc, s_gas, nu, v, energy, rng, cr);
+      collide(a.c, tab, s_proc, s_gas, nu, v, energy, rng, cr);
       if (cr.chosen < 0) {
         ++null_n;
       } else {
@@ -472,91 +485,110 @@ __device__ __forceinline__ void mark_pending(const PopArgs& a, int slot, float t
   }
 }
 
+// Counts and interval index of one population-control round, from the
+// device (graph replay) or from the launch arguments.
+struct PopCounts {
+  int n_sec, n_att;
+  uint64_t interval;
+};
+__device__ __forceinline__ PopCounts pop_counts(const PopArgs& a) {
+  PopCounts c;
+  c.n_sec = a.n_sec_dev ? *a.n_sec_dev : a.n_sec;
+  c.n_att = a.n_att_dev ? *a.n_att_dev : a.n_att;
+  c.interval = a.ctl ? a.ctl->interval : a.interval;
+  return c;
+}
+#define GRID_STRIDE(j, n) for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < (n); j += gridDim.x * blockDim.x)
+
 // (1) attached slots take secondaries, last secondary first (BoltzmannMC.C:1344-1359)
 __global__ void k_pop_fill(PopArgs a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = min(a.n_att, a.n_sec);
-  if (j >= k) return;
-  const int slot = a.att_list[j];
-  const int sidx = a.n_sec - 1 - j;
-  const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
-  a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
-  a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
-  mark_pending(a, slot, S0.w);
+  const PopCounts pc = pop_counts(a);
+  const int k = min(pc.n_att, pc.n_sec);
+  GRID_STRIDE(j, k) {
+    const int slot = a.att_list[j];
+    const int sidx = pc.n_sec - 1 - j;
+    const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
+    a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
+    a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
+    mark_pending(a, slot, S0.w);
+  }
 }
 
 // (2) remaining attached slots clone a random surviving electron
 // (BoltzmannMC.C:1360-1376); the energy-growth term gains its energy.
 __global__ void k_pop_clone(PopArgs a) {
-  const int j = a.n_sec + blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= a.n_att) return;
-  const int dest = a.att_list[j];
-  int src = -1;
-  for (uint32_t d = 0; d < 4096u; ++d) {
-    const int r = uniform_index(pop_word((uint32_t)j, a.interval, a.seed, a.salt, d), a.n_electrons);
-    if (a.state[2 * r + 1].w == 0.0f) {
-      src = r;
-      break;
+  const PopCounts pc = pop_counts(a);
+  GRID_STRIDE(jj, pc.n_att - pc.n_sec) {
+    const int j = pc.n_sec + jj;
+    const int dest = a.att_list[j];
+    int src = -1;
+    for (uint32_t d = 0; d < 4096u; ++d) {
+      const int r = uniform_index(pop_word((uint32_t)j, pc.interval, a.seed, a.salt, d), a.n_electrons);
+      if (a.state[2 * r + 1].w == 0.0f) {
+        src = r;
+        break;
+      }
     }
+    if (src < 0) {
+      atomicExch(a.error_flag, 4);
+      continue;
+    }
+    const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
+    a.state[2 * dest] = A;
+    a.state[2 * dest + 1] = B;
+    add_growth(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
+    const float t0 = a.pend_t[src];
+    if (t0 >= 0.0f) mark_pending(a, dest, t0);
   }
-  if (src < 0) {
-    atomicExch(a.error_flag, 1);
-    return;
-  }
-  const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
-  a.state[2 * dest] = A;
-  a.state[2 * dest + 1] = B;
-  add_growth(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
-  const float t0 = a.pend_t[src];
-  if (t0 >= 0.0f) mark_pending(a, dest, t0);
 }
 
 // (3) excess secondaries: remove a uniformly random subset of size m from the
 // pool of n_electrons slots + m unplaced secondaries, the outcome of the
 // reference's sequential uniform removal (BoltzmannMC.C:1379-1407).
 __global__ void k_pop_claim(PopArgs a) {
-  const int m = a.n_sec - a.n_att;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
+  const PopCounts pc = pop_counts(a);
+  const int m = pc.n_sec - pc.n_att;
   const int pool = a.n_electrons + m;
-  for (uint32_t d = 0; d < 4096u; ++d) {
-    const int r = uniform_index(pop_word((uint32_t)j, a.interval, a.seed, a.salt ^ 0x55u, d), pool);
-    const unsigned int bit = 1u << (r & 31);
-    const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
-    if (!(old & bit)) {
-      a.removed[j] = r;
-      return;
+  GRID_STRIDE(j, m) {
+    int got = -1;
+    for (uint32_t d = 0; d < 4096u; ++d) {
+      const int r = uniform_index(pop_word((uint32_t)j, pc.interval, a.seed, a.salt ^ 0x55u, d), pool);
+      const unsigned int bit = 1u << (r & 31);
+      const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
+      if (!(old & bit)) {
+        got = r;
+        break;
+      }
     }
+    a.removed[j] = got;
+    if (got < 0) atomicExch(a.error_flag, 5);
   }
-  a.removed[j] = -1;
-  atomicExch(a.error_flag, 1);
 }
 
 __global__ void k_pop_pair(PopArgs a) {
-  const int m = a.n_sec - a.n_att;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
-  const int r = a.removed[j];
-  if (r >= 0 && r < a.n_electrons) {
-    const int q = atomicAdd(&a.pair_counts[0], 1);
-    a.pair_slot[q] = r;
-  } else if (r >= a.n_electrons) {
-    // a removed secondary: its energy leaves the ensemble
-    const int sidx = r - a.n_electrons;
-    add_growth(a.growth, -(double)a.sec[2 * sidx + 1].w);
-  }
-  // secondary j survives when its pool bit was not claimed
-  const int b = a.n_electrons + j;
-  if (!(a.claim[b >> 5] & (1u << (b & 31)))) {
-    const int q = atomicAdd(&a.pair_counts[1], 1);
-    a.pair_sec[q] = j;
+  const PopCounts pc = pop_counts(a);
+  const int m = pc.n_sec - pc.n_att;
+  GRID_STRIDE(j, m) {
+    const int r = a.removed[j];
+    if (r >= 0 && r < a.n_electrons) {
+      const int q = atomicAdd(&a.pair_counts[0], 1);
+      a.pair_slot[q] = r;
+    } else if (r >= a.n_electrons) {
+      // a removed secondary: its energy leaves the ensemble
+      add_growth(a.growth, -(double)a.sec[2 * (r - a.n_electrons) + 1].w);
+    }
+    // secondary j survives when its pool bit was not claimed
+    const int b = a.n_electrons + j;
+    if (!(a.claim[b >> 5] & (1u << (b & 31)))) {
+      const int q = atomicAdd(&a.pair_counts[1], 1);
+      a.pair_sec[q] = j;
+    }
   }
 }
 
 __global__ void k_pop_place(PopArgs a) {
-  const int m = a.n_sec - a.n_att;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < min(a.pair_counts[0], a.pair_counts[1])) {
+  const int np = min(a.pair_counts[0], a.pair_counts[1]);
+  GRID_STRIDE(q, np) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
     const float4 B = a.state[2 * slot + 1];
@@ -569,11 +601,12 @@ __global__ void k_pop_place(PopArgs a) {
 }
 
 __global__ void k_pop_unclaim(PopArgs a) {
-  const int m = a.n_sec - a.n_att;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
-  const int r = a.removed[j];
-  if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
+  const PopCounts pc = pop_counts(a);
+  const int m = pc.n_sec - pc.n_att;
+  GRID_STRIDE(j, m) {
+    const int r = a.removed[j];
+    if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
+  }
 }
 
 // --------------------------------------------------------------- replay
@@ -628,11 +661,16 @@ inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; 
 }  // namespace
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
-  if (a.n <= 0) return;
-  // persistent grid: at most kAdvanceBlocksPerSM blocks per SM, fewer when
-  // the electrons do not fill them (one chunk per warp)
-  const int warps_needed = (a.n + kChunk - 1) / kChunk;
-  const int grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
+  int grid;
+  if (a.grid_blocks > 0) {
+    grid = a.grid_blocks;
+  } else {
+    if (a.n <= 0) return;
+    // persistent grid: at most kAdvanceBlocksPerSM blocks per SM, fewer when
+    // the electrons do not fill them (one chunk per warp)
+    const int warps_needed = (a.n + kChunk - 1) / kChunk;
+    grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
+  }
   switch (a.field.mode) {
     case kFieldDC: k_advance<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
     case kFieldAC: k_advance<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
@@ -665,6 +703,17 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
 }
 
 void launch_pop_control(const PopArgs& a, cudaStream_t s) {
+  if (a.grid_blocks > 0) {
+    // counts live on the device: fixed grids, every kernel strides over its count
+    const int g = a.grid_blocks;
+    k_pop_fill<<<g, 256, 0, s>>>(a);
+    k_pop_clone<<<g, 256, 0, s>>>(a);
+    k_pop_claim<<<g, 256, 0, s>>>(a);
+    k_pop_pair<<<g, 256, 0, s>>>(a);
+    k_pop_place<<<g, 256, 0, s>>>(a);
+    k_pop_unclaim<<<g, 256, 0, s>>>(a);
+    return;
+  }
   const int k = a.n_att < a.n_sec ? a.n_att : a.n_sec;
   if (k > 0) k_pop_fill<<<blocks_for(k, 128), 128, 0, s>>>(a);
   if (a.n_att > a.n_sec) k_pop_clone<<<blocks_for(a.n_att - a.n_sec, 128), 128, 0, s>>>(a);

@@ -50,6 +50,9 @@ struct AdvanceArgs {
   int* error_flag;                 // 2: secondary buffer full, 3: collision budget exhausted
   int* work_counter;               // chunk counter of the persistent grid (zero before the launch)
   int sm_count;
+  const IntervalCtl* ctl;          // when set: per-interval values are read from here
+  const int* n_dev;                // when set: the electron count is read from here (pending lists)
+  int grid_blocks;                 // when > 0: fixed grid size (launches whose count lives on the device)
 };
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);
@@ -136,6 +139,10 @@ struct PopArgs {
   uint64_t seed, interval;
   uint32_t salt;
   int* error_flag;                 // set when a bounded retry loop gives up
+  const int* n_sec_dev;            // when set: counts are read from the device and the
+  const int* n_att_dev;            //   launches use a fixed grid (graph capture)
+  const IntervalCtl* ctl;          // when set: the interval index is read from here
+  int grid_blocks;
 };
 void launch_pop_control(const PopArgs& a, cudaStream_t s);
 

@@ -75,6 +75,18 @@ struct Consts {
   int G;
 };
 
+// Per-interval parameters, written by the host into device memory before each
+// synchronisation interval so that one captured CUDA graph serves every interval.
+struct IntervalCtl {
+  float dt_sync;          // interval length (s)
+  float phi0;             // phase at the interval start (rad), reduced in FP64 on the host
+  float phase_rate;       // w (AC, AC+B) or W (resonance)
+  float nu;               // trial collision frequency (1/s)
+  float inv_step;         // 1 / table energy step (1/eV)
+  float shift_x, shift_y, shift_z;  // origin shift subtracted from every position on load
+  unsigned long long interval;      // interval index (random-number counter)
+};
+
 // Per-block tallies written by the advance kernels (reduced on the device).
 struct StepTally {
   unsigned long long null_count;

@@ -1,0 +1,91 @@
+"""GPU statistical parity: full solves against seeded FP64 solves of the
+reference built from its own sources (tests/golden/stats_*.json, made by
+tests/golden/make_golden.py --stats with 1e4 electrons).
+
+The GPU solve uses the reference's own parsed inputs (the per-process arrays
+of the matching kin_*.npz), the same numerics keys and 1e5 electrons. Every
+swarm parameter the reference pins (mean energy, flux and bulk drift velocity,
+flux and bulk diffusion along the axes) must agree within three combined
+standard errors (50-block batch means of both runs, BoltzmannMC.C:1484-1726)
+plus a 0.2% allowance for FP32 rounding; components the reference cannot
+resolve (below five of its standard errors) are skipped. Rate coefficients
+of processes with at least 2000 reference counts agree within three combined
+Poisson errors doubled for autocorrelation, plus 1%.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import golden_util as gu
+
+pytestmark = pytest.mark.gpu
+KB_EV = 1.38064852e-23 / 1.6021766208e-19
+CASES = sorted(os.path.basename(p)[6:-5] for p in glob.glob(os.path.join(gu.GOLDEN, "stats_*.json")))
+META = {"atomic": dict(N=3.22e22, red_field=100.0), "n2": dict(N=3.22e22, red_field=200.0),
+        "mix": dict(N=3.22e22, red_field=100.0)}
+GAS_TEMP = {"false": 0, "true": 1, "smartActivation": 2}
+
+
+def run_gpu(rec, n_electrons=100_000):
+    from lokigpu import capi
+
+    g = gu.load(rec["case"])
+    arrays = gu.proc_arrays(g)
+    ps = gu.processes(arrays)
+    meta = dict(META[rec["case"]], **rec["overrides"])
+    num = rec["numerics"]
+    cfg = capi.default_config(n_electrons=float(n_electrons), n_interp=int(num.get("nInterpPoints", 2000)),
+                              seed=4242, init_temp_ratio=1.0 / (KB_EV * 300.0),
+                              gas_temperature_effect=GAS_TEMP[meta.get("gas_temp", "false")],
+                              req_integration_points=float(num["nIntegrationPoints"]),
+                              max_coll_before_ss=float(num["maxCollisionsBeforeSteadyState"]),
+                              n_phases=int(num.get("nIntegrationPhases", 100)), max_seconds=600.0)
+    ctx = capi.Context(cfg)
+    ctx.set_processes(ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
+    ctx.set_conditions(meta["N"], 300.0, meta["red_field"], meta.get("angle", 180.0), meta.get("freq", 0.0),
+                       meta.get("red_mag", 0.0))
+    r = ctx.solve()
+    counts, rate, _, _ = ctx.process_results()
+    ctx.close()
+    return r, counts, rate, ps
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_swarm_parameters_match_reference(name):
+    with open(os.path.join(gu.GOLDEN, f"stats_{name}.json")) as f:
+        rec = json.load(f)
+    ref = np.array(rec["result"])
+    r, counts, rate, ps = run_gpu(rec)
+    assert r.capped == 0 and r.integration_points >= rec["numerics"]["nIntegrationPoints"] - 1
+    pairs = [("mean energy", r.mean_energy, r.mean_energy_err, ref[0], ref[1])]
+    for k in range(3):
+        pairs += [(f"flux v[{k}]", r.flux_v[k], r.flux_v_err[k], ref[2 + k], ref[5 + k]),
+                  (f"flux D[{k}{k}]", r.flux_d[4 * k], r.flux_d_err[4 * k], ref[8 + k], ref[11 + k]),
+                  (f"bulk v[{k}]", r.bulk_v[k], r.bulk_v_err[k], ref[14 + k], ref[17 + k]),
+                  (f"bulk D[{k}{k}]", r.bulk_d[4 * k], r.bulk_d_err[4 * k], ref[20 + k], ref[23 + k])]
+    failures, checked = [], 0
+    for label, gv, ge, rv, re in pairs:
+        if abs(rv) < 5.0 * re:
+            continue
+        checked += 1
+        tol = 3.0 * np.hypot(ge, re) + 2e-3 * abs(rv)
+        if abs(gv - rv) > tol:
+            failures.append(f"{label}: gpu {gv:.6g} +- {ge:.3g}, reference {rv:.6g} +- {re:.3g}")
+    assert checked >= 4, name
+    # rate coefficients (BoltzmannMC.C:1627-1638)
+    ref_rate = np.array(rec["rate"])
+    t_int = ref[31] - ref[30]
+    n_ref = float(rec["n_electrons"])
+    for p in range(ps.n):
+        if ref_rate[p] <= 0 or ps.rel_dens[p] <= 0:
+            continue
+        c_ref = ref_rate[p] * t_int * n_ref * ps.rel_dens[p] * META[rec["case"]]["N"]
+        if c_ref < 2000 or counts[p] < 2000:
+            continue
+        rel = 2.0 * 3.0 * np.sqrt(1.0 / c_ref + 1.0 / counts[p]) + 0.01
+        if abs(rate[p] / ref_rate[p] - 1.0) > rel:
+            failures.append(f"rate[{p}]: gpu {rate[p]:.6g}, reference {ref_rate[p]:.6g} (counts {counts[p]}, {c_ref:.0f})")
+    assert not failures, "\n".join(failures)
