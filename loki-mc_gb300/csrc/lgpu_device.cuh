@@ -409,9 +409,47 @@ __device__ __forceinline__ void row_weights(float eos, int M, int& i1, float& w1
   w2 = 1.0f - w1;
 }
 
+// Index of the first cumulative value >= x in one table row, i.e. the result
+// of the reference's bisection (BoltzmannMC.C:1066-1088), which returns the
+// smallest p with C_p >= x (or P-1). Instead of a chain of dependent loads it
+// counts the entries below x with independent 16-byte loads: the whole row
+// for up to 64 processes, otherwise every 16th entry first and then the 16
+// entries of the selected block.
+__device__ __forceinline__ int row_count_below(const float2* row, int P, int stride, float w1, float w2, float x) {
+  const float4* r4 = reinterpret_cast<const float4*>(row);
+  int cnt = 0;
+  if (P <= 64) {
+#pragma unroll 8
+    for (int q = 0; q < (stride >> 1); ++q) {
+      const float4 c = __ldg(&r4[q]);
+      cnt += (w1 * c.x + w2 * c.y < x) + (w1 * c.z + w2 * c.w < x);
+    }
+  } else {
+    const int nb = (P + 15) >> 4;
+    int blk = 0;
+#pragma unroll 4
+    for (int b = 0; b < nb; ++b) {
+      const int last = min((b << 4) + 15, P - 1);
+      const float2 c = __ldg(&row[last]);
+      blk += (w1 * c.x + w2 * c.y < x);
+    }
+    blk = min(blk, nb - 1);
+    cnt = blk << 4;
+    const float4* b4 = r4 + (blk << 3);
+    const int nq = min(8, (stride >> 1) - (blk << 3));
+#pragma unroll 8
+    for (int q = 0; q < nq; ++q) {
+      const float4 c = __ldg(&b4[q]);
+      cnt += (w1 * c.x + w2 * c.y < x) + (w1 * c.z + w2 * c.w < x);
+    }
+  }
+  return min(cnt, P - 1);
+}
+
 // Process choice for a cold gas (BoltzmannMC.C:1033-1097): null test on the
-// interpolated total frequency, bisection over the interpolated cumulative
-// sums, backward skip of zero-rate processes. Returns -1 for null.
+// interpolated total frequency, the first interpolated cumulative sum that
+// reaches the random number, backward skip of zero-rate processes. Returns -1
+// for null.
 template <class Rng>
 __device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, float energy, float speed, Rng& rng) {
   const float r = nu_trial * rng.oc();
@@ -421,18 +459,8 @@ __device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, flo
   const float2 nt = __ldg(&t.nu_pair[i1]);
   if (r > w1 * nt.x + w2 * nt.y) return -1;
   const float rcs = r * t.inv_N / speed;
-  const float2* cum = t.cum_pair + (size_t)i1 * t.P;
-  int L = 0, R = t.P - 1, chosen = -1;
-  while (L != R) {
-    const int m = (L + R) >> 1;
-    const float2 c2 = __ldg(&cum[m]);
-    const float tvl = w1 * c2.x + w2 * c2.y;
-    if (rcs < tvl) R = m;
-    else if (rcs > tvl) L = m + 1;
-    else { chosen = m; break; }
-  }
-  if (L == R) chosen = L;
-  const float2* sig = t.sig_pair + (size_t)i1 * t.P;
+  int chosen = row_count_below(t.cum_pair + (size_t)i1 * t.stride, t.P, t.stride, w1, w2, rcs);
+  const float2* sig = t.sig_pair + (size_t)i1 * t.stride;
   while (chosen > 0) {
     const float2 s2 = __ldg(&sig[chosen]);
     if (!(w1 * s2.x == 0.0f && w2 * s2.y == 0.0f)) break;
@@ -473,7 +501,7 @@ __device__ __forceinline__ int choose_thermal(const TablesF& t, const GasF* gase
     // BoltzmannMC.C:959-967: the weight is 0 or 1
     const float w1 = ((float)i2 - reos < 0.0f) ? 0.0f : 1.0f;
     const float w2 = 1.0f - w1;
-    const float2* cum = t.cum_pair + (size_t)i1 * t.P;
+    const float2* cum = t.cum_pair + (size_t)i1 * t.stride;
     float ref = 0.0f;
     if (L > 0) {
       const float2 c2 = __ldg(&cum[L - 1]);
@@ -494,7 +522,7 @@ __device__ __forceinline__ int choose_thermal(const TablesF& t, const GasF* gase
       else { chosen = m; break; }
     }
     if (L == R) chosen = L;
-    const float2* sig = t.sig_pair + (size_t)i1 * t.P;
+    const float2* sig = t.sig_pair + (size_t)i1 * t.stride;
     while (chosen > 0) {
       const float2 s2 = __ldg(&sig[chosen]);
       if (!(w1 * s2.x == 0.0f && w2 * s2.y == 0.0f)) break;

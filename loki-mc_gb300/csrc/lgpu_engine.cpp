@@ -247,8 +247,9 @@ class Engine {
     if (d_cum_pair_) cudaFree(d_cum_pair_);
     if (d_sig_pair_) cudaFree(d_sig_pair_);
     d_cum_pair_ = d_sig_pair_ = nullptr;
-    LGPU_TRY(dalloc(&d_cum_pair_, (size_t)M_ * nP));
-    LGPU_TRY(dalloc(&d_sig_pair_, (size_t)M_ * nP));
+    stride_ = (nP + 1) & ~1;
+    LGPU_TRY(dalloc(&d_cum_pair_, (size_t)M_ * stride_));
+    LGPU_TRY(dalloc(&d_sig_pair_, (size_t)M_ * stride_));
     for (auto** d : {&d_proc_gain_, &d_proc_loss_}) {
       if (*d) cudaFree(*d);
       *d = nullptr;
@@ -381,6 +382,7 @@ class Engine {
     t.sig_pair = d_sig_pair_;
     t.M = M_;
     t.P = P_;
+    t.stride = stride_;
     t.inv_step = (float)(1.0 / step_);
     t.inv_N = (float)(1.0 / Ngas_);
     return t;
@@ -395,6 +397,7 @@ class Engine {
     TableBuildArgs a{};
     a.M = M_;
     a.P = P_;
+    a.stride = stride_;
     a.step = step_;
     a.N = Ngas_;
     a.is_super = d_is_super_;
@@ -600,7 +603,6 @@ class Engine {
   // pending, with every count read on the device.
   void enqueue_pop_round(uint32_t round) {
     cudaMemsetAsync(&d_sc_->pend_count, 0, sizeof(int), stream_);
-    cudaMemsetAsync(d_sc_->pair_counts, 0, 2 * sizeof(int), stream_);
     launch_pop_control(pop_args(round), stream_);
     cudaMemsetAsync(&d_sc_->sec_count, 0, 2 * sizeof(int), stream_);  // sec_count, att_count
     cudaMemsetAsync(&d_sc_->work_counter, 0, sizeof(int), stream_);
@@ -608,9 +610,9 @@ class Engine {
     b.list = d_pend_list_;
     b.n_dev = &d_sc_->pend_count;
     b.salt = round;
-    b.grid_blocks = sm_count_;
+    b.grid_blocks = std::max(1, sm_count_ / 8);
     launch_advance(b, stream_);
-    launches_ += 7;
+    launches_ += 2;
   }
 
   // The device work of one interval: the advance of every electron, two
@@ -1323,22 +1325,24 @@ class Engine {
     LGPU_TRY(build_tables(max_energy));
     if (nu_tot) LGPU_CU(copy(nu_tot, d_nu_tot_, M_ * sizeof(double), cudaMemcpyDeviceToHost));
     if (nu_max) std::copy(h_nu_max_.begin(), h_nu_max_.end(), nu_max);
-    std::vector<float2> pairs((size_t)M_ * P_);
+    std::vector<float2> pairs((size_t)M_ * stride_);
     if (sig) {
       LGPU_CU(copy(pairs.data(), d_sig_pair_, pairs.size() * sizeof(float2), cudaMemcpyDeviceToHost));
       LGPU_TRY(sync("tables_out"));
-      for (size_t k = 0; k < pairs.size(); ++k) sig[k] = pairs[k].x;
+      for (int i = 0; i < M_; ++i)
+        for (int p = 0; p < P_; ++p) sig[(size_t)i * P_ + p] = pairs[(size_t)i * stride_ + p].x;
     }
     if (cum) {
       LGPU_CU(copy(pairs.data(), d_cum_pair_, pairs.size() * sizeof(float2), cudaMemcpyDeviceToHost));
       LGPU_TRY(sync("tables_out"));
-      for (size_t k = 0; k < pairs.size(); ++k) cum[k] = pairs[k].x;
+      for (int i = 0; i < M_; ++i)
+        for (int p = 0; p < P_; ++p) cum[(size_t)i * P_ + p] = pairs[(size_t)i * stride_ + p].x;
     }
     return sync("tables_out");
   }
 
   // ------------------------------------------------------------ state
-  int N_ = 0, P_ = 0, M_ = 0, sec_cap_ = 0, sm_count_ = 1;
+  int N_ = 0, P_ = 0, M_ = 0, sec_cap_ = 0, sm_count_ = 1, stride_ = 2;
   size_t claim_words_ = 0;
   std::vector<lgpu_process> procs_;
   std::vector<lgpu_gas> gases_;

@@ -67,7 +67,7 @@ constexpr int kChunk = 128;  // electrons a warp takes from the global work coun
 // so the lanes of a warp stay busy although the number of collisions per
 // electron and interval is random (Poisson-distributed).
 template <int MODE>
-__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance(AdvanceArgs a) {
+__device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   __shared__ unsigned int s_count[kMaxProcesses];
   __shared__ float s_gain[kMaxProcesses];
   __shared__ float s_loss[kMaxProcesses];
@@ -267,6 +267,17 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
   }
 }
 
+// the main pass over every electron and the pass over the pending list carry
+// different names so that profiles can tell them apart
+template <int MODE>
+__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance(AdvanceArgs a) {
+  advance_body<MODE>(a);
+}
+template <int MODE>
+__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance_pending(AdvanceArgs a) {
+  advance_body<MODE>(a);
+}
+
 // ------------------------------------------------------------------ init
 __global__ void k_init(InitArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -321,20 +332,26 @@ __global__ void k_build_tables(TableBuildArgs a) {
       value = __dmul_rn(interp_raw(a.raw_e + a.raw_off[p], a.raw_v + a.raw_off[p], a.raw_len[p], energy), a.rel_dens[p]);
     }
     cur = __dadd_rn(cur, value);
-    const size_t k = (size_t)i * P + p;
-    if (a.sig64) a.sig64[k] = value;
-    if (a.cum64) a.cum64[k] = cur;
+    if (a.sig64) a.sig64[(size_t)i * P + p] = value;
+    if (a.cum64) a.cum64[(size_t)i * P + p] = cur;
+    const size_t k = (size_t)i * a.stride + p;
     const float vf = (float)value, cf = (float)cur;
     a.sig_pair[k].x = vf;
     a.cum_pair[k].x = cf;
     if (i > 0) {
-      a.sig_pair[k - P].y = vf;
-      a.cum_pair[k - P].y = cf;
+      a.sig_pair[k - a.stride].y = vf;
+      a.cum_pair[k - a.stride].y = cf;
     }
     if (i == a.M - 1) {
       a.sig_pair[k].y = vf;
       a.cum_pair[k].y = cf;
     }
+  }
+  // row padding: a cumulative value no random number reaches, zero rate
+  for (int p = P; p < a.stride; ++p) {
+    const size_t k = (size_t)i * a.stride + p;
+    a.cum_pair[k] = make_float2(3.0e38f, 3.0e38f);
+    a.sig_pair[k] = make_float2(0.0f, 0.0f);
   }
   const double kq = 1.6021766208e-19, km = 9.10938356e-31;
   const double nu = __dmul_rn(cur, __dmul_rn(a.N, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(energy, 2.0), kq), km))));
@@ -498,13 +515,12 @@ __device__ __forceinline__ PopCounts pop_counts(const PopArgs& a) {
   c.interval = a.ctl ? a.ctl->interval : a.interval;
   return c;
 }
-#define GRID_STRIDE(j, n) for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < (n); j += gridDim.x * blockDim.x)
+#define THREAD_STRIDE(j, n) for (int j = tid; j < (n); j += nthreads)
 
 // (1) attached slots take secondaries, last secondary first (BoltzmannMC.C:1344-1359)
-__global__ void k_pop_fill(PopArgs a) {
-  const PopCounts pc = pop_counts(a);
+__device__ void pop_fill(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
   const int k = min(pc.n_att, pc.n_sec);
-  GRID_STRIDE(j, k) {
+  THREAD_STRIDE(j, k) {
     const int slot = a.att_list[j];
     const int sidx = pc.n_sec - 1 - j;
     const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
@@ -516,9 +532,8 @@ __global__ void k_pop_fill(PopArgs a) {
 
 // (2) remaining attached slots clone a random surviving electron
 // (BoltzmannMC.C:1360-1376); the energy-growth term gains its energy.
-__global__ void k_pop_clone(PopArgs a) {
-  const PopCounts pc = pop_counts(a);
-  GRID_STRIDE(jj, pc.n_att - pc.n_sec) {
+__device__ void pop_clone(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
+  THREAD_STRIDE(jj, pc.n_att - pc.n_sec) {
     const int j = pc.n_sec + jj;
     const int dest = a.att_list[j];
     int src = -1;
@@ -545,11 +560,10 @@ __global__ void k_pop_clone(PopArgs a) {
 // (3) excess secondaries: remove a uniformly random subset of size m from the
 // pool of n_electrons slots + m unplaced secondaries, the outcome of the
 // reference's sequential uniform removal (BoltzmannMC.C:1379-1407).
-__global__ void k_pop_claim(PopArgs a) {
-  const PopCounts pc = pop_counts(a);
+__device__ void pop_claim(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
   const int m = pc.n_sec - pc.n_att;
   const int pool = a.n_electrons + m;
-  GRID_STRIDE(j, m) {
+  THREAD_STRIDE(j, m) {
     int got = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
       const int r = uniform_index(pop_word((uint32_t)j, pc.interval, a.seed, a.salt ^ 0x55u, d), pool);
@@ -565,13 +579,12 @@ __global__ void k_pop_claim(PopArgs a) {
   }
 }
 
-__global__ void k_pop_pair(PopArgs a) {
-  const PopCounts pc = pop_counts(a);
+__device__ void pop_pair(const PopArgs& a, const PopCounts& pc, int* pair_counts, int tid, int nthreads) {
   const int m = pc.n_sec - pc.n_att;
-  GRID_STRIDE(j, m) {
+  THREAD_STRIDE(j, m) {
     const int r = a.removed[j];
     if (r >= 0 && r < a.n_electrons) {
-      const int q = atomicAdd(&a.pair_counts[0], 1);
+      const int q = atomicAdd(&pair_counts[0], 1);
       a.pair_slot[q] = r;
     } else if (r >= a.n_electrons) {
       // a removed secondary: its energy leaves the ensemble
@@ -580,15 +593,14 @@ __global__ void k_pop_pair(PopArgs a) {
     // secondary j survives when its pool bit was not claimed
     const int b = a.n_electrons + j;
     if (!(a.claim[b >> 5] & (1u << (b & 31)))) {
-      const int q = atomicAdd(&a.pair_counts[1], 1);
+      const int q = atomicAdd(&pair_counts[1], 1);
       a.pair_sec[q] = j;
     }
   }
 }
 
-__global__ void k_pop_place(PopArgs a) {
-  const int np = min(a.pair_counts[0], a.pair_counts[1]);
-  GRID_STRIDE(q, np) {
+__device__ void pop_place(const PopArgs& a, int np, int tid, int nthreads) {
+  THREAD_STRIDE(q, np) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
     const float4 B = a.state[2 * slot + 1];
@@ -600,13 +612,42 @@ __global__ void k_pop_place(PopArgs a) {
   }
 }
 
-__global__ void k_pop_unclaim(PopArgs a) {
-  const PopCounts pc = pop_counts(a);
+__device__ void pop_unclaim(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
   const int m = pc.n_sec - pc.n_att;
-  GRID_STRIDE(j, m) {
+  THREAD_STRIDE(j, m) {
     const int r = a.removed[j];
     if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
   }
+}
+
+// multi-kernel form (large counts known on the host)
+#define GRID_TID (blockIdx.x * blockDim.x + threadIdx.x), (gridDim.x * blockDim.x)
+__global__ void k_pop_fill(PopArgs a) { pop_fill(a, pop_counts(a), GRID_TID); }
+__global__ void k_pop_clone(PopArgs a) { pop_clone(a, pop_counts(a), GRID_TID); }
+__global__ void k_pop_claim(PopArgs a) { pop_claim(a, pop_counts(a), GRID_TID); }
+__global__ void k_pop_pair(PopArgs a) { pop_pair(a, pop_counts(a), a.pair_counts, GRID_TID); }
+__global__ void k_pop_place(PopArgs a) { pop_place(a, min(a.pair_counts[0], a.pair_counts[1]), GRID_TID); }
+__global__ void k_pop_unclaim(PopArgs a) { pop_unclaim(a, pop_counts(a), GRID_TID); }
+
+// single-block form: every phase in one launch, separated by block barriers
+// (counts read on the device; used inside the captured interval)
+constexpr int kPopThreads = 1024;
+__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
+  __shared__ int s_pairs[2];
+  const PopCounts pc = pop_counts(a);
+  if (pc.n_sec == 0 && pc.n_att == 0) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid < 2) s_pairs[tid] = 0;
+  pop_fill(a, pc, tid, nt);
+  __syncthreads();
+  pop_clone(a, pc, tid, nt);
+  pop_claim(a, pc, tid, nt);
+  __syncthreads();
+  pop_pair(a, pc, s_pairs, tid, nt);
+  __syncthreads();
+  pop_place(a, min(s_pairs[0], s_pairs[1]), tid, nt);
+  __syncthreads();
+  pop_unclaim(a, pc, tid, nt);
 }
 
 // --------------------------------------------------------------- replay
@@ -671,13 +712,20 @@ void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
     const int warps_needed = (a.n + kChunk - 1) / kChunk;
     grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
   }
-  switch (a.field.mode) {
-    case kFieldDC: k_advance<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
-    case kFieldAC: k_advance<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;
-    case kFieldB: k_advance<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(a); break;
-    case kFieldECR: k_advance<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(a); break;
-    default: k_advance<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(a); break;
+#define LGPU_ADVANCE(K)                                          \
+  switch (a.field.mode) {                                        \
+    case kFieldDC: K<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;   \
+    case kFieldAC: K<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;   \
+    case kFieldB: K<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(a); break;     \
+    case kFieldECR: K<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(a); break; \
+    default: K<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(a); break;       \
   }
+  if (a.list) {
+    LGPU_ADVANCE(k_advance_pending)
+  } else {
+    LGPU_ADVANCE(k_advance)
+  }
+#undef LGPU_ADVANCE
 }
 
 void launch_init(const InitArgs& a, cudaStream_t s) {
@@ -704,14 +752,8 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
 
 void launch_pop_control(const PopArgs& a, cudaStream_t s) {
   if (a.grid_blocks > 0) {
-    // counts live on the device: fixed grids, every kernel strides over its count
-    const int g = a.grid_blocks;
-    k_pop_fill<<<g, 256, 0, s>>>(a);
-    k_pop_clone<<<g, 256, 0, s>>>(a);
-    k_pop_claim<<<g, 256, 0, s>>>(a);
-    k_pop_pair<<<g, 256, 0, s>>>(a);
-    k_pop_place<<<g, 256, 0, s>>>(a);
-    k_pop_unclaim<<<g, 256, 0, s>>>(a);
+    // counts live on the device: one block runs every phase
+    k_pop_all<<<1, kPopThreads, 0, s>>>(a);
     return;
   }
   const int k = a.n_att < a.n_sec ? a.n_att : a.n_sec;

@@ -69,7 +69,7 @@ void launch_init(const InitArgs& a, cudaStream_t s);
 
 // Table build on the device in FP64 (BoltzmannMC.C:561-615).
 struct TableBuildArgs {
-  int M, P;
+  int M, P, stride;
   double step, N;
   const int* is_super;
   const double* superw;

@@ -59,6 +59,7 @@ struct TablesF {
   const float2* cum_pair;  // [M*P] cumulative sigma*n
   const float2* sig_pair;  // [M*P] sigma*n
   int M, P;
+  int stride;              // row stride in pairs: P rounded up to even (16-byte rows), padded with +inf / 0
   float inv_step;          // 1 / energy step (1/eV)
   float inv_N;             // 1 / gas density
 };
