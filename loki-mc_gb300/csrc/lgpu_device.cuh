@@ -85,6 +85,32 @@ struct PhiloxStream {
   __device__ __forceinline__ float cc() { return u01_oc(word()); }
 };
 
+// The per-electron stream of the advance kernels: PCG32 (XSH-RR output of a
+// 64-bit LCG, O'Neill 2014), seeded for each (electron, interval, pass) by one
+// Philox4x32-10 block, so results stay reproducible from the run seed while
+// each uniform costs a handful of integer instructions and no divergent
+// buffer refills.
+struct PcgStream {
+  uint64_t state, inc;
+  __device__ __forceinline__ void init(uint32_t electron, uint64_t interval, uint64_t seed, uint32_t salt) {
+    Philox ph;
+    ph.ctr = make_uint4(electron, (uint32_t)interval, (uint32_t)(interval >> 32) ^ (salt << 16), 0x5EEDu);
+    ph.key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint4 w = ph.next();
+    state = ((uint64_t)w.x << 32) | w.y;
+    inc = ((((uint64_t)w.z << 32) | w.w) << 1) | 1ull;
+  }
+  __device__ __forceinline__ uint32_t word() {
+    const uint64_t old = state;
+    state = old * 6364136223846793005ull + inc;
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    return __funnelshift_r(xs, xs, (uint32_t)(old >> 59));
+  }
+  __device__ __forceinline__ float oc() { return u01_oc(word()); }
+  __device__ __forceinline__ float oo() { return u01_oo(word()); }
+  __device__ __forceinline__ float cc() { return u01_oc(word()); }
+};
+
 // Replay of recorded uniforms (parity tests): values are taken in order.
 struct ReplayStream {
   const double* u;

@@ -3,8 +3,8 @@
 //
 // The runtime owns the device state of one swarm condition and drives the
 // kernels through the reference's control flow: per synchronisation interval
-// the trial-frequency check, one advance launch, population control and the
-// pending rounds; per sample the ensemble moments, steady-state detection,
+// the trial-frequency check, one advance launch (ensemble and secondaries) and
+// population control; per sample the ensemble moments, steady-state detection,
 // error control and distribution tallies; at the end the time averages. The
 // control flow and the FP64 bookkeeping restate Code/LoKI-MC/Sources/BoltzmannMC.C
 // (line numbers cited per routine).
@@ -31,7 +31,6 @@ constexpr double kMeD = 9.10938356e-31;    // Constant.h:8
 constexpr double kKbD = 1.38064852e-23;    // Constant.h:6
 constexpr double kNonDef = -123456789.0;   // Constant.h:23
 constexpr double kPi = 3.14159265358979323846;
-constexpr uint32_t kGraphPopRounds = 2;  // population-control rounds inside the captured interval
 
 struct Kahan {
   double s = 0, c = 0;
@@ -46,14 +45,14 @@ struct Kahan {
 // Device scalars read back after a launch sequence.
 // Per-interval fields first (cleared before every interval), cumulative after.
 struct DevScalars {
-  int sec_count, att_count, pend_count, error_flag;
-  int pair_counts[2];
+  int sec_count, att_count, sec_next, error_flag;
   unsigned int max_energy_bits;
   int work_counter;
   unsigned long long null_count;
   unsigned long long real_count;
   double field_gain;
   double growth;
+  double time_adjust;   // electron-time beyond N x interval: + secondaries, - attachments (s)
   unsigned int sample_max_bits;
   int pad2;
   double moments[kMoments];
@@ -132,8 +131,7 @@ class Engine {
     N_ = (int)cfg_.n_electrons;
     sec_cap_ = std::max(N_, 4096);
     LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
-    LGPU_TRY(dalloc(&d_pend_t_, (size_t)N_));
-    LGPU_TRY(dalloc(&d_pend_list_, (size_t)N_));
+    LGPU_TRY(dalloc(&d_alive_, (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_sec_, 2 * (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_att_, (size_t)N_));
     claim_words_ = ((size_t)N_ + sec_cap_ + 31) / 32;
@@ -147,7 +145,6 @@ class Engine {
     LGPU_CU(cudaMallocHost((void**)&h_ctl_, sizeof(IntervalCtl)));
     std::memset(h_ctl_, 0, sizeof(IntervalCtl));
     LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
-    LGPU_CU(cudaMemsetAsync(d_pend_t_, 0xFF, (size_t)N_ * sizeof(float), stream_));  // NaN: not pending
     LGPU_CU(cudaMemsetAsync(d_sc_, 0, sizeof(DevScalars), stream_));
     M_ = cfg_.n_interp;
     LGPU_TRY(dalloc(&d_nu_pair_, (size_t)M_));
@@ -169,7 +166,7 @@ class Engine {
     if (h_ctl_) cudaFreeHost(h_ctl_);
     d_ctl_ = nullptr;
     h_ctl_ = nullptr;
-    void* ptrs[] = {d_state_, d_pend_t_, d_pend_list_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
+    void* ptrs[] = {d_state_, d_alive_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
                     d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_cum_pair_, d_sig_pair_, d_procf_,
                     d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
                     d_raw_e_, d_raw_v_, d_proc_count_, d_proc_gain_, d_proc_loss_, d_eedf_, d_eedf_per_, d_eadf_,
@@ -475,7 +472,6 @@ class Engine {
     origin_[0] = origin_[1] = origin_[2] = 0;
     shift_[0] = shift_[1] = shift_[2] = 0;
     LGPU_CU(cudaMemsetAsync(d_sc_, 0, sizeof(DevScalars), stream_));
-    LGPU_CU(cudaMemsetAsync(d_pend_t_, 0xFF, (size_t)N_ * sizeof(float), stream_));
     InitArgs ia{};
     ia.state = d_state_;
     ia.n = N_;
@@ -507,7 +503,7 @@ class Engine {
     base_proc_gain_.assign(P_, 0.0);
     base_proc_loss_.assign(P_, 0.0);
     base_null_ = 0;
-    base_field_gain_ = base_growth_ = 0;
+    base_field_gain_ = base_growth_ = base_time_adjust_ = 0;
     // series
     ts_.clear();
     me_.clear();
@@ -546,7 +542,7 @@ class Engine {
   AdvanceArgs advance_args() const {
     AdvanceArgs a{};
     a.state = d_state_;
-    a.pend_t = d_pend_t_;
+    a.n = N_;
     a.seed = cfg_.seed;
     a.field = field_;
     a.c = consts();
@@ -556,6 +552,7 @@ class Engine {
     a.P = P_;
     a.sec = d_sec_;
     a.sec_count = &d_sc_->sec_count;
+    a.sec_next = &d_sc_->sec_next;
     a.sec_cap = sec_cap_;
     a.att_list = d_att_;
     a.att_count = &d_sc_->att_count;
@@ -565,6 +562,7 @@ class Engine {
     a.null_count = &d_sc_->null_count;
     a.real_count = &d_sc_->real_count;
     a.field_gain = &d_sc_->field_gain;
+    a.time_adjust = &d_sc_->time_adjust;
     a.max_energy_bits = &d_sc_->max_energy_bits;
     a.error_flag = &d_sc_->error_flag;
     a.work_counter = &d_sc_->work_counter;
@@ -573,62 +571,46 @@ class Engine {
     return a;
   }
 
-  PopArgs pop_args(uint32_t round) const {
+  PopArgs pop_args() const {
     PopArgs p{};
     p.state = d_state_;
     p.n_electrons = N_;
     p.sec = d_sec_;
+    p.sec_count = &d_sc_->sec_count;
     p.att_list = d_att_;
-    p.pend_t = d_pend_t_;
-    p.pend_list = d_pend_list_;
-    p.pend_count = &d_sc_->pend_count;
+    p.att_count = &d_sc_->att_count;
     p.claim = d_claim_;
+    p.alive = d_alive_;
     p.removed = d_removed_;
     p.pair_slot = d_pair_slot_;
     p.pair_sec = d_pair_sec_;
-    p.pair_counts = d_sc_->pair_counts;
     p.growth = &d_sc_->growth;
     p.half_me_over_e = (float)(0.5 * kMeD / kQeD);
     p.seed = cfg_.seed;
-    p.salt = round;
-    p.error_flag = &d_sc_->error_flag;
-    p.n_sec_dev = &d_sc_->sec_count;
-    p.n_att_dev = &d_sc_->att_count;
     p.ctl = d_ctl_;
-    p.grid_blocks = 2 * sm_count_;
+    p.error_flag = &d_sc_->error_flag;
     return p;
   }
 
-  // One population-control round and the advance of the electrons it left
-  // pending, with every count read on the device.
-  void enqueue_pop_round(uint32_t round) {
-    cudaMemsetAsync(&d_sc_->pend_count, 0, sizeof(int), stream_);
-    launch_pop_control(pop_args(round), stream_);
-    cudaMemsetAsync(&d_sc_->sec_count, 0, 2 * sizeof(int), stream_);  // sec_count, att_count
-    cudaMemsetAsync(&d_sc_->work_counter, 0, sizeof(int), stream_);
-    AdvanceArgs b = advance_args();
-    b.list = d_pend_list_;
-    b.n_dev = &d_sc_->pend_count;
-    b.salt = round;
-    b.grid_blocks = std::max(1, sm_count_ / 8);
-    launch_advance(b, stream_);
-    launches_ += 2;
-  }
-
-  // The device work of one interval: the advance of every electron, two
-  // population-control rounds (when the mixture ionizes or attaches), the
-  // ensemble sample and the scalar read-back. Captured once as a CUDA graph.
+  // The device work of one interval: the advance of every electron and of the
+  // secondaries they create, the drain of any secondary left in the queue,
+  // population control (when the mixture ionizes or attaches), the ensemble
+  // sample and the scalar read-back. Captured once as a CUDA graph.
   void enqueue_interval(bool sample) {
     copy(d_ctl_, h_ctl_, sizeof(IntervalCtl), cudaMemcpyHostToDevice);
     cudaMemsetAsync(d_sc_, 0, offsetof(DevScalars, null_count), stream_);
     AdvanceArgs a = advance_args();
-    a.n = N_;
     cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
     launch_advance(a, stream_);
     cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
     ++launches_;
-    if (have_ion_att_)
-      for (uint32_t r = 1; r <= kGraphPopRounds; ++r) enqueue_pop_round(r);
+    if (have_ion_att_) {
+      AdvanceArgs d = a;
+      d.queue_only = 1;
+      launch_advance(d, stream_);
+      launch_pop_control(pop_args(), stream_);
+      launches_ += 2;
+    }
     if (sample) enqueue_sample();
     copy(h_sc_, d_sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost);
   }
@@ -716,23 +698,11 @@ class Engine {
       adv_electron_steps_ += N_;
     }
     LGPU_TRY(check_device_errors());
-    // rounds beyond the captured ones (rare: secondaries of secondaries within
-    // one interval), then a fresh sample
-    bool extra = false;
-    for (uint32_t round = kGraphPopRounds + 1; have_ion_att_ && (h_sc_->sec_count > 0 || h_sc_->att_count > 0);
-         ++round) {
-      if (round > 256) return fail(LGPU_ERR_OVERFLOW, "population control did not settle");
-      if (h_sc_->sec_count > sec_cap_)
-        return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", h_sc_->sec_count, sec_cap_);
-      enqueue_pop_round(round);
-      LGPU_TRY(read_scalars());
-      LGPU_TRY(check_device_errors());
-      extra = true;
-    }
-    if (extra && sample) {
-      enqueue_sample();
-      LGPU_TRY(read_scalars());
-    }
+    if (h_sc_->sec_count > sec_cap_)
+      return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", h_sc_->sec_count, sec_cap_);
+    if (h_sc_->sec_next < h_sc_->sec_count)
+      return fail(LGPU_ERR_OVERFLOW, "secondaries left unadvanced (%d of %d)", h_sc_->sec_count - h_sc_->sec_next,
+                  h_sc_->sec_count);
     {
       float f;
       std::memcpy(&f, &h_sc_->max_energy_bits, 4);
@@ -947,6 +917,7 @@ class Engine {
       base_proc_count_ = cnt;
       base_field_gain_ = h_sc_->field_gain;
       base_growth_ = h_sc_->growth;
+      base_time_adjust_ = h_sc_->time_adjust;
     }
     total_int_time_ = 0;
     // distribution grids (BoltzmannMC.C:1862-1889)
@@ -973,6 +944,15 @@ class Engine {
       mean[c] = n ? m.s / n : NAN;
       err[c] = statistical_error(col.data(), n, 50);
     }
+  }
+
+  // Electron-time simulated since the steady state (s). The reference divides
+  // by nElectrons x totalIntegratedTime (BoltzmannMC.C:1632, 1643-1648); here
+  // secondaries are pushed from their creation time and attached electrons
+  // stop at attachment, so the exact electron-time of the simulation is
+  // N x time plus the time secondaries added minus the time attachments removed.
+  double electron_time() const {
+    return (double)N_ * total_int_time_ + (h_sc_->time_adjust - base_time_adjust_);
   }
 
   // power sums since the steady state (device totals minus the reset values)
@@ -1087,7 +1067,7 @@ class Engine {
     }
     double field, growth;
     power_sums(&field, &growth, nullptr, nullptr);
-    const double denom = (double)N_ * total_int_time_ * Ngas_;
+    const double denom = electron_time() * Ngas_;
     r->power_field = field / denom;
     r->power_growth = growth / denom;
     r->power_balance_rel_err = power_balance();
@@ -1112,13 +1092,13 @@ class Engine {
     LGPU_CU(copy(g.data(), d_proc_gain_, P_ * sizeof(double), cudaMemcpyDeviceToHost));
     LGPU_CU(copy(l.data(), d_proc_loss_, P_ * sizeof(double), cudaMemcpyDeviceToHost));
     LGPU_TRY(sync("process_results"));
-    const double tint = total_int_time_;
+    const double etime = electron_time();
     for (int p = 0; p < P_; ++p) {
       const double c = (double)(cnt[p] - base_proc_count_[p]);
       if (counts) counts[p] = cnt[p] - base_proc_count_[p];
-      // BoltzmannMC.C:1630-1637
-      if (rate) rate[p] = procs_[p].rel_dens != 0 ? c / (tint * N_ * procs_[p].rel_dens * Ngas_) : 0.0;
-      const double denom = (double)N_ * tint * Ngas_;
+      // BoltzmannMC.C:1630-1637, over the simulated electron-time
+      if (rate) rate[p] = procs_[p].rel_dens != 0 ? c / (etime * procs_[p].rel_dens * Ngas_) : 0.0;
+      const double denom = etime * Ngas_;
       if (gain) gain[p] = (g[p] - base_proc_gain_[p]) / denom;
       if (loss) loss[p] = (l[p] - base_proc_loss_[p]) / denom;
     }
@@ -1365,7 +1345,7 @@ class Engine {
   std::vector<unsigned long long> base_proc_count_;
   std::vector<double> base_proc_gain_, base_proc_loss_;
   unsigned long long base_null_ = 0;
-  double base_field_gain_ = 0, base_growth_ = 0;
+  double base_field_gain_ = 0, base_growth_ = 0, base_time_adjust_ = 0;
   double pb_rel_err_ = 0;
   // series
   std::vector<double> ts_, me_, mp_, mv_, fd_, pc_, bv_, bd_;
@@ -1380,8 +1360,7 @@ class Engine {
   long long adv_launches_ = 0, launches_ = 0;
   // device buffers
   float4* d_state_ = nullptr;
-  float* d_pend_t_ = nullptr;
-  int* d_pend_list_ = nullptr;
+  int* d_alive_ = nullptr;
   float4* d_sec_ = nullptr;
   int* d_att_ = nullptr;
   unsigned int* d_claim_ = nullptr;

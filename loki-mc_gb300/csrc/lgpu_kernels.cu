@@ -59,13 +59,28 @@ constexpr int kAdvanceBlocksPerSM = 4;
 constexpr int kChunk = 128;  // electrons a warp takes from the global work counter at a time
 
 // ---------------------------------------------------------------- advance
+// Claims the next queued secondary for this lane, or returns -1 when the queue
+// is empty at this moment.
+__device__ __forceinline__ int claim_secondary(const AdvanceArgs& a) {
+  for (int tries = 0; tries < 64; ++tries) {
+    const int cur = *(volatile int*)a.sec_next;
+    const int cnt = min(*(volatile int*)a.sec_count, a.sec_cap);
+    if (cur >= cnt) return -1;
+    if (atomicCAS(a.sec_next, cur, cur + 1) == cur) return cur;
+  }
+  return -1;
+}
+
 // Every electron is flown and collided until the synchronisation time
 // (BoltzmannMC.C:617-688). Work distribution: a persistent grid; each warp
 // takes chunks of electrons from a global counter and every lane holds one
 // electron. A lane whose electron reaches the synchronisation time (or is
 // attached) writes it back and takes the next electron of the warp's chunk,
 // so the lanes of a warp stay busy although the number of collisions per
-// electron and interval is random (Poisson-distributed).
+// electron and interval is random. Once the ensemble is exhausted, lanes take
+// queued secondaries and push them from their creation time to the end of
+// the interval. A warp keeps running while any of its lanes is busy, so a
+// secondary is always taken by a live warp (at least its creator's).
 template <int MODE>
 __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   __shared__ unsigned int s_count[kMaxProcesses];
@@ -74,14 +89,15 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   __shared__ ProcF s_proc[kMaxProcesses];
   __shared__ GasF s_gas[kMaxGases];
   __shared__ double s_red[kAdvanceThreads / 32];
+  __shared__ double s_redt[kAdvanceThreads / 32];
   __shared__ unsigned long long s_redn[kAdvanceThreads / 32];
   __shared__ unsigned long long s_redr[kAdvanceThreads / 32];
 
-  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
-    s_count[p] = 0u;
-    s_gain[p] = 0.0f;
-    s_loss[p] = 0.0f;
-    s_proc[p] = a.procs[p];
+  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
+    s_count[q] = 0u;
+    s_gain[q] = 0.0f;
+    s_loss[q] = 0.0f;
+    s_proc[q] = a.procs[q];
   }
   if (threadIdx.x < a.c.G) s_gas[threadIdx.x] = a.gases[threadIdx.x];
   __syncthreads();
@@ -102,39 +118,39 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     interval = c.interval;
     tab.inv_step = c.inv_step;
   }
-  const int n_el = a.n_dev ? *a.n_dev : a.n;
+  const int n_el = a.queue_only ? 0 : a.n;
   const float inv_nu = 1.0f / nu;
   const float hme = a.c.half_me_over_e;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
 
-  float gain_sum = 0.0f;
+  float gain_sum = 0.0f, time_adj = 0.0f;
   unsigned int null_n = 0, real_n = 0;
   float e_max = 0.0f;
 
-  // warp-uniform chunk cursor
+  // warp-uniform chunk cursor over the ensemble
   int next = 0, end = 0;
-  bool exhausted = false;
-  // per-lane electron
+  bool exhausted = a.queue_only != 0;
+  // per-lane electron: ensemble slot (>= 0) or secondary (-1 - index)
   bool have = false;
   int slot = 0;
   float3 p = make_float3(0.f, 0.f, 0.f), v = make_float3(0.f, 0.f, 0.f);
   float s = -1.0f, t = 0.0f, energy = 0.0f;
   int events = 0;
-  PhiloxStream rng;
+  PcgStream rng;
 
   for (;;) {
-    // ---- refill lanes without an electron from the warp's chunk
+    // ---- refill lanes without an electron: the warp's ensemble chunk first,
+    // then the secondary queue
     const unsigned need = __ballot_sync(0xffffffffu, !have);
-    if (need) {
+    if (need && !exhausted) {
       const int n_need = __popc(need);
       const int r = __popc(need & lt_mask);
       int idx = -1;
-      int avail = end - next;
-      int take = min(n_need, avail);
+      const int take = min(n_need, end - next);
       if (!have && r < take) idx = next + r;
       next += take;
-      if (n_need > take && !exhausted) {
+      if (n_need > take) {
         int base = 0;
         if (lane == 0) base = atomicAdd(a.work_counter, kChunk);
         base = __shfl_sync(0xffffffffu, base, 0);
@@ -150,23 +166,36 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
         }
       }
       if (idx >= 0) {
-        slot = a.list ? a.list[idx] : idx;
-        const float4 A = a.state[2 * slot];
-        const float4 B = a.state[2 * slot + 1];
+        const float4 A = a.state[2 * idx];
+        const float4 B = a.state[2 * idx + 1];
         if (B.w == 0.0f) {
+          slot = idx;
           p = make_float3(A.x - shift.x, A.y - shift.y, A.z - shift.z);
           v = make_float3(B.x, B.y, B.z);
           s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
           t = 0.0f;
-          if (a.list) {
-            t = a.pend_t[slot];
-            a.pend_t[slot] = -1.0f;
-          }
-          rng.init((uint32_t)slot, interval, a.seed, a.salt);
+          rng.init((uint32_t)idx, interval, a.seed, a.salt);
           energy = energy_of(v, hme);
           events = 0;
           have = true;
         }
+      }
+    }
+    if (exhausted && !have) {
+      const int k = claim_secondary(a);
+      if (k >= 0) {
+        const float4 A = a.sec[2 * k];
+        const float4 B = a.sec[2 * k + 1];
+        slot = -1 - k;
+        p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
+        v = make_float3(B.x, B.y, B.z);
+        s = -1.0f;
+        t = A.w;
+        time_adj += T - t;  // electron-time this secondary adds to the interval
+        rng.init(0x80000000u | (uint32_t)k, interval, a.seed, a.salt + 1u);
+        energy = energy_of(v, hme);
+        events = 0;
+        have = true;
       }
     }
     if (!__any_sync(0xffffffffu, have)) {
@@ -175,26 +204,25 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     }
     if (!have) continue;
 
-    // ---- one event of this lane's electron
+    // ---- one event of this lane's electron: a free flight to the next
+    // collision or, when that lies beyond the synchronisation time, to the
+    // synchronisation time (BoltzmannMC.C:650-675); the flight code is the
+    // same for both so the lanes stay converged
     if (s < 0.0f) s = -__logf(rng.oo());
     const float tau = s * inv_nu;
-    const float phi = phi0 + phase_rate * t;
-    bool finished = false, dead = false;
-    if (t + tau > T) {
-      // partial flight to the synchronisation time (BoltzmannMC.C:657-663)
-      const float dt = T - t;
-      free_flight(field, phi, dt, p, v);
+    const bool partial = t + tau > T;
+    const float dt = partial ? T - t : tau;
+    free_flight(field, phi0 + phase_rate * t, dt, p, v);
+    {
+      const float e1 = energy_of(v, hme);
+      gain_sum += e1 - energy;
+      energy = e1;
+    }
+    bool finished = partial, dead = false;
+    if (partial) {
       s = fmaxf(s - nu * dt, 0.0f);
-      const float e1 = energy_of(v, hme);
-      gain_sum += e1 - energy;
-      energy = e1;
-      finished = true;
     } else {
-      free_flight(field, phi, tau, p, v);
       t += tau;
-      const float e1 = energy_of(v, hme);
-      gain_sum += e1 - energy;
-      energy = e1;
       CollResult cr;
       collide(a.c, tab, s_proc, s_gas, nu, v, energy, rng, cr);
       if (cr.chosen < 0) {
@@ -209,15 +237,18 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
           const int k = append_slot(a.sec_count);
           if (k < a.sec_cap) {
             a.sec[2 * k] = make_float4(p.x, p.y, p.z, t);
-            a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, energy_of(cr.ej_v, hme));
+            a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
           } else {
             atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
           }
         } else if (ptype == kAttachment) {
-          const int k = append_slot(a.att_count);
-          a.att_list[k] = slot;
           dead = true;
           finished = true;
+          time_adj -= T - t;  // electron-time the attached electron no longer spends
+          if (slot >= 0) {
+            const int k = append_slot(a.att_count);
+            a.att_list[k] = slot;
+          }
         }
       }
       s = -__logf(rng.oo());  // next free flight (BoltzmannMC.C:670)
@@ -227,8 +258,9 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
       }
     }
     if (finished) {
-      a.state[2 * slot] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
-      a.state[2 * slot + 1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
+      float4* dst = slot >= 0 ? a.state + 2 * slot : a.sec + 2 * (-1 - slot);
+      dst[0] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
+      dst[1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
       if (!dead) e_max = fmaxf(e_max, energy);
       have = false;
     }
@@ -236,25 +268,29 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
 
   // block reductions -> global tallies
   double g = warp_sum((double)gain_sum);
+  double ta = warp_sum((double)time_adj);
   unsigned long long nn = warp_sum_u64((unsigned long long)null_n);
   unsigned long long nr = warp_sum_u64((unsigned long long)real_n);
   float em = warp_max(e_max);
   if (lane == 0) {
     s_red[wid] = g;
+    s_redt[wid] = ta;
     s_redn[wid] = nn;
     s_redr[wid] = nr;
     if (em > 0.0f) atomic_max_energy(a.max_energy_bits, em);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double gs = 0.0;
+    double gs = 0.0, ts = 0.0;
     unsigned long long ns = 0, rs = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
       gs += s_red[w];
+      ts += s_redt[w];
       ns += s_redn[w];
       rs += s_redr[w];
     }
     if (gs != 0.0) atomicAdd(a.field_gain, gs);
+    if (ts != 0.0) atomicAdd(a.time_adjust, ts);
     if (ns) atomicAdd(a.null_count, ns);
     if (rs) atomicAdd(a.real_count, rs);
   }
@@ -267,14 +303,14 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   }
 }
 
-// the main pass over every electron and the pass over the pending list carry
-// different names so that profiles can tell them apart
+// the main pass over the ensemble and the drain of left-over secondaries
+// carry different names so that profiles can tell them apart
 template <int MODE>
 __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance(AdvanceArgs a) {
   advance_body<MODE>(a);
 }
 template <int MODE>
-__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance_pending(AdvanceArgs a) {
+__global__ void __launch_bounds__(32) k_advance_drain(AdvanceArgs a) {
   advance_body<MODE>(a);
 }
 
@@ -484,9 +520,6 @@ __device__ __forceinline__ int uniform_index(uint32_t w, int n) {
   return (int)(((unsigned long long)w * (unsigned long long)n) >> 32);
 }
 
-// A slot that must still be advanced from time t0 to the synchronisation
-// time. pend_t[slot] holds the start time (NaN or negative: not pending); a
-// slot enters the list once even when it is refilled twice in one round.
 // adds a per-thread energy to the growth accumulator with one atomic per warp
 __device__ __forceinline__ void add_growth(double* growth, double e) {
   cg::coalesced_group g = cg::coalesced_threads();
@@ -494,52 +527,58 @@ __device__ __forceinline__ void add_growth(double* growth, double e) {
   if (g.thread_rank() == 0) atomicAdd(growth, tot);
 }
 
-__device__ __forceinline__ void mark_pending(const PopArgs& a, int slot, float t0) {
-  const float old = atomicExch(&a.pend_t[slot], t0);
-  if (!(old >= 0.0f)) {
-    const int k = append_slot(a.pend_count);
-    a.pend_list[k] = slot;
-  }
-}
+__device__ __forceinline__ float energy4(float4 B, float hme) { return (B.x * B.x + B.y * B.y + B.z * B.z) * hme; }
 
-// Counts and interval index of one population-control round, from the
-// device (graph replay) or from the launch arguments.
-struct PopCounts {
-  int n_sec, n_att;
-  uint64_t interval;
-};
-__device__ __forceinline__ PopCounts pop_counts(const PopArgs& a) {
-  PopCounts c;
-  c.n_sec = a.n_sec_dev ? *a.n_sec_dev : a.n_sec;
-  c.n_att = a.n_att_dev ? *a.n_att_dev : a.n_att;
-  c.interval = a.ctl ? a.ctl->interval : a.interval;
-  return c;
-}
-#define THREAD_STRIDE(j, n) for (int j = tid; j < (n); j += nthreads)
-
-// (1) attached slots take secondaries, last secondary first (BoltzmannMC.C:1344-1359)
-__device__ void pop_fill(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
-  const int k = min(pc.n_att, pc.n_sec);
-  THREAD_STRIDE(j, k) {
+// Population control (BoltzmannMC.C:1282-1408) in one block, every phase
+// separated by a block barrier. All electrons and secondaries are at the
+// synchronisation time here.
+//  (0) secondaries that did not attach are compacted;
+//  (1) attached slots take secondaries, last secondary first (:1344-1359);
+//  (2) remaining attached slots clone a random non-attached electron, whose
+//      energy enters the growth term (:1360-1376);
+//  (3) excess secondaries: a uniformly random subset of size m is removed from
+//      the pool of N slots + m unplaced secondaries - the outcome of the
+//      reference's sequential uniform removal (:1379-1407) - and the surviving
+//      secondaries take the removed slots; removed energies leave the growth term.
+constexpr int kPopThreads = 1024;
+__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
+  __shared__ int s_n[4];  // alive secondaries, removed slots, surviving secondaries
+  const int n_sec_all = min(*a.sec_count, 1 << 30);
+  const int n_att = *a.att_count;
+  if (n_sec_all == 0 && n_att == 0) return;
+  const uint64_t interval = a.ctl->interval;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const float hme = a.half_me_over_e;
+  if (tid < 4) s_n[tid] = 0;
+  __syncthreads();
+  // (0)
+  for (int j = tid; j < n_sec_all; j += nt)
+    if (a.sec[2 * j + 1].w == 0.0f) a.alive[atomicAdd(&s_n[0], 1)] = j;
+  __syncthreads();
+  const int n_sec = s_n[0];
+  // (1)
+  const int k = min(n_att, n_sec);
+  for (int j = tid; j < k; j += nt) {
     const int slot = a.att_list[j];
-    const int sidx = pc.n_sec - 1 - j;
-    const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
-    a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
-    a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
-    mark_pending(a, slot, S0.w);
+    const int sidx = a.alive[n_sec - 1 - j];
+    a.state[2 * slot] = a.sec[2 * sidx];
+    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
-}
-
-// (2) remaining attached slots clone a random surviving electron
-// (BoltzmannMC.C:1360-1376); the energy-growth term gains its energy.
-__device__ void pop_clone(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
-  THREAD_STRIDE(jj, pc.n_att - pc.n_sec) {
-    const int j = pc.n_sec + jj;
+  __syncthreads();
+  // (2) the slots still attached are marked first, so that no clone is made
+  // from another clone
+  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
+    const int dest = a.att_list[n_sec + jj];
+    atomicOr(&a.claim[dest >> 5], 1u << (dest & 31));
+  }
+  __syncthreads();
+  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
+    const int j = n_sec + jj;
     const int dest = a.att_list[j];
     int src = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
-      const int r = uniform_index(pop_word((uint32_t)j, pc.interval, a.seed, a.salt, d), a.n_electrons);
-      if (a.state[2 * r + 1].w == 0.0f) {
+      const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
+      if (!(a.claim[r >> 5] & (1u << (r & 31))) && a.state[2 * r + 1].w == 0.0f) {
         src = r;
         break;
       }
@@ -551,22 +590,21 @@ __device__ void pop_clone(const PopArgs& a, const PopCounts& pc, int tid, int nt
     const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
     a.state[2 * dest] = A;
     a.state[2 * dest + 1] = B;
-    add_growth(a.growth, (double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
-    const float t0 = a.pend_t[src];
-    if (t0 >= 0.0f) mark_pending(a, dest, t0);
+    add_growth(a.growth, (double)energy4(B, hme));
   }
-}
-
-// (3) excess secondaries: remove a uniformly random subset of size m from the
-// pool of n_electrons slots + m unplaced secondaries, the outcome of the
-// reference's sequential uniform removal (BoltzmannMC.C:1379-1407).
-__device__ void pop_claim(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
-  const int m = pc.n_sec - pc.n_att;
+  __syncthreads();
+  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
+    const int dest = a.att_list[n_sec + jj];
+    atomicAnd(&a.claim[dest >> 5], ~(1u << (dest & 31)));
+  }
+  __syncthreads();
+  // (3)
+  const int m = n_sec - n_att;
   const int pool = a.n_electrons + m;
-  THREAD_STRIDE(j, m) {
+  for (int j = tid; j < m; j += nt) {
     int got = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
-      const int r = uniform_index(pop_word((uint32_t)j, pc.interval, a.seed, a.salt ^ 0x55u, d), pool);
+      const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 2u, d), pool);
       const unsigned int bit = 1u << (r & 31);
       const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
       if (!(old & bit)) {
@@ -577,77 +615,30 @@ __device__ void pop_claim(const PopArgs& a, const PopCounts& pc, int tid, int nt
     a.removed[j] = got;
     if (got < 0) atomicExch(a.error_flag, 5);
   }
-}
-
-__device__ void pop_pair(const PopArgs& a, const PopCounts& pc, int* pair_counts, int tid, int nthreads) {
-  const int m = pc.n_sec - pc.n_att;
-  THREAD_STRIDE(j, m) {
+  __syncthreads();
+  for (int j = tid; j < m; j += nt) {
     const int r = a.removed[j];
     if (r >= 0 && r < a.n_electrons) {
-      const int q = atomicAdd(&pair_counts[0], 1);
-      a.pair_slot[q] = r;
+      a.pair_slot[atomicAdd(&s_n[1], 1)] = r;
+      add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], hme));
     } else if (r >= a.n_electrons) {
-      // a removed secondary: its energy leaves the ensemble
-      add_growth(a.growth, -(double)a.sec[2 * (r - a.n_electrons) + 1].w);
+      add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], hme));
     }
-    // secondary j survives when its pool bit was not claimed
     const int b = a.n_electrons + j;
-    if (!(a.claim[b >> 5] & (1u << (b & 31)))) {
-      const int q = atomicAdd(&pair_counts[1], 1);
-      a.pair_sec[q] = j;
-    }
+    if (!(a.claim[b >> 5] & (1u << (b & 31)))) a.pair_sec[atomicAdd(&s_n[2], 1)] = a.alive[j];
   }
-}
-
-__device__ void pop_place(const PopArgs& a, int np, int tid, int nthreads) {
-  THREAD_STRIDE(q, np) {
+  __syncthreads();
+  const int np = min(s_n[1], s_n[2]);
+  for (int q = tid; q < np; q += nt) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
-    const float4 B = a.state[2 * slot + 1];
-    add_growth(a.growth, -(double)((B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e));
-    const float4 S0 = a.sec[2 * sidx], S1 = a.sec[2 * sidx + 1];
-    a.state[2 * slot] = make_float4(S0.x, S0.y, S0.z, -1.0f);
-    a.state[2 * slot + 1] = make_float4(S1.x, S1.y, S1.z, 0.0f);
-    mark_pending(a, slot, S0.w);
+    a.state[2 * slot] = a.sec[2 * sidx];
+    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
-}
-
-__device__ void pop_unclaim(const PopArgs& a, const PopCounts& pc, int tid, int nthreads) {
-  const int m = pc.n_sec - pc.n_att;
-  THREAD_STRIDE(j, m) {
+  for (int j = tid; j < m; j += nt) {
     const int r = a.removed[j];
     if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
   }
-}
-
-// multi-kernel form (large counts known on the host)
-#define GRID_TID (blockIdx.x * blockDim.x + threadIdx.x), (gridDim.x * blockDim.x)
-__global__ void k_pop_fill(PopArgs a) { pop_fill(a, pop_counts(a), GRID_TID); }
-__global__ void k_pop_clone(PopArgs a) { pop_clone(a, pop_counts(a), GRID_TID); }
-__global__ void k_pop_claim(PopArgs a) { pop_claim(a, pop_counts(a), GRID_TID); }
-__global__ void k_pop_pair(PopArgs a) { pop_pair(a, pop_counts(a), a.pair_counts, GRID_TID); }
-__global__ void k_pop_place(PopArgs a) { pop_place(a, min(a.pair_counts[0], a.pair_counts[1]), GRID_TID); }
-__global__ void k_pop_unclaim(PopArgs a) { pop_unclaim(a, pop_counts(a), GRID_TID); }
-
-// single-block form: every phase in one launch, separated by block barriers
-// (counts read on the device; used inside the captured interval)
-constexpr int kPopThreads = 1024;
-__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
-  __shared__ int s_pairs[2];
-  const PopCounts pc = pop_counts(a);
-  if (pc.n_sec == 0 && pc.n_att == 0) return;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  if (tid < 2) s_pairs[tid] = 0;
-  pop_fill(a, pc, tid, nt);
-  __syncthreads();
-  pop_clone(a, pc, tid, nt);
-  pop_claim(a, pc, tid, nt);
-  __syncthreads();
-  pop_pair(a, pc, s_pairs, tid, nt);
-  __syncthreads();
-  pop_place(a, min(s_pairs[0], s_pairs[1]), tid, nt);
-  __syncthreads();
-  pop_unclaim(a, pc, tid, nt);
 }
 
 // --------------------------------------------------------------- replay
@@ -702,28 +693,22 @@ inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; 
 }  // namespace
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
-  int grid;
-  if (a.grid_blocks > 0) {
-    grid = a.grid_blocks;
+#define LGPU_ADVANCE(K, G, B)                                  \
+  switch (a.field.mode) {                                      \
+    case kFieldDC: K<kFieldDC><<<G, B, 0, s>>>(a); break;      \
+    case kFieldAC: K<kFieldAC><<<G, B, 0, s>>>(a); break;      \
+    case kFieldB: K<kFieldB><<<G, B, 0, s>>>(a); break;        \
+    case kFieldECR: K<kFieldECR><<<G, B, 0, s>>>(a); break;    \
+    default: K<kFieldACB><<<G, B, 0, s>>>(a); break;           \
+  }
+  if (a.queue_only) {
+    LGPU_ADVANCE(k_advance_drain, 1, 32)
   } else {
-    if (a.n <= 0) return;
     // persistent grid: at most kAdvanceBlocksPerSM blocks per SM, fewer when
     // the electrons do not fill them (one chunk per warp)
     const int warps_needed = (a.n + kChunk - 1) / kChunk;
-    grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
-  }
-#define LGPU_ADVANCE(K)                                          \
-  switch (a.field.mode) {                                        \
-    case kFieldDC: K<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(a); break;   \
-    case kFieldAC: K<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(a); break;   \
-    case kFieldB: K<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(a); break;     \
-    case kFieldECR: K<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(a); break; \
-    default: K<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(a); break;       \
-  }
-  if (a.list) {
-    LGPU_ADVANCE(k_advance_pending)
-  } else {
-    LGPU_ADVANCE(k_advance)
+    const int grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
+    LGPU_ADVANCE(k_advance, grid, kAdvanceThreads)
   }
 #undef LGPU_ADVANCE
 }
@@ -750,24 +735,7 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
   k_hist<<<grid, kHistThreads, 0, s>>>(a);
 }
 
-void launch_pop_control(const PopArgs& a, cudaStream_t s) {
-  if (a.grid_blocks > 0) {
-    // counts live on the device: one block runs every phase
-    k_pop_all<<<1, kPopThreads, 0, s>>>(a);
-    return;
-  }
-  const int k = a.n_att < a.n_sec ? a.n_att : a.n_sec;
-  if (k > 0) k_pop_fill<<<blocks_for(k, 128), 128, 0, s>>>(a);
-  if (a.n_att > a.n_sec) k_pop_clone<<<blocks_for(a.n_att - a.n_sec, 128), 128, 0, s>>>(a);
-  const int m = a.n_sec - a.n_att;
-  if (m > 0) {
-    const int g = blocks_for(m, 128);
-    k_pop_claim<<<g, 128, 0, s>>>(a);
-    k_pop_pair<<<g, 128, 0, s>>>(a);
-    k_pop_place<<<g, 128, 0, s>>>(a);
-    k_pop_unclaim<<<g, 128, 0, s>>>(a);
-  }
-}
+void launch_pop_control(const PopArgs& a, cudaStream_t s) { k_pop_all<<<1, kPopThreads, 0, s>>>(a); }
 
 void launch_replay_flight(const ReplayFlightArgs& a, cudaStream_t s) {
   if (a.n > 0) k_replay_flight<<<blocks_for(a.n, 128), 128, 0, s>>>(a);

@@ -13,20 +13,20 @@ constexpr int kMaxProcesses = 512;
 constexpr int kMaxGases = 16;
 constexpr int kMoments = 22;  // sum e, r(3), v(3), r r^T (6 unique), r v^T (9)
 
-// Arguments of one advance launch: every listed electron is pushed from its
-// start time to the end of the synchronisation interval, colliding on the way.
+// Arguments of one advance launch: every electron of the ensemble is pushed
+// from the start of the synchronisation interval to its end, colliding on the
+// way; secondaries created on the way are queued and pushed from their
+// creation time to the end of the interval by the same launch.
 struct AdvanceArgs {
-  float4* state;            // [2*cap]: (x, y, z, s) and (vx, vy, vz, dead flag)
-  int n;                    // electrons to advance (list length when `list` is set)
-  const int* list;          // optional slot list (pending electrons)
-  float* pend_t;            // start time of each pending slot (s, from the interval start); reset on use
+  float4* state;            // [2*N]: (x, y, z, s) and (vx, vy, vz, dead flag)
+  int n;                    // electrons of the ensemble
   float dt_sync;            // interval length (s)
   float phi0;               // phase at the interval start (rad), FP64-reduced on the host
   float phase_rate;         // w (AC, AC+B) or W (resonance)
   float nu;                 // trial collision frequency (1/s)
   uint64_t seed;
-  uint64_t interval;        // synchronisation interval index (RNG counter)
-  uint32_t salt;            // distinguishes the main pass from pending rounds
+  uint64_t interval;        // synchronisation interval index (random-number counter)
+  uint32_t salt;
   float3 shift;             // origin shift subtracted from every position on load
   FieldF field;
   Consts c;
@@ -34,11 +34,13 @@ struct AdvanceArgs {
   const ProcF* procs;
   const GasF* gases;
   int P;
-  // outputs
-  float4* sec;              // [2*sec_cap]: (x, y, z, t_c), (vx, vy, vz, energy)
+  // secondaries: created as (x, y, z, t_c), (vx, vy, vz, 0); after their
+  // advance (x, y, z, s), (vx, vy, vz, dead flag) at the end of the interval
+  float4* sec;
   int* sec_count;
+  int* sec_next;                   // queue cursor over the secondaries
   int sec_cap;
-  int* att_list;
+  int* att_list;                   // attached ensemble slots
   int* att_count;
   unsigned long long* proc_count;  // [P]
   double* proc_gain;               // [P]
@@ -46,13 +48,13 @@ struct AdvanceArgs {
   unsigned long long* null_count;
   unsigned long long* real_count;
   double* field_gain;
+  double* time_adjust;             // simulated electron-time beyond N * dt: + secondaries, - attachments (s)
   unsigned int* max_energy_bits;   // float bits of the largest final energy
   int* error_flag;                 // 2: secondary buffer full, 3: collision budget exhausted
   int* work_counter;               // chunk counter of the persistent grid (zero before the launch)
   int sm_count;
   const IntervalCtl* ctl;          // when set: per-interval values are read from here
-  const int* n_dev;                // when set: the electron count is read from here (pending lists)
-  int grid_blocks;                 // when > 0: fixed grid size (launches whose count lives on the device)
+  int queue_only;                  // 1: only drain the secondary queue (one warp)
 };
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);
@@ -118,31 +120,25 @@ struct HistArgs {
 };
 void launch_hist(const HistArgs& a, cudaStream_t s);
 
-// Population control (BoltzmannMC.C:1282-1408), in parallel.
+// Population control (BoltzmannMC.C:1282-1408) at the end of an interval,
+// when every electron and every secondary is at the synchronisation time.
 struct PopArgs {
   float4* state;
   int n_electrons;
-  float4* sec;                     // secondaries (x, y, z, t_c), (vx, vy, vz, energy)
-  int n_sec;
+  const float4* sec;               // advanced secondaries (x, y, z, s), (vx, vy, vz, dead flag)
+  const int* sec_count;
   const int* att_list;
-  int n_att;
-  float* pend_t;                   // [cap] start time of pending slots (<0: not pending)
-  int* pend_list;                  // pending slot list
-  int* pend_count;
-  unsigned int* claim;             // bitmap over n_electrons + n_sec, all zero on entry and on exit
-  int* removed;                    // [n_sec] scratch
-  int* pair_slot;                  // [n_sec] scratch
-  int* pair_sec;                   // [n_sec] scratch
-  int* pair_counts;                // [2] scratch counters (zeroed by the caller)
+  const int* att_count;
+  unsigned int* claim;             // bitmap over n_electrons + sec_cap, all zero on entry and on exit
+  int* alive;                      // [sec_cap] scratch: indices of secondaries that did not attach
+  int* removed;                    // [sec_cap] scratch
+  int* pair_slot;                  // [sec_cap] scratch
+  int* pair_sec;                   // [sec_cap] scratch
   double* growth;                  // energy growth accumulator (eV)
   float half_me_over_e;
-  uint64_t seed, interval;
-  uint32_t salt;
+  uint64_t seed;
+  const IntervalCtl* ctl;
   int* error_flag;                 // set when a bounded retry loop gives up
-  const int* n_sec_dev;            // when set: counts are read from the device and the
-  const int* n_att_dev;            //   launches use a fixed grid (graph capture)
-  const IntervalCtl* ctl;          // when set: the interval index is read from here
-  int grid_blocks;
 };
 void launch_pop_control(const PopArgs& a, cudaStream_t s);
 
