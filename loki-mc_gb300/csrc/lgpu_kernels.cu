@@ -119,6 +119,7 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     tab.inv_step = c.inv_step;
   }
   const int n_el = a.queue_only ? 0 : a.n;
+  const unsigned int ready_tag = (unsigned int)interval + 1u;
   const float inv_nu = 1.0f / nu;
   const float hme = a.c.half_me_over_e;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -184,8 +185,20 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     if (exhausted && !have) {
       const int k = claim_secondary(a);
       if (k >= 0) {
-        const float4 A = a.sec[2 * k];
-        const float4 B = a.sec[2 * k + 1];
+        // the creator publishes the entry after writing it; wait (bounded)
+        // for the tag, then read past L1
+        bool ok = false;
+        for (int spin = 0; spin < (1 << 22); ++spin) {
+          if (*(volatile unsigned int*)&a.sec_ready[k] == ready_tag) {
+            ok = true;
+            break;
+          }
+          __nanosleep(32);
+        }
+        if (!ok) atomicExch(a.error_flag, 6);
+        __threadfence();
+        const float4 A = __ldcg(&a.sec[2 * k]);
+        const float4 B = __ldcg(&a.sec[2 * k + 1]);
         slot = -1 - k;
         p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
         v = make_float3(B.x, B.y, B.z);
@@ -236,8 +249,10 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
         if (ptype == kIonization) {
           const int k = append_slot(a.sec_count);
           if (k < a.sec_cap) {
-            a.sec[2 * k] = make_float4(p.x, p.y, p.z, t);
-            a.sec[2 * k + 1] = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
+            __stcg(&a.sec[2 * k], make_float4(p.x, p.y, p.z, t));
+            __stcg(&a.sec[2 * k + 1], make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f));
+            __threadfence();
+            atomicExch(&a.sec_ready[k], ready_tag);
           } else {
             atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
           }

@@ -39,6 +39,7 @@ struct AdvanceArgs {
   float4* sec;
   int* sec_count;
   int* sec_next;                   // queue cursor over the secondaries
+  unsigned int* sec_ready;         // per-entry publication tag (interval index + 1) set after the data
   int sec_cap;
   int* att_list;                   // attached ensemble slots
   int* att_count;

@@ -5,10 +5,12 @@ tests/golden/make_golden.py --stats with 1e4 electrons).
 The GPU solve uses the reference's own parsed inputs (the per-process arrays
 of the matching kin_*.npz), the same numerics keys and 1e5 electrons. Every
 swarm parameter the reference pins (mean energy, flux and bulk drift velocity,
-flux and bulk diffusion along the axes) must agree within three combined
-standard errors (50-block batch means of both runs, BoltzmannMC.C:1484-1726)
-plus a 0.2% allowance for FP32 rounding; components the reference cannot
-resolve (below five of its standard errors) are skipped. Rate coefficients
+flux and bulk diffusion along the axes) must agree within 0.5% or within
+three combined standard errors (50-block batch means of both runs,
+BoltzmannMC.C:1484-1726); components the reference cannot resolve (below five
+of its standard errors) are skipped. The batch-means errors of a 1e4-electron
+run understate its scatter (seeded reference runs of the atomic case differ by
+about 2 of their own errors), hence 0.5% as the floor. Rate coefficients
 of processes with at least 2000 reference counts agree within three combined
 Poisson errors doubled for autocorrelation, plus 1%.
 """
@@ -38,7 +40,7 @@ def run_gpu(rec, n_electrons=100_000):
     meta = dict(META[rec["case"]], **rec["overrides"])
     num = rec["numerics"]
     cfg = capi.default_config(n_electrons=float(n_electrons), n_interp=int(num.get("nInterpPoints", 2000)),
-                              seed=4242, init_temp_ratio=1.0 / (KB_EV * 300.0),
+                              seed=int(os.environ.get("LGPU_TEST_SEED", "4242")), init_temp_ratio=1.0 / (KB_EV * 300.0),
                               gas_temperature_effect=GAS_TEMP[meta.get("gas_temp", "false")],
                               req_integration_points=float(num["nIntegrationPoints"]),
                               max_coll_before_ss=float(num["maxCollisionsBeforeSteadyState"]),
@@ -71,7 +73,7 @@ def test_swarm_parameters_match_reference(name):
         if abs(rv) < 5.0 * re:
             continue
         checked += 1
-        tol = 3.0 * np.hypot(ge, re) + 2e-3 * abs(rv)
+        tol = max(3.0 * np.hypot(ge, re), 5e-3 * abs(rv))
         if abs(gv - rv) > tol:
             failures.append(f"{label}: gpu {gv:.6g} +- {ge:.3g}, reference {rv:.6g} +- {re:.3g}")
     assert checked >= 4, name
