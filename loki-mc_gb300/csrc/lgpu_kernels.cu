@@ -59,18 +59,6 @@ constexpr int kAdvanceBlocksPerSM = 4;
 constexpr int kChunk = 128;  // electrons a warp takes from the global work counter at a time
 
 // ---------------------------------------------------------------- advance
-// Claims the next queued secondary for this lane, or returns -1 when the queue
-// is empty at this moment.
-__device__ __forceinline__ int claim_secondary(const AdvanceArgs& a) {
-  for (int tries = 0; tries < 64; ++tries) {
-    const int cur = *(volatile int*)a.sec_next;
-    const int cnt = min(*(volatile int*)a.sec_count, a.sec_cap);
-    if (cur >= cnt) return -1;
-    if (atomicCAS(a.sec_next, cur, cur + 1) == cur) return cur;
-  }
-  return -1;
-}
-
 // Every electron is flown and collided until the synchronisation time
 // (BoltzmannMC.C:617-688). Work distribution: a persistent grid; each warp
 // takes chunks of electrons from a global counter and every lane holds one
@@ -138,6 +126,7 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   float3 p = make_float3(0.f, 0.f, 0.f), v = make_float3(0.f, 0.f, 0.f);
   float s = -1.0f, t = 0.0f, energy = 0.0f;
   int events = 0;
+  int pend_k = -1, pend_polls = 0;  // claimed secondary waiting for publication
   PcgStream rng;
 
   for (;;) {
@@ -182,37 +171,57 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
         }
       }
     }
-    if (exhausted && !have) {
-      const int k = claim_secondary(a);
-      if (k >= 0) {
-        // the creator publishes the entry after writing it; wait (bounded)
-        // for the tag, then read past L1
-        bool ok = false;
-        for (int spin = 0; spin < (1 << 22); ++spin) {
-          if (*(volatile unsigned int*)&a.sec_ready[k] == ready_tag) {
-            ok = true;
-            break;
-          }
-          __nanosleep(32);
+    bool queue_empty = true;
+    if (exhausted) {
+      // the warp leader claims a batch of queued secondaries for the idle
+      // lanes; a lane loads its entry once the creator has published it
+      // (checked once per iteration, never waited for in a loop)
+      const unsigned idle = __ballot_sync(0xffffffffu, !have && pend_k < 0);
+      int base = 0, n = 0, left = 0;
+      if (lane == 0) {
+        const int cur = *(volatile int*)a.sec_next;
+        const int cnt = min(*(volatile int*)a.sec_count, a.sec_cap);
+        left = cnt - cur;
+        const int want = min(__popc(idle), left);
+        if (want > 0 && atomicCAS(a.sec_next, cur, cur + want) == cur) {
+          base = cur;
+          n = want;
         }
-        if (!ok) atomicExch(a.error_flag, 6);
-        __threadfence();
-        const float4 A = __ldcg(&a.sec[2 * k]);
-        const float4 B = __ldcg(&a.sec[2 * k + 1]);
-        slot = -1 - k;
-        p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
-        v = make_float3(B.x, B.y, B.z);
-        s = -1.0f;
-        t = A.w;
-        time_adj += T - t;  // electron-time this secondary adds to the interval
-        rng.init(0x80000000u | (uint32_t)k, interval, a.seed, a.salt + 1u);
-        energy = energy_of(v, hme);
-        events = 0;
-        have = true;
+      }
+      base = __shfl_sync(0xffffffffu, base, 0);
+      n = __shfl_sync(0xffffffffu, n, 0);
+      left = __shfl_sync(0xffffffffu, left, 0);
+      queue_empty = left <= n;
+      const int r = __popc(idle & lt_mask);
+      if (((idle >> lane) & 1u) && r < n) {
+        pend_k = base + r;
+        pend_polls = 0;
+      }
+      if (!have && pend_k >= 0) {
+        if (*(volatile unsigned int*)&a.sec_ready[pend_k] == ready_tag) {
+          __threadfence();
+          const int k = pend_k;
+          pend_k = -1;
+          const float4 A = __ldcg(&a.sec[2 * k]);
+          const float4 B = __ldcg(&a.sec[2 * k + 1]);
+          slot = -1 - k;
+          p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
+          v = make_float3(B.x, B.y, B.z);
+          s = -1.0f;
+          t = A.w;
+          time_adj += T - t;  // electron-time this secondary adds to the interval
+          rng.init(0x80000000u | (uint32_t)k, interval, a.seed, a.salt + 1u);
+          energy = energy_of(v, hme);
+          events = 0;
+          have = true;
+        } else if (++pend_polls > (1 << 24)) {
+          atomicExch(a.error_flag, 6);  // never published
+          pend_k = -1;
+        }
       }
     }
-    if (!__any_sync(0xffffffffu, have)) {
-      if (exhausted) break;
+    if (!__any_sync(0xffffffffu, have || pend_k >= 0)) {
+      if (exhausted && queue_empty) break;
       continue;
     }
     if (!have) continue;
