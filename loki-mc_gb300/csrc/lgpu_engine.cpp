@@ -45,7 +45,7 @@ struct Kahan {
 // Device scalars read back after a launch sequence.
 // Per-interval fields first (cleared before every interval), cumulative after.
 struct DevScalars {
-  int sec_count, att_count, sec_next, error_flag;
+  int sec_count, att_count, spill_count, error_flag;
   unsigned int max_energy_bits;
   int work_counter;
   unsigned long long null_count;
@@ -132,8 +132,7 @@ class Engine {
     sec_cap_ = std::max(N_, 4096);
     LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
     LGPU_TRY(dalloc(&d_alive_, (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_sec_ready_, (size_t)sec_cap_));
-    LGPU_CU(cudaMemsetAsync(d_sec_ready_, 0, (size_t)sec_cap_ * sizeof(unsigned int), stream_));
+    LGPU_TRY(dalloc(&d_spill_, 2 * (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_sec_, 2 * (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_att_, (size_t)N_));
     claim_words_ = ((size_t)N_ + sec_cap_ + 31) / 32;
@@ -168,7 +167,7 @@ class Engine {
     if (h_ctl_) cudaFreeHost(h_ctl_);
     d_ctl_ = nullptr;
     h_ctl_ = nullptr;
-    void* ptrs[] = {d_state_, d_alive_, d_sec_ready_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
+    void* ptrs[] = {d_state_, d_alive_, d_spill_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
                     d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_cum_pair_, d_sig_pair_, d_procf_,
                     d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
                     d_raw_e_, d_raw_v_, d_proc_count_, d_proc_gain_, d_proc_loss_, d_eedf_, d_eedf_per_, d_eadf_,
@@ -554,9 +553,10 @@ class Engine {
     a.P = P_;
     a.sec = d_sec_;
     a.sec_count = &d_sc_->sec_count;
-    a.sec_next = &d_sc_->sec_next;
-    a.sec_ready = d_sec_ready_;
     a.sec_cap = sec_cap_;
+    a.spill = d_spill_;
+    a.spill_count = &d_sc_->spill_count;
+    a.spill_cap = sec_cap_;
     a.att_list = d_att_;
     a.att_count = &d_sc_->att_count;
     a.proc_count = d_proc_count_;
@@ -610,6 +610,7 @@ class Engine {
     if (have_ion_att_) {
       AdvanceArgs d = a;
       d.queue_only = 1;
+      d.salt = 2;
       launch_advance(d, stream_);
       launch_pop_control(pop_args(), stream_);
       launches_ += 2;
@@ -703,9 +704,6 @@ class Engine {
     LGPU_TRY(check_device_errors());
     if (h_sc_->sec_count > sec_cap_)
       return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", h_sc_->sec_count, sec_cap_);
-    if (h_sc_->sec_next < h_sc_->sec_count)
-      return fail(LGPU_ERR_OVERFLOW, "secondaries left unadvanced (%d of %d)", h_sc_->sec_count - h_sc_->sec_next,
-                  h_sc_->sec_count);
     {
       float f;
       std::memcpy(&f, &h_sc_->max_energy_bits, 4);
@@ -720,9 +718,8 @@ class Engine {
   int check_device_errors() {
     const int e = h_sc_->error_flag;
     if (e == 0) return LGPU_OK;
-    if (e == 2) return fail(LGPU_ERR_OVERFLOW, "secondary buffer full within one interval");
+    if (e == 2) return fail(LGPU_ERR_OVERFLOW, "secondary or spill buffer full within one interval");
     if (e == 3) return fail(LGPU_ERR_OVERFLOW, "collision budget of one interval exhausted");
-    if (e == 6) return fail(LGPU_ERR_TIMEOUT, "a queued secondary was never published");
     return fail(LGPU_ERR_OVERFLOW, "population control retry limit reached (code %d)", e);
   }
 
@@ -1365,7 +1362,7 @@ class Engine {
   // device buffers
   float4* d_state_ = nullptr;
   int* d_alive_ = nullptr;
-  unsigned int* d_sec_ready_ = nullptr;
+  float4* d_spill_ = nullptr;
   float4* d_sec_ = nullptr;
   int* d_att_ = nullptr;
   unsigned int* d_claim_ = nullptr;

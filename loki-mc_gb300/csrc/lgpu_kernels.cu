@@ -65,21 +65,27 @@ constexpr int kChunk = 128;  // electrons a warp takes from the global work coun
 // electron. A lane whose electron reaches the synchronisation time (or is
 // attached) writes it back and takes the next electron of the warp's chunk,
 // so the lanes of a warp stay busy although the number of collisions per
-// electron and interval is random. Once the ensemble is exhausted, lanes take
-// queued secondaries and push them from their creation time to the end of
-// the interval. A warp keeps running while any of its lanes is busy, so a
-// secondary is always taken by a live warp (at least its creator's).
+// electron and interval is random. A secondary created by a lane goes on its
+// warp's own queue (shared memory) and an idle lane of the same warp pushes it
+// from its creation time to the end of the interval: the creating lane keeps
+// the warp alive, so no warp ever waits on another. A warp whose queue is full
+// spills to a global buffer that the one-warp drain launch works off after.
+constexpr int kLocalQ = 32;
 template <int MODE>
 __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
+  constexpr int kWarps = kAdvanceThreads / 32;
   __shared__ unsigned int s_count[kMaxProcesses];
   __shared__ float s_gain[kMaxProcesses];
   __shared__ float s_loss[kMaxProcesses];
   __shared__ ProcF s_proc[kMaxProcesses];
   __shared__ GasF s_gas[kMaxGases];
-  __shared__ double s_red[kAdvanceThreads / 32];
-  __shared__ double s_redt[kAdvanceThreads / 32];
-  __shared__ unsigned long long s_redn[kAdvanceThreads / 32];
-  __shared__ unsigned long long s_redr[kAdvanceThreads / 32];
+  __shared__ float4 s_qa[kWarps][kLocalQ];  // (x, y, z, t_c)
+  __shared__ float4 s_qb[kWarps][kLocalQ];  // (vx, vy, vz, 0)
+  __shared__ int s_qn[kWarps];
+  __shared__ double s_red[kWarps];
+  __shared__ double s_redt[kWarps];
+  __shared__ unsigned long long s_redn[kWarps];
+  __shared__ unsigned long long s_redr[kWarps];
 
   for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
     s_count[q] = 0u;
@@ -88,6 +94,7 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     s_proc[q] = a.procs[q];
   }
   if (threadIdx.x < a.c.G) s_gas[threadIdx.x] = a.gases[threadIdx.x];
+  if (threadIdx.x < kWarps) s_qn[threadIdx.x] = 0;
   __syncthreads();
 
   FieldF field = a.field;
@@ -106,8 +113,8 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
     interval = c.interval;
     tab.inv_step = c.inv_step;
   }
-  const int n_el = a.queue_only ? 0 : a.n;
-  const unsigned int ready_tag = (unsigned int)interval + 1u;
+  const bool drain = a.queue_only != 0;
+  const int n_el = drain ? 0 : a.n;
   const float inv_nu = 1.0f / nu;
   const float hme = a.c.half_me_over_e;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -117,21 +124,36 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
   unsigned int null_n = 0, real_n = 0;
   float e_max = 0.0f;
 
-  // warp-uniform chunk cursor over the ensemble
-  int next = 0, end = 0;
-  bool exhausted = a.queue_only != 0;
-  // per-lane electron: ensemble slot (>= 0) or secondary (-1 - index)
+  // warp-uniform cursors: ensemble chunk, spill buffer (drain only)
+  int next = 0, end = 0, sp_next = 0;
+  bool exhausted = drain;
+  // per-lane electron: ensemble slot (>= 0) or secondary (-1)
   bool have = false;
   int slot = 0;
   float3 p = make_float3(0.f, 0.f, 0.f), v = make_float3(0.f, 0.f, 0.f);
   float s = -1.0f, t = 0.0f, energy = 0.0f;
   int events = 0;
-  int pend_k = -1, pend_polls = 0;  // claimed secondary waiting for publication
+  uint32_t sec_id = 0;
   PcgStream rng;
 
+  auto start_secondary = [&](float4 A, float4 B, uint32_t id) {
+    slot = -1;
+    p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
+    v = make_float3(B.x, B.y, B.z);
+    s = -1.0f;
+    t = A.w;
+    time_adj += T - t;  // electron-time this secondary adds to the interval
+    rng.init(id, interval, a.seed, a.salt + 1u);
+    energy = energy_of(v, hme);
+    events = 0;
+    have = true;
+  };
+
   for (;;) {
+    __syncwarp();
+    if (drain) __threadfence();
     // ---- refill lanes without an electron: the warp's ensemble chunk first,
-    // then the secondary queue
+    // then the warp's own secondaries, then (drain) the spilled ones
     const unsigned need = __ballot_sync(0xffffffffu, !have);
     if (need && !exhausted) {
       const int n_need = __popc(need);
@@ -171,57 +193,35 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
         }
       }
     }
-    bool queue_empty = true;
+    int qn = min(s_qn[wid], kLocalQ);
     if (exhausted) {
-      // the warp leader claims a batch of queued secondaries for the idle
-      // lanes; a lane loads its entry once the creator has published it
-      // (checked once per iteration, never waited for in a loop)
-      const unsigned idle = __ballot_sync(0xffffffffu, !have && pend_k < 0);
-      int base = 0, n = 0, left = 0;
-      if (lane == 0) {
-        const int cur = *(volatile int*)a.sec_next;
-        const int cnt = min(*(volatile int*)a.sec_count, a.sec_cap);
-        left = cnt - cur;
-        const int want = min(__popc(idle), left);
-        if (want > 0 && atomicCAS(a.sec_next, cur, cur + want) == cur) {
-          base = cur;
-          n = want;
-        }
-      }
-      base = __shfl_sync(0xffffffffu, base, 0);
-      n = __shfl_sync(0xffffffffu, n, 0);
-      left = __shfl_sync(0xffffffffu, left, 0);
-      queue_empty = left <= n;
+      const unsigned idle = __ballot_sync(0xffffffffu, !have);
       const int r = __popc(idle & lt_mask);
-      if (((idle >> lane) & 1u) && r < n) {
-        pend_k = base + r;
-        pend_polls = 0;
+      const int take = min(__popc(idle), qn);
+      if (((idle >> lane) & 1u) && r < take) {
+        const int e = qn - 1 - r;
+        start_secondary(s_qa[wid][e], s_qb[wid][e], 0x80000000u | ((uint32_t)(blockIdx.x * kWarps + wid) << 12) |
+                                                       ((uint32_t)(sec_id + r) & 0xFFFu));
       }
-      if (!have && pend_k >= 0) {
-        if (*(volatile unsigned int*)&a.sec_ready[pend_k] == ready_tag) {
-          __threadfence();
-          const int k = pend_k;
-          pend_k = -1;
-          const float4 A = __ldcg(&a.sec[2 * k]);
-          const float4 B = __ldcg(&a.sec[2 * k + 1]);
-          slot = -1 - k;
-          p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
-          v = make_float3(B.x, B.y, B.z);
-          s = -1.0f;
-          t = A.w;
-          time_adj += T - t;  // electron-time this secondary adds to the interval
-          rng.init(0x80000000u | (uint32_t)k, interval, a.seed, a.salt + 1u);
-          energy = energy_of(v, hme);
-          events = 0;
-          have = true;
-        } else if (++pend_polls > (1 << 24)) {
-          atomicExch(a.error_flag, 6);  // never published
-          pend_k = -1;
+      sec_id += take;
+      qn -= take;
+      __syncwarp();
+      if (lane == 0) s_qn[wid] = qn;
+      if (drain) {
+        const unsigned idle2 = __ballot_sync(0xffffffffu, !have);
+        const int cnt = min(*(volatile int*)a.spill_count, a.spill_cap);
+        const int r2 = __popc(idle2 & lt_mask);
+        const int take2 = min(__popc(idle2), cnt - sp_next);
+        if (((idle2 >> lane) & 1u) && r2 < take2) {
+          const int k = sp_next + r2;
+          start_secondary(__ldcg(&a.spill[2 * k]), __ldcg(&a.spill[2 * k + 1]), 0xC0000000u | (uint32_t)k);
         }
+        sp_next += max(take2, 0);
       }
     }
-    if (!__any_sync(0xffffffffu, have || pend_k >= 0)) {
-      if (exhausted && queue_empty) break;
+    if (!__any_sync(0xffffffffu, have)) {
+      const bool spill_left = drain && sp_next < min(*(volatile int*)a.spill_count, a.spill_cap);
+      if (exhausted && qn == 0 && !spill_left) break;
       continue;
     }
     if (!have) continue;
@@ -256,14 +256,20 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
         else atomicAdd(&s_loss[cr.chosen], cr.dE);
         const int ptype = s_proc[cr.chosen].type;
         if (ptype == kIonization) {
-          const int k = append_slot(a.sec_count);
-          if (k < a.sec_cap) {
-            __stcg(&a.sec[2 * k], make_float4(p.x, p.y, p.z, t));
-            __stcg(&a.sec[2 * k + 1], make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f));
-            __threadfence();
-            atomicExch(&a.sec_ready[k], ready_tag);
+          const float4 A = make_float4(p.x, p.y, p.z, t);
+          const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
+          const int k = atomicAdd(&s_qn[wid], 1);
+          if (k < kLocalQ) {
+            s_qa[wid][k] = A;
+            s_qb[wid][k] = B;
           } else {
-            atomicExch(a.error_flag, 2);  // secondary buffer full: the host reports it
+            const int g = append_slot(a.spill_count);
+            if (g < a.spill_cap) {
+              a.spill[2 * g] = A;
+              a.spill[2 * g + 1] = B;
+            } else {
+              atomicExch(a.error_flag, 2);  // spill buffer full: the host reports it
+            }
           }
         } else if (ptype == kAttachment) {
           dead = true;
@@ -282,9 +288,18 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
       }
     }
     if (finished) {
-      float4* dst = slot >= 0 ? a.state + 2 * slot : a.sec + 2 * (-1 - slot);
-      dst[0] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
-      dst[1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
+      if (slot >= 0) {
+        a.state[2 * slot] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
+        a.state[2 * slot + 1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
+      } else if (!dead) {
+        const int k = append_slot(a.sec_count);
+        if (k < a.sec_cap) {
+          a.sec[2 * k] = make_float4(p.x, p.y, p.z, s);
+          a.sec[2 * k + 1] = make_float4(v.x, v.y, v.z, 0.0f);
+        } else {
+          atomicExch(a.error_flag, 2);
+        }
+      }
       if (!dead) e_max = fmaxf(e_max, energy);
       have = false;
     }

@@ -34,13 +34,14 @@ struct AdvanceArgs {
   const ProcF* procs;
   const GasF* gases;
   int P;
-  // secondaries: created as (x, y, z, t_c), (vx, vy, vz, 0); after their
-  // advance (x, y, z, s), (vx, vy, vz, dead flag) at the end of the interval
+  // secondaries pushed to the end of the interval: (x, y, z, s), (vx, vy, vz, 0)
   float4* sec;
   int* sec_count;
-  int* sec_next;                   // queue cursor over the secondaries
-  unsigned int* sec_ready;         // per-entry publication tag (interval index + 1) set after the data
   int sec_cap;
+  // secondaries a warp could not keep in its own queue: (x, y, z, t_c), (vx, vy, vz, 0)
+  float4* spill;
+  int* spill_count;
+  int spill_cap;
   int* att_list;                   // attached ensemble slots
   int* att_count;
   unsigned long long* proc_count;  // [P]
@@ -55,7 +56,7 @@ struct AdvanceArgs {
   int* work_counter;               // chunk counter of the persistent grid (zero before the launch)
   int sm_count;
   const IntervalCtl* ctl;          // when set: per-interval values are read from here
-  int queue_only;                  // 1: only drain the secondary queue (one warp)
+  int queue_only;                  // 1: only drain the spilled secondaries (one warp)
 };
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);
