@@ -38,6 +38,10 @@ T_GAS = 300.0
 E_N = 200.0
 N_ELECTRONS = 1_000_000
 STATE_BYTES_PER_ELECTRON_STEP = 64  # 32 B state read + 32 B written per electron per interval
+# DRAM bytes per electron and interval of k_advance, from one ncu capture of the
+# same kernel on 4e6 electrons (profiles/k_advance_n2_dc200.md): 130.5 MB read +
+# 73.6 MB written; traffic grows in proportion to the electrons advanced
+DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
 WORKLOAD = "n2_like_dc200Td_1e6e"
 
 
@@ -163,6 +167,19 @@ def run_reference_arm(args):
 
 
 # --------------------------------------------------------------------- GPU arm
+def aggregate_ranks(total_ms, real, null, device):
+    """Replicas only: every rank advances its own ensemble; the job time is the
+    slowest rank's, the collisions are summed over ranks."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    c = torch.tensor([real, null], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(c[0]), float(c[1])
+
+
 def run_gpu_arm(args):
     import torch
 
@@ -226,13 +243,7 @@ def run_gpu_arm(args):
     real = r1.real_collisions - r0.real_collisions
     null = r1.null_collisions - r0.null_collisions
     if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([total_ms, real, null], dtype=torch.float64, device=f"cuda:{local}")
-        mx = tt.clone()
-        dist.all_reduce(mx[0:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
-        total_ms, real, null = float(mx[0]), float(tt[1]), float(tt[2])
+        total_ms, real, null = aggregate_ranks(total_ms, real, null, torch.device("cuda", local))
     value = real / (total_ms * 1e-3)
 
     adv_ms = t1.advance_ms - t0.advance_ms
@@ -281,7 +292,9 @@ def run_gpu_arm(args):
                        "relax_intervals": args.relax, "l2": "256 MiB flush before every timed step",
                        "null_collisions_per_s": null / (total_ms * 1e-3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": DRAM_BYTES_PER_ELECTRON_STEP * args.electrons,
+                         "traffic_source": "ncu dram__bytes_read+write of k_advance at 4e6 electrons, scaled per electron",
                          "kernel": "k_advance", "peak_source": peak_kind,
                          "algorithmic_bytes": f"{STATE_BYTES_PER_ELECTRON_STEP} B per electron-interval",
                          "kernel_ms_per_launch": adv_ms / max(adv_n, 1)},

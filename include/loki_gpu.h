@@ -192,6 +192,13 @@ int lgpu_get_distributions(lgpu_ctx* ctx, double* eedf_cells, double* eedf, doub
                            double* eadf, double* evdf, double* radial_cells, double* axial_cells,
                            double* eedf_periodic);
 
+/* Phase-resolved averages of an AC solve (BoltzmannMC.C:1468-1481, 1728-1734):
+ * per integration phase the number of samples and the averages of the mean
+ * energy, flux and bulk velocity (x3) and flux and bulk diffusion (x9).
+ * Arrays have n_phases rows; any pointer may be NULL. */
+int lgpu_get_periodic(lgpu_ctx* ctx, double* n_points, double* mean_energy, double* flux_v, double* bulk_v,
+                      double* flux_d, double* bulk_d);
+
 /* Sampled time series (BoltzmannMC.h:124-175). which: 0 samplingTimes,
  * 1 meanEnergies, 2 meanPositions (x3), 3 meanVelocities (x3),
  * 4 fluxDiffusionCoeffs (x9), 5 positionCovariances (x9), 6 bulkVelocities (x3),

@@ -1166,6 +1166,25 @@ class Engine {
     return LGPU_OK;
   }
 
+  // getAveragedPeriodicParams (BoltzmannMC.C:1728-1734)
+  int periodic(double* n, double* me, double* fv, double* bv, double* fd, double* bd) const {
+    const int nPh = (int)phase_n_.size();
+    for (int q = 0; q < nPh; ++q) {
+      const double c = phase_n_[q];
+      if (n) n[q] = c;
+      if (me) me[q] = phase_me_[q] / c;
+      for (int k = 0; k < 3; ++k) {
+        if (fv) fv[3 * q + k] = phase_fv_[3 * q + k] / c;
+        if (bv) bv[3 * q + k] = phase_bv_[3 * q + k] / c;
+      }
+      for (int k = 0; k < 9; ++k) {
+        if (fd) fd[9 * q + k] = phase_fd_[9 * q + k] / c;
+        if (bd) bd[9 * q + k] = phase_bd_[9 * q + k] / c;
+      }
+    }
+    return LGPU_OK;
+  }
+
   long long series(int which, double* out, long long max_rows) {
     const std::vector<double>* v = nullptr;
     int w = 1;
@@ -1499,6 +1518,11 @@ int lgpu_get_distributions(lgpu_ctx* ctx, double* cells, double* eedf, double* e
                            double* evdf, double* rcells, double* acells, double* eedf_per) {
   CTX_CHECK(ctx);
   return ctx->e->distributions(cells, eedf, efadf, esadf, eadf, evdf, rcells, acells, eedf_per);
+}
+
+int lgpu_get_periodic(lgpu_ctx* ctx, double* n, double* me, double* fv, double* bv, double* fd, double* bd) {
+  CTX_CHECK(ctx);
+  return ctx->e->periodic(n, me, fv, bv, fd, bd);
 }
 
 long long lgpu_get_series(lgpu_ctx* ctx, int which, double* out, long long max_rows) {

@@ -25,7 +25,8 @@ STATUS = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ENERGY_ABOVE_TABLE", 4: "TIMEOUT"
 
 EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_stream",
             "lgpu_set_processes", "lgpu_set_conditions", "lgpu_init_ensemble", "lgpu_advance", "lgpu_solve",
-            "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_series", "lgpu_get_timing",
+            "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
+            "lgpu_get_timing",
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions")
 
 
@@ -110,6 +111,7 @@ def load(path: str | None = None):
     lib.lgpu_solve.argtypes = [ctypes.c_void_p, P_(Result)]
     lib.lgpu_get_process_results.argtypes = [ctypes.c_void_p, P_(ctypes.c_ulonglong), P_(D), P_(D), P_(D), I]
     lib.lgpu_get_distributions.argtypes = [ctypes.c_void_p] + [P_(D)] * 9
+    lib.lgpu_get_periodic.argtypes = [ctypes.c_void_p] + [P_(D)] * 6
     lib.lgpu_get_series.argtypes = [ctypes.c_void_p, I, P_(D), LL]
     lib.lgpu_get_series.restype = LL
     lib.lgpu_get_timing.argtypes = [ctypes.c_void_p, P_(Timing)]
@@ -231,6 +233,14 @@ class Context:
                    axial_cells=np.zeros(nA), eedf_periodic=np.zeros((nPh, nEC)))
         self.check(self.lib.lgpu_get_distributions(self.h, *[dptr(out[k]) for k in (
             "eedf_cells", "eedf", "efadf", "esadf", "eadf", "evdf", "radial_cells", "axial_cells", "eedf_periodic")]))
+        return out
+
+    def periodic(self):
+        nPh = self.cfg.n_phases
+        out = dict(n=np.zeros(nPh), mean_energy=np.zeros(nPh), flux_v=np.zeros((nPh, 3)),
+                   bulk_v=np.zeros((nPh, 3)), flux_d=np.zeros((nPh, 9)), bulk_d=np.zeros((nPh, 9)))
+        self.check(self.lib.lgpu_get_periodic(self.h, *[dptr(out[k]) for k in (
+            "n", "mean_energy", "flux_v", "bulk_v", "flux_d", "bulk_d")]))
         return out
 
     def series(self, which, width):

@@ -1,0 +1,33 @@
+"""The drop-in entry point (loki-mc_gb300/adapter/) builds with the
+reference's own sources and runs a setup up to the GPU backend: without a
+device it must stop the reference's way (Message::error, errorLog.txt), with
+no CPU fallback. Needs the reference source tree; skipped elsewhere."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference/Code"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference source tree not present")
+def test_dropin_reaches_the_backend(tmp_path):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a CUDA device is present: the run would not stop at the backend")
+    except ImportError:
+        pass
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={REF}", "dropin"])
+    sys.path.insert(0, os.path.join(ROOT, "loki-mc_gb300", "python"))
+    from lokigpu import synth
+
+    synth.write_case(str(tmp_path), [synth.atomic_gas()], pressure_pa=3.22e22 * 1.38064852e-23 * 300,
+                     red_field=100.0, n_electrons=1000, kte_init_ev=1.0,
+                     extra_numerics={"backend": "gpu", "nIntegrationPoints": "500"})
+    r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "lokimc_gpu"), "case.in", "1"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=120)
+    log = (tmp_path / "errorLog.txt").read_text()
+    assert "lgpu_create: no CUDA device" in log, r.stdout[-2000:]
