@@ -235,6 +235,25 @@ int lgpu_replay_flights(lgpu_ctx* ctx, int n, const double* t, const double* dt,
 int lgpu_replay_collisions(lgpu_ctx* ctx, int n, const double* nu_trial, const double* vel, const double* energy,
                            const double* uniforms, int u_stride, double* out, int* used);
 
+/* ---- free flights without device allocation ----
+ *
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory - a serving process that reserved the device up front, a host
+ * application whose allocator owns the device, a pipeline stage that must not
+ * allocate or synchronise on an allocation - this runs the same free-flight
+ * kernel as lgpu_replay_flights without a context: inputs and outputs are the
+ * caller's host arrays, staged through a static device array of at most 4096
+ * flights (512 KiB, held on every GPU that loads the library until exit).
+ * More than 4096 flights return LGPU_ERR_BAD_ARG. The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress), so make it before any
+ * stream capture. Calls share the array: calls that overlap on the GPU (from
+ * several host threads or streams) race. Synchronous: returns when the outputs
+ * are written. The field arguments are those of lgpu_set_field_raw. */
+int lgpu_replay_flights_noalloc(int device, const double e_field[3], double freq_hz, double red_mag_hx,
+                                double cyclotron, int n, const double* t, const double* dt, const double* pos,
+                                const double* vel, double* pos_out, double* vel_out, double* energy_out,
+                                double* gain_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,8 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_set_processes", "lgpu_set_conditions", "lgpu_init_ensemble", "lgpu_advance", "lgpu_solve",
             "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
             "lgpu_get_timing",
-            "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions")
+            "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
+            "lgpu_replay_flights_noalloc")
 
 
 class LokiGpuError(RuntimeError):
@@ -119,6 +120,7 @@ def load(path: str | None = None):
     lib.lgpu_set_field_raw.argtypes = [ctypes.c_void_p, P_(D), D, D, D]
     lib.lgpu_replay_flights.argtypes = [ctypes.c_void_p, I] + [P_(D)] * 8
     lib.lgpu_replay_collisions.argtypes = [ctypes.c_void_p, I, P_(D), P_(D), P_(D), P_(D), I, P_(D), P_(I)]
+    lib.lgpu_replay_flights_noalloc.argtypes = [I, P_(D), D, D, D, I] + [P_(D)] * 8
     _lib = lib
     return lib
 
@@ -133,6 +135,24 @@ def default_config(**kw) -> Config:
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+def replay_flights_noalloc(device, E, freq_hz, red_mag, cyclotron, t, dt, pos, vel):
+    """lgpu_replay_flights_noalloc: free flights staged through the library's
+    static device array, without a context or any device allocation."""
+    lib = load()
+    n = len(t)
+    t = np.ascontiguousarray(t, np.float64)
+    dt = np.ascontiguousarray(dt, np.float64)
+    pos = np.ascontiguousarray(pos, np.float64).reshape(n, 3)
+    vel = np.ascontiguousarray(vel, np.float64).reshape(n, 3)
+    e = np.ascontiguousarray(E, np.float64)
+    po, vo, eo, go = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n), np.zeros(n)
+    rc = lib.lgpu_replay_flights_noalloc(int(device), dptr(e), float(freq_hz), float(red_mag), float(cyclotron), n,
+                                         dptr(t), dptr(dt), dptr(pos), dptr(vel), dptr(po), dptr(vo), dptr(eo), dptr(go))
+    if rc != LGPU_OK:
+        raise LokiGpuError(rc, "lgpu_replay_flights_noalloc failed")
+    return po, vo, eo, go
 
 
 class Context:
