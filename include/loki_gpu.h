@@ -254,6 +254,109 @@ int lgpu_replay_flights_noalloc(int device, const double e_field[3], double freq
                                 const double* vel, double* pos_out, double* vel_out, double* energy_out,
                                 double* gain_out);
 
+/* ---- batches: many swarm conditions per launch sequence ----
+ *
+ * No counterpart in the reference, which solves one condition per run
+ * (lokimc.C:78-80); a sweep there is one run per setup. A batch solves many
+ * contexts together: each context keeps its own ensemble, tables, tallies and
+ * host control flow (the steps of lgpu_solve, BoltzmannMC.C:299-426), while
+ * each synchronisation interval of all of them is one launch sequence (a CUDA
+ * graph) over every context's electrons. Contexts are created on the batch's
+ * device with processes and conditions set, and may differ in everything
+ * (mixture, field, electron count, numerics). When more contexts are added
+ * than the batch has slots, the rest start as running ones finish. After
+ * lgpu_batch_run every lgpu_get_* call on a context works as after lgpu_solve;
+ * lgpu_solve and lgpu_advance refuse a context while a batch holds it. */
+typedef struct lgpu_batch lgpu_batch;
+
+typedef struct lgpu_batch_report {
+  long long intervals;          /* batched launch sequences */
+  long long kernel_launches;    /* kernels launched for them */
+  double elapsed;               /* wall time of the run (s) */
+  double real_collisions;       /* summed over the contexts */
+  double null_collisions;
+  double advance_ms;            /* device time of the advance launches */
+  double electron_steps;        /* electrons x intervals advanced */
+  double h2d_bytes, d2h_bytes;  /* host<->device copies of the batched intervals */
+} lgpu_batch_report;
+
+int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);
+int lgpu_batch_destroy(lgpu_batch* batch);
+int lgpu_batch_last_error(const lgpu_batch* batch, char* buf, size_t size);
+/* Queues a context for the next lgpu_batch_run (not owned by the batch). */
+int lgpu_batch_add(lgpu_batch* batch, lgpu_ctx* ctx);
+/* Solves every queued context; results[i] and status[i] (an LGPU_* code) are
+ * those of the i-th added context (n = number added). The batch is empty
+ * afterwards. Returns LGPU_OK when the batch itself ran, whatever the
+ * contexts' own status. */
+int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, lgpu_batch_report* report);
+
+/* ---- serving: continuous batching of swarm jobs ----
+ *
+ * No counterpart in the reference. A server owns one device and one thread
+ * that runs a batch without pause: submitted jobs wait in arrival order and
+ * are admitted while a slot is free and their device footprint (ensemble,
+ * secondary buffers, tables, tallies) fits the memory budget; every
+ * synchronisation interval advances all admitted jobs in one launch sequence;
+ * a job leaves when its own stop criteria hold, its results are copied to the
+ * host and its device memory is freed for the next admission. Jobs are
+ * independent: each result is that of lgpu_solve on the same input, within
+ * the statistical tolerance of a Monte Carlo run. Submission is thread-safe. */
+typedef struct lgpu_server lgpu_server;
+
+typedef struct lgpu_job {
+  lgpu_config config;             /* config.device is ignored: the server's device */
+  const lgpu_process* procs;      /* copied at submission, raw cross sections included */
+  int n_procs;
+  const lgpu_gas* gases;
+  int n_gases;
+  double emax_elastic;            /* as lgpu_set_processes */
+  lgpu_conditions conditions;
+} lgpu_job;
+
+#define LGPU_JOB_QUEUED 0
+#define LGPU_JOB_RUNNING 1
+#define LGPU_JOB_DONE 2
+#define LGPU_JOB_FAILED 3
+#define LGPU_JOB_CANCELLED 4
+
+typedef struct lgpu_job_status {
+  int state;                      /* LGPU_JOB_* */
+  int status;                     /* LGPU_* code of a failed job */
+  double submit_time;             /* seconds since the server started */
+  double start_time;              /* admission */
+  double end_time;                /* results available */
+  double footprint_bytes;         /* device memory the job held */
+  lgpu_result result;
+} lgpu_job_status;
+
+typedef struct lgpu_server_report {
+  long long submitted, completed, failed, running, queued;
+  long long intervals;            /* batched launch sequences so far */
+  double real_collisions;         /* of completed jobs */
+  double null_collisions;
+  double busy_seconds;            /* wall time with at least one job admitted */
+  double peak_footprint_bytes;
+} lgpu_server_report;
+
+/* max_slots: jobs advanced together; memory_budget_bytes: device memory the
+ * admitted jobs may hold (0: 80% of the free memory at start). */
+int lgpu_server_start(int device, int max_slots, double memory_budget_bytes, lgpu_server** out);
+int lgpu_server_submit(lgpu_server* server, const lgpu_job* job, long long* job_id);
+int lgpu_server_poll(lgpu_server* server, long long job_id, lgpu_job_status* status);
+/* Blocks until the job is done, failed or cancelled, or timeout_s passes
+ * (LGPU_ERR_TIMEOUT; timeout_s <= 0 waits without limit). */
+int lgpu_server_wait(lgpu_server* server, long long job_id, double timeout_s, lgpu_job_status* status);
+/* Per-process collision counts and rate coefficients of a finished job
+ * (as lgpu_get_process_results; n = the job's process count). */
+int lgpu_server_job_rates(lgpu_server* server, long long job_id, unsigned long long* counts, double* rate, int n);
+/* A queued job is dropped; a running one stops at its next interval. */
+int lgpu_server_cancel(lgpu_server* server, long long job_id);
+int lgpu_server_report_get(lgpu_server* server, lgpu_server_report* report);
+int lgpu_server_last_error(const lgpu_server* server, char* buf, size_t size);
+/* Cancels what is left, joins the thread, frees the device memory. */
+int lgpu_server_stop(lgpu_server* server);
+
 #ifdef __cplusplus
 }
 #endif

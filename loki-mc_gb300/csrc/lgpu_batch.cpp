@@ -1,0 +1,83 @@
+// lgpu_batch.cpp - the batch entry points of include/loki_gpu.h over lgpu::Batch.
+#include "lgpu_batch.h"
+
+#include <new>
+
+extern "C" {
+
+int lgpu_batch_create(int device, int max_slots, lgpu_batch** out) {
+  if (!out) return LGPU_ERR_BAD_ARG;
+  *out = nullptr;
+  lgpu::Batch* b = new (std::nothrow) lgpu::Batch();
+  if (!b) return LGPU_ERR_OOM;
+  lgpu_batch* h = new (std::nothrow) lgpu_batch{b};
+  if (!h) {
+    delete b;
+    return LGPU_ERR_OOM;
+  }
+  *out = h;
+  return b->init(device, max_slots);
+}
+
+int lgpu_batch_destroy(lgpu_batch* batch) {
+  if (!batch) return LGPU_OK;
+  delete batch->b;
+  delete batch;
+  return LGPU_OK;
+}
+
+int lgpu_batch_last_error(const lgpu_batch* batch, char* buf, size_t size) {
+  if (!batch || !batch->b) return 0;
+  const std::string& s = batch->b->err_;
+  if (buf && size) std::snprintf(buf, size, "%s", s.c_str());
+  return (int)s.size();
+}
+
+int lgpu_batch_add(lgpu_batch* batch, lgpu_ctx* ctx) {
+  if (!batch || !batch->b || !ctx || !ctx->e) return LGPU_ERR_BAD_ARG;
+  return batch->b->add(ctx->e);
+}
+
+int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, lgpu_batch_report* report) {
+  if (!batch || !batch->b) return LGPU_ERR_BAD_ARG;
+  lgpu::Batch& b = *batch->b;
+  if (n != (int)b.members_.size()) return b.fail(LGPU_ERR_BAD_ARG, "n must be the number of added contexts");
+  const long long i0 = b.intervals_, l0 = b.launches_;
+  const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_;
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = b.run();
+  const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  // a failed launch sequence ends every member that is still running
+  for (auto& m : b.members_)
+    if (!m.done) {
+      if (m.started) m.e->sync("batch");
+      m.status = rc != LGPU_OK ? rc : LGPU_ERR_STATE;
+      m.done = true;
+      m.e->leave_batch();
+    }
+  double real = 0, null = 0;
+  for (int i = 0; i < n; ++i) {
+    const auto& m = b.members_[i];
+    if (results) results[i] = m.result;
+    if (status) status[i] = m.status;
+    real += m.result.real_collisions;
+    null += m.result.null_collisions;
+  }
+  if (report) {
+    report->intervals = b.intervals_ - i0;
+    report->kernel_launches = b.launches_ - l0;
+    report->elapsed = elapsed;
+    report->real_collisions = real;
+    report->null_collisions = null;
+    report->advance_ms = b.adv_ms_ - a0;
+    report->electron_steps = b.electron_steps_ - s0;
+    report->h2d_bytes = b.h2d_bytes_ - u0;
+    report->d2h_bytes = b.d2h_bytes_ - d0;
+  }
+  b.members_.clear();
+  b.active_.clear();
+  b.next_start_ = 0;
+  return rc;
+}
+
+}  // extern "C"

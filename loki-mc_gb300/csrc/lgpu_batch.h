@@ -1,0 +1,302 @@
+// lgpu_batch.h - many swarm conditions per launch sequence.
+//
+// A Batch drives any number of Engines (one swarm condition each) through
+// their own solve steps - the control flow of BoltzmannMC::evaluateEEDF
+// (BoltzmannMC.C:299-426) stays per condition, on the host - while the device
+// work of one synchronisation interval of every running condition is one CUDA
+// graph launch: slot control blocks and scalars (prep), deferred distribution
+// tallies, one persistent advance launch per field branch over all slots'
+// electrons, the drain of spilled secondaries, population control (one block
+// per slot), the moment sums and a gather of every slot's scalars, followed by
+// a single read-back. Per interval the host stages one BatchSlot per running
+// condition (the argument blocks the single-condition launches take, plus the
+// interval's control block) into pinned memory and copies it over once.
+//
+// Slots: at most max_slots conditions run at a time; conditions beyond that
+// wait in order of addition and start as running ones finish, so a long run
+// of uneven conditions keeps the device busy (continuous batching).
+#pragma once
+
+#include <algorithm>
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "lgpu_engine.h"
+
+namespace lgpu {
+
+class Batch {
+ public:
+  std::string err_;
+  int device_ = 0, max_slots_ = 0, sm_count_ = 1;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  char* h_stage_ = nullptr;
+  char* d_stage_ = nullptr;
+  DevScalars* h_gather_ = nullptr;
+  DevScalars* d_gather_ = nullptr;
+  cudaGraphExec_t graph_ = nullptr;
+  long long graph_kernels_ = 0;
+  // totals since creation
+  long long intervals_ = 0, launches_ = 0;
+  double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
+
+  struct Member {
+    Engine* e = nullptr;
+    bool started = false, done = false;
+    int status = LGPU_OK;
+    lgpu_result result{};
+  };
+  std::vector<Member> members_;
+  std::vector<int> active_;  // started, unfinished members
+  size_t next_start_ = 0;    // first member not started yet
+
+  ~Batch() { release(); }
+
+  int fail(int code, const std::string& msg) {
+    err_ = msg;
+    return code;
+  }
+  int cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return LGPU_OK;
+    return fail(e == cudaErrorMemoryAllocation ? LGPU_ERR_OOM : LGPU_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+  }
+
+  static size_t stage_bytes() { return batch_slots_offset() + (size_t)kBatchMaxSlots * sizeof(BatchSlot); }
+
+  int init(int device, int max_slots) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LGPU_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(LGPU_ERR_BAD_ARG, "device out of range");
+    if (max_slots < 1 || max_slots > kBatchMaxSlots)
+      return fail(LGPU_ERR_BAD_ARG, "max_slots must be 1.." + std::to_string(kBatchMaxSlots));
+    device_ = device;
+    max_slots_ = max_slots;
+    int rc;
+    if ((rc = cuda(cudaSetDevice(device), "cudaSetDevice"))) return rc;
+    if ((rc = cuda(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device), "attribute"))) return rc;
+    if ((rc = cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream"))) return rc;
+    if ((rc = cuda(cudaEventCreate(&ev0_), "event")) || (rc = cuda(cudaEventCreate(&ev1_), "event"))) return rc;
+    const size_t sb = stage_bytes();
+    if ((rc = cuda(cudaMallocHost((void**)&h_stage_, sb), "cudaMallocHost"))) return rc;
+    if ((rc = cuda(cudaMalloc((void**)&d_stage_, sb), "cudaMalloc"))) return rc;
+    std::memset(h_stage_, 0, sb);
+    if ((rc = cuda(cudaMemsetAsync(d_stage_, 0, sb, stream_), "memset"))) return rc;
+    if ((rc = cuda(cudaMallocHost((void**)&h_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMallocHost")))
+      return rc;
+    if ((rc = cuda(cudaMalloc((void**)&d_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMalloc"))) return rc;
+    return cuda(cudaStreamSynchronize(stream_), "init");
+  }
+
+  void release() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (Member& m : members_)
+      if (m.e && !m.done) m.e->leave_batch();
+    members_.clear();
+    active_.clear();
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+    if (d_stage_) cudaFree(d_stage_);
+    if (h_stage_) cudaFreeHost(h_stage_);
+    if (d_gather_) cudaFree(d_gather_);
+    if (h_gather_) cudaFreeHost(h_gather_);
+    d_stage_ = h_stage_ = nullptr;
+    d_gather_ = h_gather_ = nullptr;
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    ev0_ = ev1_ = nullptr;
+    if (stream_) cudaStreamDestroy(stream_);
+    stream_ = nullptr;
+  }
+
+  BatchArgs args() const {
+    BatchArgs b{};
+    b.hdr = reinterpret_cast<BatchHeader*>(d_stage_);
+    b.adv_prefix = reinterpret_cast<const int*>(d_stage_ + batch_prefix_offset());
+    b.smp_prefix = b.adv_prefix + (kBatchMaxSlots + 1);
+    b.hist_prefix = b.smp_prefix + (kBatchMaxSlots + 1);
+    b.slots = reinterpret_cast<const BatchSlot*>(d_stage_ + batch_slots_offset());
+    b.gather = d_gather_;
+    return b;
+  }
+
+  // the kernels of one interval, captured once (their sizes come from the
+  // staged header, so one graph serves every interval and every membership)
+  int graph(cudaGraphExec_t* out) {
+    if (!graph_) {
+      cudaGraph_t g;
+      int rc;
+      if ((rc = cuda(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture"))) return rc;
+      const BatchArgs b = args();
+      launch_batch_pre(b, sm_count_, max_slots_, stream_);
+      cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
+      launch_batch_advance(b, sm_count_, stream_);
+      cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
+      launch_batch_post(b, sm_count_, max_slots_, stream_);
+      if ((rc = cuda(cudaStreamEndCapture(stream_, &g), "capture"))) return rc;
+      rc = cuda(cudaGraphInstantiate(&graph_, g, 0), "instantiate");
+      cudaGraphDestroy(g);
+      if (rc) return rc;
+      graph_kernels_ = kBatchLaunches;
+    }
+    *out = graph_;
+    return LGPU_OK;
+  }
+
+  // ------------------------------------------------------------ membership
+  int add(Engine* e) {
+    if (!e) return fail(LGPU_ERR_BAD_ARG, "null context");
+    if (e->batch_) return fail(LGPU_ERR_STATE, "the context is already in a batch");
+    if (e->cfg_.device != device_) return fail(LGPU_ERR_BAD_ARG, "the context is on another device");
+    if (!e->have_procs_ || !e->have_cond_) return fail(LGPU_ERR_STATE, "set_processes and set_conditions come first");
+    for (const Member& m : members_)
+      if (m.e == e && !m.done) return fail(LGPU_ERR_BAD_ARG, "the context was added twice");
+    Member m;
+    m.e = e;
+    members_.push_back(m);
+    e->enter_batch(stream_);  // held by the batch from here on
+    return LGPU_OK;
+  }
+
+  void finish(Member& m, int rc) {
+    if (rc == LGPU_OK) rc = m.e->solve_end(&m.result);
+    if (rc != LGPU_OK) m.e->sync("finish");  // the context's own work ends before it leaves
+    m.status = rc;
+    m.done = true;
+    m.e->leave_batch();
+  }
+
+  // starts waiting members while slots are free
+  void admit() {
+    while ((int)active_.size() < max_slots_ && next_start_ < members_.size()) {
+      Member& m = members_[next_start_];
+      m.started = true;
+      const int rc = m.e->solve_begin();
+      if (rc != LGPU_OK) finish(m, rc);
+      else active_.push_back((int)next_start_);
+      ++next_start_;
+    }
+  }
+
+  bool idle() const { return active_.empty() && next_start_ >= members_.size(); }
+
+  // ends a running member between intervals with the given status
+  void stop_member(int idx, int status) {
+    Member& m = members_[idx];
+    if (!m.started || m.done) return;
+    m.e->sync("stop");
+    m.status = status;
+    m.done = true;
+    m.e->leave_batch();
+    active_.erase(std::remove(active_.begin(), active_.end(), idx), active_.end());
+  }
+
+  // One synchronisation interval of every running member. Members whose stop
+  // criteria hold (or that fail) finish here; *finished lists them.
+  int step(std::vector<int>* finished = nullptr) {
+    std::vector<int> go;
+    go.reserve(active_.size());
+    for (int idx : active_) {
+      Member& m = members_[idx];
+      bool done = false;
+      int rc = m.e->solve_next(&done);
+      if (rc == LGPU_OK && !done) rc = m.e->interval_pre();
+      if (rc != LGPU_OK || done) {
+        finish(m, rc);
+        if (finished) finished->push_back(idx);
+      } else {
+        go.push_back(idx);
+      }
+    }
+    active_ = go;
+    if (go.empty()) return LGPU_OK;
+    // slots ordered by field branch: one advance launch per branch
+    std::stable_sort(go.begin(), go.end(),
+                     [&](int a, int b) { return members_[a].e->field_mode() < members_[b].e->field_mode(); });
+    const int n = (int)go.size();
+    auto* hdr = reinterpret_cast<BatchHeader*>(h_stage_);
+    int* ap = reinterpret_cast<int*>(h_stage_ + batch_prefix_offset());
+    int* sp = ap + (kBatchMaxSlots + 1);
+    int* hp = sp + (kBatchMaxSlots + 1);
+    auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
+    int na = 0, ns = 0, nh = 0;
+    double electrons = 0;
+    for (int s = 0; s < n; ++s) {
+      Engine* e = members_[go[s]].e;
+      e->fill_slot(&sl[s]);
+      const int N = e->n_electrons();
+      electrons += N;
+      ap[s] = na;
+      sp[s] = ns;
+      hp[s] = nh;
+      na += (N + kBatchAdvanceChunk - 1) / kBatchAdvanceChunk;
+      if (sl[s].flags & kSlotSample) ns += (N + kBatchSampleChunk - 1) / kBatchSampleChunk;
+      if (sl[s].flags & kSlotHist) nh += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+    }
+    ap[n] = na;
+    sp[n] = ns;
+    hp[n] = nh;
+    std::memset(hdr, 0, sizeof(BatchHeader));
+    hdr->n_slots = n;
+    hdr->adv_chunks = na;
+    hdr->smp_chunks = ns;
+    hdr->hist_chunks = nh;
+    for (int m = 0, s = 0; m <= kFieldModes; ++m) {
+      while (s < n && members_[go[s]].e->field_mode() < m) ++s;
+      hdr->mode_chunk[m] = ap[s];
+    }
+    cudaGraphExec_t ge;
+    int rc;
+    if ((rc = graph(&ge))) return rc;
+    const size_t up = batch_slots_offset() + (size_t)n * sizeof(BatchSlot);
+    const size_t down = (size_t)n * sizeof(DevScalars);
+    if ((rc = cuda(cudaMemcpyAsync(d_stage_, h_stage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
+    if ((rc = cuda(cudaGraphLaunch(ge, stream_), "graph launch"))) return rc;
+    if ((rc = cuda(cudaMemcpyAsync(h_gather_, d_gather_, down, cudaMemcpyDeviceToHost, stream_), "gather"))) return rc;
+    if ((rc = cuda(cudaStreamSynchronize(stream_), "batched interval"))) return rc;
+    if ((rc = cuda(cudaGetLastError(), "batched interval"))) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    adv_ms_ += ms;
+    electron_steps_ += electrons;
+    ++intervals_;
+    launches_ += graph_kernels_;
+    h2d_bytes_ += (double)up;
+    d2h_bytes_ += (double)down;
+    std::vector<int> still;
+    still.reserve(go.size());
+    for (int s = 0; s < n; ++s) {
+      Member& m = members_[go[s]];
+      std::memcpy(m.e->h_sc_, &h_gather_[s], sizeof(DevScalars));
+      rc = m.e->interval_post();
+      if (rc == LGPU_OK) rc = m.e->solve_post();
+      if (rc != LGPU_OK) {
+        finish(m, rc);
+        if (finished) finished->push_back(go[s]);
+      } else {
+        still.push_back(go[s]);
+      }
+    }
+    active_ = still;
+    return LGPU_OK;
+  }
+
+  // every added member to the end
+  int run() {
+    for (;;) {
+      admit();
+      if (active_.empty()) break;
+      const int rc = step();
+      if (rc != LGPU_OK) return rc;
+    }
+    return LGPU_OK;
+  }
+};
+
+}  // namespace lgpu
+
+struct lgpu_batch {
+  lgpu::Batch* b;
+};

@@ -127,8 +127,10 @@ struct ReplayStream {
 // w*t (AC, AC+B) or W*t (resonance) at the flight start, reduced to [0, 2pi)
 // by the caller in FP64. Position is an FP32 offset. Returns nothing; the
 // caller recomputes the energy from the new velocity.
+// MODE >= 0 selects the branch at compile time, -1 at run time from f.mode
+template <int MODE = -1>
 __device__ __forceinline__ void free_flight(const FieldF& f, float phi0, float dt, float3& p, float3& v) {
-  switch (f.mode) {
+  switch (MODE >= 0 ? MODE : f.mode) {
     case kFieldDC: {
       // x += v dt + a dt^2/2 ; v += a dt
       const float hdt2 = 0.5f * dt * dt;

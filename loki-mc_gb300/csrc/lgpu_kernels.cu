@@ -56,6 +56,7 @@ __device__ __forceinline__ int append_slot(int* counter) {
 
 constexpr int kAdvanceThreads = 256;
 constexpr int kAdvanceBlocksPerSM = 4;
+constexpr int kAdvanceWarps = kAdvanceThreads / 32;
 constexpr int kChunk = 128;  // electrons a warp takes from the global work counter at a time
 
 // ---------------------------------------------------------------- advance
@@ -71,96 +72,315 @@ constexpr int kChunk = 128;  // electrons a warp takes from the global work coun
 // the warp alive, so no warp ever waits on another. A warp whose queue is full
 // spills to a global buffer that the one-warp drain launch works off after.
 constexpr int kLocalQ = 32;
+
+// Shared memory of an advance block: constants and per-process tallies of the
+// block's current condition, the warps' secondary queues, reduction scratch.
+struct AdvShared {
+  unsigned int count[kMaxProcesses];
+  float gain[kMaxProcesses];
+  float loss[kMaxProcesses];
+  ProcF proc[kMaxProcesses];
+  GasF gas[kMaxGases];
+  float4 qa[kAdvanceWarps][kLocalQ];  // (x, y, z, t_c)
+  float4 qb[kAdvanceWarps][kLocalQ];  // (vx, vy, vz, 0)
+  int qn[kAdvanceWarps];
+  double red[kAdvanceWarps];
+  double redt[kAdvanceWarps];
+  unsigned long long redn[kAdvanceWarps];
+  unsigned long long redr[kAdvanceWarps];
+};
+
+// The values of one interval: launch arguments, overridden by the control block.
+struct IntervalView {
+  FieldF field;
+  TablesF tab;
+  float T, nu, inv_nu, phi0, phase_rate;
+  float3 shift;
+  uint64_t interval;
+};
+
+// MODE >= 0 fixes the field branch at compile time; -1 keeps the argument's
 template <int MODE>
-__device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
-  constexpr int kWarps = kAdvanceThreads / 32;
-  __shared__ unsigned int s_count[kMaxProcesses];
-  __shared__ float s_gain[kMaxProcesses];
-  __shared__ float s_loss[kMaxProcesses];
-  __shared__ ProcF s_proc[kMaxProcesses];
-  __shared__ GasF s_gas[kMaxGases];
-  __shared__ float4 s_qa[kWarps][kLocalQ];  // (x, y, z, t_c)
-  __shared__ float4 s_qb[kWarps][kLocalQ];  // (vx, vy, vz, 0)
-  __shared__ int s_qn[kWarps];
-  __shared__ double s_red[kWarps];
-  __shared__ double s_redt[kWarps];
-  __shared__ unsigned long long s_redn[kWarps];
-  __shared__ unsigned long long s_redr[kWarps];
-
-  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
-    s_count[q] = 0u;
-    s_gain[q] = 0.0f;
-    s_loss[q] = 0.0f;
-    s_proc[q] = a.procs[q];
-  }
-  if (threadIdx.x < a.c.G) s_gas[threadIdx.x] = a.gases[threadIdx.x];
-  if (threadIdx.x < kWarps) s_qn[threadIdx.x] = 0;
-  __syncthreads();
-
-  FieldF field = a.field;
-  field.mode = MODE;
-  float T = a.dt_sync, nu = a.nu, phi0 = a.phi0, phase_rate = a.phase_rate;
-  float3 shift = a.shift;
-  uint64_t interval = a.interval;
-  TablesF tab = a.t;
+__device__ __forceinline__ IntervalView interval_view(const AdvanceArgs& a) {
+  IntervalView iv;
+  iv.field = a.field;
+  if (MODE >= 0) iv.field.mode = MODE;
+  iv.tab = a.t;
+  iv.T = a.dt_sync;
+  iv.nu = a.nu;
+  iv.phi0 = a.phi0;
+  iv.phase_rate = a.phase_rate;
+  iv.shift = a.shift;
+  iv.interval = a.interval;
   if (a.ctl) {
     const IntervalCtl c = *a.ctl;
-    T = c.dt_sync;
-    nu = c.nu;
-    phi0 = c.phi0;
-    phase_rate = c.phase_rate;
-    shift = make_float3(c.shift_x, c.shift_y, c.shift_z);
-    interval = c.interval;
-    tab.inv_step = c.inv_step;
+    iv.T = c.dt_sync;
+    iv.nu = c.nu;
+    iv.phi0 = c.phi0;
+    iv.phase_rate = c.phase_rate;
+    iv.shift = make_float3(c.shift_x, c.shift_y, c.shift_z);
+    iv.interval = c.interval;
+    iv.tab.inv_step = c.inv_step;
   }
+  iv.inv_nu = 1.0f / iv.nu;
+  return iv;
+}
+
+// The electron a lane holds.
+struct Lane {
+  bool have;
+  int slot;  // ensemble slot, -1 for a secondary
+  float3 p, v;
+  float s, t, energy;
+  int events;
+  PcgStream rng;
+};
+
+// Per-lane sums of one condition, reduced when the block flushes.
+struct LaneTally {
+  float gain, time_adj, e_max;
+  unsigned int null_n, real_n;
+};
+
+__device__ __forceinline__ void reset_lane(Lane& L) {
+  L.have = false;
+  L.slot = 0;
+  L.p = make_float3(0.f, 0.f, 0.f);
+  L.v = make_float3(0.f, 0.f, 0.f);
+  L.s = -1.0f;
+  L.t = 0.0f;
+  L.energy = 0.0f;
+  L.events = 0;
+}
+
+__device__ __forceinline__ void reset_tally(LaneTally& tl) {
+  tl.gain = 0.0f;
+  tl.time_adj = 0.0f;
+  tl.e_max = 0.0f;
+  tl.null_n = 0u;
+  tl.real_n = 0u;
+}
+
+// process constants to shared memory, tallies and queues cleared
+__device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, AdvShared& sh) {
+  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
+    sh.count[q] = 0u;
+    sh.gain[q] = 0.0f;
+    sh.loss[q] = 0.0f;
+    sh.proc[q] = a.procs[q];
+  }
+  if (threadIdx.x < a.c.G) sh.gas[threadIdx.x] = a.gases[threadIdx.x];
+  if (threadIdx.x < kAdvanceWarps) sh.qn[threadIdx.x] = 0;
+}
+
+// an ensemble electron (left alone when its slot is attached)
+__device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const IntervalView& iv, Lane& L, int idx) {
+  const float4 A = a.state[2 * idx];
+  const float4 B = a.state[2 * idx + 1];
+  if (B.w == 0.0f) {
+    L.slot = idx;
+    L.p = make_float3(A.x - iv.shift.x, A.y - iv.shift.y, A.z - iv.shift.z);
+    L.v = make_float3(B.x, B.y, B.z);
+    L.s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
+    L.t = 0.0f;
+    L.rng.init((uint32_t)idx, iv.interval, a.seed, a.salt);
+    L.energy = energy_of(L.v, a.c.half_me_over_e);
+    L.events = 0;
+    L.have = true;
+  }
+}
+
+// a secondary, pushed from its creation time t_c = A.w
+__device__ __forceinline__ void lane_take_secondary(const AdvanceArgs& a, const IntervalView& iv, Lane& L,
+                                                    LaneTally& tl, float4 A, float4 B, uint32_t id) {
+  L.slot = -1;
+  L.p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
+  L.v = make_float3(B.x, B.y, B.z);
+  L.s = -1.0f;
+  L.t = A.w;
+  tl.time_adj += iv.T - L.t;  // electron-time this secondary adds to the interval
+  L.rng.init(id, iv.interval, a.seed, a.salt + 1u);
+  L.energy = energy_of(L.v, a.c.half_me_over_e);
+  L.events = 0;
+  L.have = true;
+}
+
+// idle lanes take secondaries from their warp's queue (newest first);
+// returns the entries left
+__device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const IntervalView& iv, AdvShared& sh, int wid,
+                                                int lane, unsigned lt_mask, Lane& L, LaneTally& tl, uint32_t& sec_id,
+                                                uint32_t id_hi, uint32_t id_mask) {
+  int qn = min(sh.qn[wid], kLocalQ);
+  const unsigned idle = __ballot_sync(0xffffffffu, !L.have);
+  const int r = __popc(idle & lt_mask);
+  const int take = min(__popc(idle), qn);
+  if (((idle >> lane) & 1u) && r < take) {
+    const int e = qn - 1 - r;
+    lane_take_secondary(a, iv, L, tl, sh.qa[wid][e], sh.qb[wid][e], id_hi | ((sec_id + (uint32_t)r) & id_mask));
+  }
+  sec_id += (uint32_t)take;
+  qn -= take;
+  __syncwarp();
+  if (lane == 0) sh.qn[wid] = qn;
+  return qn;
+}
+
+// One event of a lane's electron: a free flight to the next collision or,
+// when that lies beyond the synchronisation time, to the synchronisation time
+// (BoltzmannMC.C:650-675); the flight code is the same for both so the lanes
+// stay converged.
+template <int MODE>
+__device__ __forceinline__ void lane_event(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
+                                           Lane& L, LaneTally& tl) {
+  if (L.s < 0.0f) L.s = -__logf(L.rng.oo());
+  const float tau = L.s * iv.inv_nu;
+  const bool partial = L.t + tau > iv.T;
+  const float dt = partial ? iv.T - L.t : tau;
+  free_flight<MODE>(iv.field, iv.phi0 + iv.phase_rate * L.t, dt, L.p, L.v);
+  {
+    const float e1 = energy_of(L.v, a.c.half_me_over_e);
+    tl.gain += e1 - L.energy;
+    L.energy = e1;
+  }
+  bool finished = partial, dead = false;
+  if (partial) {
+    L.s = fmaxf(L.s - iv.nu * dt, 0.0f);
+  } else {
+    L.t += tau;
+    CollResult cr;
+    collide(a.c, iv.tab, sh.proc, sh.gas, iv.nu, L.v, L.energy, L.rng, cr);
+    if (cr.chosen < 0) {
+      ++tl.null_n;
+    } else {
+      ++tl.real_n;
+      atomicAdd(&sh.count[cr.chosen], 1u);
+      if (cr.dE >= 0.0f) atomicAdd(&sh.gain[cr.chosen], cr.dE);
+      else atomicAdd(&sh.loss[cr.chosen], cr.dE);
+      const int ptype = sh.proc[cr.chosen].type;
+      if (ptype == kIonization) {
+        const float4 A = make_float4(L.p.x, L.p.y, L.p.z, L.t);
+        const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
+        const int k = atomicAdd(&sh.qn[wid], 1);
+        if (k < kLocalQ) {
+          sh.qa[wid][k] = A;
+          sh.qb[wid][k] = B;
+        } else {
+          const int g = append_slot(a.spill_count);
+          if (g < a.spill_cap) {
+            a.spill[2 * g] = A;
+            a.spill[2 * g + 1] = B;
+          } else {
+            atomicExch(a.error_flag, 2);  // spill buffer full: the host reports it
+          }
+        }
+      } else if (ptype == kAttachment) {
+        dead = true;
+        finished = true;
+        tl.time_adj -= iv.T - L.t;  // electron-time the attached electron no longer spends
+        if (L.slot >= 0) {
+          const int k = append_slot(a.att_count);
+          a.att_list[k] = L.slot;
+        }
+      }
+    }
+    L.s = -__logf(L.rng.oo());  // next free flight (BoltzmannMC.C:670)
+    if (++L.events >= (1 << 20) && !finished) {
+      atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+      finished = true;
+    }
+  }
+  if (finished) {
+    if (L.slot >= 0) {
+      a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
+      a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
+    } else if (!dead) {
+      const int k = append_slot(a.sec_count);
+      if (k < a.sec_cap) {
+        a.sec[2 * k] = make_float4(L.p.x, L.p.y, L.p.z, L.s);
+        a.sec[2 * k + 1] = make_float4(L.v.x, L.v.y, L.v.z, 0.0f);
+      } else {
+        atomicExch(a.error_flag, 2);
+      }
+    }
+    if (!dead) tl.e_max = fmaxf(tl.e_max, L.energy);
+    L.have = false;
+  }
+}
+
+// block reductions of the lane sums and the per-process tallies -> the
+// condition's global tallies (every thread of the block calls this)
+__device__ __forceinline__ void block_flush(const AdvanceArgs& a, AdvShared& sh, const LaneTally& tl, int lane,
+                                            int wid) {
+  const double g = warp_sum((double)tl.gain);
+  const double ta = warp_sum((double)tl.time_adj);
+  const unsigned long long nn = warp_sum_u64((unsigned long long)tl.null_n);
+  const unsigned long long nr = warp_sum_u64((unsigned long long)tl.real_n);
+  const float em = warp_max(tl.e_max);
+  if (lane == 0) {
+    sh.red[wid] = g;
+    sh.redt[wid] = ta;
+    sh.redn[wid] = nn;
+    sh.redr[wid] = nr;
+    if (em > 0.0f) atomic_max_energy(a.max_energy_bits, em);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double gs = 0.0, ts = 0.0;
+    unsigned long long ns = 0, rs = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      gs += sh.red[w];
+      ts += sh.redt[w];
+      ns += sh.redn[w];
+      rs += sh.redr[w];
+    }
+    if (gs != 0.0) atomicAdd(a.field_gain, gs);
+    if (ts != 0.0) atomicAdd(a.time_adjust, ts);
+    if (ns) atomicAdd(a.null_count, ns);
+    if (rs) atomicAdd(a.real_count, rs);
+  }
+  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
+    if (sh.count[q]) {
+      atomicAdd(&a.proc_count[q], (unsigned long long)sh.count[q]);
+      if (sh.gain[q] != 0.0f) atomicAdd(&a.proc_gain[q], (double)sh.gain[q]);
+      if (sh.loss[q] != 0.0f) atomicAdd(&a.proc_loss[q], (double)sh.loss[q]);
+    }
+  }
+}
+
+// One condition: the ensemble in warp chunks from the global work counter
+// (or, drain, only the spilled secondaries).
+template <int MODE>
+__device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh) {
+  load_block_consts(a, sh);
+  __syncthreads();
+  const IntervalView iv = interval_view<MODE>(a);
   const bool drain = a.queue_only != 0;
   const int n_el = drain ? 0 : a.n;
-  const float inv_nu = 1.0f / nu;
-  const float hme = a.c.half_me_over_e;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
+  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 12);
 
-  float gain_sum = 0.0f, time_adj = 0.0f;
-  unsigned int null_n = 0, real_n = 0;
-  float e_max = 0.0f;
-
+  LaneTally tl;
+  reset_tally(tl);
+  Lane L;
+  reset_lane(L);
   // warp-uniform cursors: ensemble chunk, spill buffer (drain only)
   int next = 0, end = 0, sp_next = 0;
   bool exhausted = drain;
-  // per-lane electron: ensemble slot (>= 0) or secondary (-1)
-  bool have = false;
-  int slot = 0;
-  float3 p = make_float3(0.f, 0.f, 0.f), v = make_float3(0.f, 0.f, 0.f);
-  float s = -1.0f, t = 0.0f, energy = 0.0f;
-  int events = 0;
   uint32_t sec_id = 0;
-  PcgStream rng;
-
-  auto start_secondary = [&](float4 A, float4 B, uint32_t id) {
-    slot = -1;
-    p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
-    v = make_float3(B.x, B.y, B.z);
-    s = -1.0f;
-    t = A.w;
-    time_adj += T - t;  // electron-time this secondary adds to the interval
-    rng.init(id, interval, a.seed, a.salt + 1u);
-    energy = energy_of(v, hme);
-    events = 0;
-    have = true;
-  };
 
   for (;;) {
     __syncwarp();
     if (drain) __threadfence();
     // ---- refill lanes without an electron: the warp's ensemble chunk first,
     // then the warp's own secondaries, then (drain) the spilled ones
-    const unsigned need = __ballot_sync(0xffffffffu, !have);
+    const unsigned need = __ballot_sync(0xffffffffu, !L.have);
     if (need && !exhausted) {
       const int n_need = __popc(need);
       const int r = __popc(need & lt_mask);
       int idx = -1;
       const int take = min(n_need, end - next);
-      if (!have && r < take) idx = next + r;
+      if (!L.have && r < take) idx = next + r;
       next += take;
       if (n_need > take) {
         int base = 0;
@@ -173,184 +393,173 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a) {
           end = min(base + kChunk, n_el);
           const int r2 = r - take;
           const int take2 = min(n_need - take, end - next);
-          if (!have && r2 >= 0 && r2 < take2) idx = next + r2;
+          if (!L.have && r2 >= 0 && r2 < take2) idx = next + r2;
           next += take2;
         }
       }
-      if (idx >= 0) {
-        const float4 A = a.state[2 * idx];
-        const float4 B = a.state[2 * idx + 1];
-        if (B.w == 0.0f) {
-          slot = idx;
-          p = make_float3(A.x - shift.x, A.y - shift.y, A.z - shift.z);
-          v = make_float3(B.x, B.y, B.z);
-          s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
-          t = 0.0f;
-          rng.init((uint32_t)idx, interval, a.seed, a.salt);
-          energy = energy_of(v, hme);
-          events = 0;
-          have = true;
-        }
-      }
+      if (idx >= 0) lane_take_electron(a, iv, L, idx);
     }
-    int qn = min(s_qn[wid], kLocalQ);
+    int qn = min(sh.qn[wid], kLocalQ);
     if (exhausted) {
-      const unsigned idle = __ballot_sync(0xffffffffu, !have);
-      const int r = __popc(idle & lt_mask);
-      const int take = min(__popc(idle), qn);
-      if (((idle >> lane) & 1u) && r < take) {
-        const int e = qn - 1 - r;
-        start_secondary(s_qa[wid][e], s_qb[wid][e], 0x80000000u | ((uint32_t)(blockIdx.x * kWarps + wid) << 12) |
-                                                       ((uint32_t)(sec_id + r) & 0xFFFu));
-      }
-      sec_id += take;
-      qn -= take;
-      __syncwarp();
-      if (lane == 0) s_qn[wid] = qn;
+      qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, 0xFFFu);
       if (drain) {
-        const unsigned idle2 = __ballot_sync(0xffffffffu, !have);
+        const unsigned idle2 = __ballot_sync(0xffffffffu, !L.have);
         const int cnt = min(*(volatile int*)a.spill_count, a.spill_cap);
         const int r2 = __popc(idle2 & lt_mask);
         const int take2 = min(__popc(idle2), cnt - sp_next);
         if (((idle2 >> lane) & 1u) && r2 < take2) {
           const int k = sp_next + r2;
-          start_secondary(__ldcg(&a.spill[2 * k]), __ldcg(&a.spill[2 * k + 1]), 0xC0000000u | (uint32_t)k);
+          lane_take_secondary(a, iv, L, tl, __ldcg(&a.spill[2 * k]), __ldcg(&a.spill[2 * k + 1]),
+                              0xC0000000u | (uint32_t)k);
         }
         sp_next += max(take2, 0);
       }
     }
-    if (!__any_sync(0xffffffffu, have)) {
+    if (!__any_sync(0xffffffffu, L.have)) {
       const bool spill_left = drain && sp_next < min(*(volatile int*)a.spill_count, a.spill_cap);
       if (exhausted && qn == 0 && !spill_left) break;
       continue;
     }
-    if (!have) continue;
-
-    // ---- one event of this lane's electron: a free flight to the next
-    // collision or, when that lies beyond the synchronisation time, to the
-    // synchronisation time (BoltzmannMC.C:650-675); the flight code is the
-    // same for both so the lanes stay converged
-    if (s < 0.0f) s = -__logf(rng.oo());
-    const float tau = s * inv_nu;
-    const bool partial = t + tau > T;
-    const float dt = partial ? T - t : tau;
-    free_flight(field, phi0 + phase_rate * t, dt, p, v);
-    {
-      const float e1 = energy_of(v, hme);
-      gain_sum += e1 - energy;
-      energy = e1;
-    }
-    bool finished = partial, dead = false;
-    if (partial) {
-      s = fmaxf(s - nu * dt, 0.0f);
-    } else {
-      t += tau;
-      CollResult cr;
-      collide(a.c, tab, s_proc, s_gas, nu, v, energy, rng, cr);
-      if (cr.chosen < 0) {
-        ++null_n;
-      } else {
-        ++real_n;
-        atomicAdd(&s_count[cr.chosen], 1u);
-        if (cr.dE >= 0.0f) atomicAdd(&s_gain[cr.chosen], cr.dE);
-        else atomicAdd(&s_loss[cr.chosen], cr.dE);
-        const int ptype = s_proc[cr.chosen].type;
-        if (ptype == kIonization) {
-          const float4 A = make_float4(p.x, p.y, p.z, t);
-          const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
-          const int k = atomicAdd(&s_qn[wid], 1);
-          if (k < kLocalQ) {
-            s_qa[wid][k] = A;
-            s_qb[wid][k] = B;
-          } else {
-            const int g = append_slot(a.spill_count);
-            if (g < a.spill_cap) {
-              a.spill[2 * g] = A;
-              a.spill[2 * g + 1] = B;
-            } else {
-              atomicExch(a.error_flag, 2);  // spill buffer full: the host reports it
-            }
-          }
-        } else if (ptype == kAttachment) {
-          dead = true;
-          finished = true;
-          time_adj -= T - t;  // electron-time the attached electron no longer spends
-          if (slot >= 0) {
-            const int k = append_slot(a.att_count);
-            a.att_list[k] = slot;
-          }
-        }
-      }
-      s = -__logf(rng.oo());  // next free flight (BoltzmannMC.C:670)
-      if (++events >= (1 << 20) && !finished) {
-        atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
-        finished = true;
-      }
-    }
-    if (finished) {
-      if (slot >= 0) {
-        a.state[2 * slot] = make_float4(p.x, p.y, p.z, dead ? -1.0f : s);
-        a.state[2 * slot + 1] = make_float4(v.x, v.y, v.z, dead ? 1.0f : 0.0f);
-      } else if (!dead) {
-        const int k = append_slot(a.sec_count);
-        if (k < a.sec_cap) {
-          a.sec[2 * k] = make_float4(p.x, p.y, p.z, s);
-          a.sec[2 * k + 1] = make_float4(v.x, v.y, v.z, 0.0f);
-        } else {
-          atomicExch(a.error_flag, 2);
-        }
-      }
-      if (!dead) e_max = fmaxf(e_max, energy);
-      have = false;
-    }
+    if (!L.have) continue;
+    lane_event<MODE>(a, sh, wid, iv, L, tl);
   }
-
-  // block reductions -> global tallies
-  double g = warp_sum((double)gain_sum);
-  double ta = warp_sum((double)time_adj);
-  unsigned long long nn = warp_sum_u64((unsigned long long)null_n);
-  unsigned long long nr = warp_sum_u64((unsigned long long)real_n);
-  float em = warp_max(e_max);
-  if (lane == 0) {
-    s_red[wid] = g;
-    s_redt[wid] = ta;
-    s_redn[wid] = nn;
-    s_redr[wid] = nr;
-    if (em > 0.0f) atomic_max_energy(a.max_energy_bits, em);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double gs = 0.0, ts = 0.0;
-    unsigned long long ns = 0, rs = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      gs += s_red[w];
-      ts += s_redt[w];
-      ns += s_redn[w];
-      rs += s_redr[w];
-    }
-    if (gs != 0.0) atomicAdd(a.field_gain, gs);
-    if (ts != 0.0) atomicAdd(a.time_adjust, ts);
-    if (ns) atomicAdd(a.null_count, ns);
-    if (rs) atomicAdd(a.real_count, rs);
-  }
-  for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
-    if (s_count[q]) {
-      atomicAdd(&a.proc_count[q], (unsigned long long)s_count[q]);
-      if (s_gain[q] != 0.0f) atomicAdd(&a.proc_gain[q], (double)s_gain[q]);
-      if (s_loss[q] != 0.0f) atomicAdd(&a.proc_loss[q], (double)s_loss[q]);
-    }
-  }
+  block_flush(a, sh, tl, lane, wid);
 }
 
 // the main pass over the ensemble and the drain of left-over secondaries
 // carry different names so that profiles can tell them apart
 template <int MODE>
 __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance(AdvanceArgs a) {
-  advance_body<MODE>(a);
+  __shared__ AdvShared sh;
+  advance_body<MODE>(a, sh);
 }
 template <int MODE>
 __global__ void __launch_bounds__(32) k_advance_drain(AdvanceArgs a) {
-  advance_body<MODE>(a);
+  __shared__ AdvShared sh;
+  advance_body<MODE>(a, sh);
+}
+
+// ------------------------------------------------------------ batched advance
+// largest s < n_slots with prefix[s] <= c, for 0 <= c < prefix[n_slots]
+__device__ __forceinline__ int slot_of_chunk(const int* prefix, int n_slots, int c) {
+  int lo = 0, hi = n_slots;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= c) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// word copy of a slot's advance arguments into shared memory (all threads)
+__device__ __forceinline__ void load_slot_args(const AdvanceArgs* src, AdvanceArgs* dst) {
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int k = threadIdx.x; k < (int)(sizeof(AdvanceArgs) / sizeof(int)); k += blockDim.x) d[k] = s[k];
+}
+
+// One block-chunk [first, first + cnt) of a slot: the warps take electrons
+// from the block counter *next, then push their queued secondaries. The field
+// branch is a template parameter so each instantiation keeps only its own
+// flight code live.
+template <int MODE>
+__device__ __forceinline__ void batch_chunk(const AdvanceArgs& a, AdvShared& sh, const IntervalView& iv,
+                                            LaneTally& tl, int first, int cnt, int* next, uint32_t& sec_id,
+                                            uint32_t id_hi) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  Lane L;
+  reset_lane(L);
+  bool exhausted = false;
+  for (;;) {
+    __syncwarp();
+    const unsigned need = __ballot_sync(0xffffffffu, !L.have);
+    if (need && !exhausted) {
+      const int n_need = __popc(need);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(next, n_need);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const int take = min(n_need, cnt - base);
+      if (base + n_need >= cnt) exhausted = true;
+      const int r = __popc(need & lt_mask);
+      if (!L.have && r < take) lane_take_electron(a, iv, L, first + base + r);
+    }
+    int qn = min(sh.qn[wid], kLocalQ);
+    if (exhausted) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, 0x3FFFFu);
+    if (!__any_sync(0xffffffffu, L.have)) {
+      if (exhausted && qn == 0) break;
+      continue;
+    }
+    if (!L.have) continue;
+    lane_event<MODE>(a, sh, wid, iv, L, tl);
+  }
+}
+
+// Many conditions in one persistent grid. A block takes chunks of
+// kBatchAdvanceChunk electrons of one slot at a time from the batch counter,
+// its warps take the chunk's electrons from a block counter, and the warps'
+// queued secondaries are pushed before the block moves on, so that every
+// chunk ends with empty queues. The slot's constants and per-process tallies
+// stay in shared memory while the block's chunks belong to the same slot and
+// are flushed to that slot's tallies when it changes. One launch per field
+// branch, over the chunks of the slots with that branch.
+template <int MODE>
+__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance_batch(BatchArgs b) {
+  __shared__ AdvShared sh;
+  __shared__ AdvanceArgs s_a;
+  __shared__ IntervalView s_iv;
+  __shared__ int s_chunk, s_slot, s_next;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // secondary ids: 13 bits of warp index (< 8192 warps), 18 bits of count
+  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 18);
+  const int n_slots = b.hdr->n_slots;
+  const int c0 = b.hdr->mode_chunk[MODE], c1 = b.hdr->mode_chunk[MODE + 1];
+  int cur = -1;
+  LaneTally tl;
+  reset_tally(tl);
+  uint32_t sec_id = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int c = c0 + atomicAdd(&b.hdr->chunk_counter[MODE], 1);
+      s_chunk = c;
+      s_slot = c < c1 ? slot_of_chunk(b.adv_prefix, n_slots, c) : -1;
+      s_next = 0;
+    }
+    __syncthreads();
+    const int slot = s_slot;
+    if (slot != cur) {
+      if (cur >= 0) block_flush(s_a, sh, tl, lane, wid);
+      reset_tally(tl);
+      __syncthreads();
+      if (slot < 0) break;
+      load_slot_args(&b.slots[slot].adv, &s_a);
+      __syncthreads();
+      load_block_consts(s_a, sh);
+      if (threadIdx.x == 0) s_iv = interval_view<-1>(s_a);
+      __syncthreads();
+      cur = slot;
+    }
+    const int first = (s_chunk - b.adv_prefix[slot]) * kBatchAdvanceChunk;
+    const int cnt = min(kBatchAdvanceChunk, s_a.n - first);
+    batch_chunk<MODE>(s_a, sh, s_iv, tl, first, cnt, &s_next, sec_id, id_hi);
+    __syncthreads();  // every warp is done with the chunk before the counters are reused
+  }
+}
+
+// the drain of every slot's spilled secondaries: one warp per slot
+__global__ void __launch_bounds__(32) k_advance_drain_batch(BatchArgs b) {
+  __shared__ AdvShared sh;
+  __shared__ AdvanceArgs s_a;
+  const int slot = blockIdx.x;
+  if (slot >= b.hdr->n_slots || !(b.slots[slot].flags & kSlotIonAtt)) return;
+  load_slot_args(&b.slots[slot].adv, &s_a);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_a.queue_only = 1;
+    s_a.salt = 2;
+  }
+  __syncthreads();
+  advance_body<-1>(s_a, sh);
 }
 
 // ------------------------------------------------------------------ init
@@ -465,15 +674,16 @@ __global__ void k_prefix_max(const double* nu_tot, double* nu_max, int M) {
 // ---------------------------------------------------------------- sample
 constexpr int kSampleThreads = 256;
 
-__global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
-  __shared__ double s_m[kSampleThreads / 32][kMoments];
-  // per-thread partial sums in FP32 (a handful of electrons each), FP64 from
-  // the warp reduction on
+// Moment sums of electrons begin, begin+step, ... < end into a.moments: per
+// thread in FP32 (a handful of electrons each), FP64 from the warp reduction on.
+// Every thread of the block calls this; s_m is the block's scratch.
+__device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int end, int step,
+                                             double (*s_m)[kMoments]) {
   float m[kMoments];
 #pragma unroll
   for (int k = 0; k < kMoments; ++k) m[k] = 0.0f;
   float e_max = 0.0f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+  for (int i = begin; i < end; i += step) {
     const float4 A = a.state[2 * i];
     const float4 B = a.state[2 * i + 1];
     const float e = (B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e;
@@ -500,21 +710,28 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
   if (lane == 0 && e_max > 0.0f) atomic_max_energy(a.max_energy_bits, e_max);
   __syncthreads();
   if (threadIdx.x < kMoments) {
-    double s = 0.0;
-    for (int w = 0; w < kSampleThreads / 32; ++w) s += s_m[w][threadIdx.x];
-    atomicAdd(&a.moments[threadIdx.x], s);
+    double sum = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_m[w][threadIdx.x];
+    atomicAdd(&a.moments[threadIdx.x], sum);
   }
+}
+
+__global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
+  __shared__ double s_m[kSampleThreads / 32][kMoments];
+  sample_range(a, blockIdx.x * blockDim.x + threadIdx.x, a.n, gridDim.x * blockDim.x, s_m);
 }
 
 // ------------------------------------------------------------- histograms
 constexpr int kHistThreads = 512;
 constexpr int kMaxEedfCells = 4096;
 
-__global__ void __launch_bounds__(kHistThreads) k_hist(HistArgs a) {
-  __shared__ unsigned int s_h[kMaxEedfCells];
+// Tallies of electrons begin, begin+step, ... < end: the EEDF counts go
+// through a shared-memory histogram, EADF and EVDF straight to global memory.
+// Every thread of the block calls this; s_h is the block's scratch.
+__device__ __forceinline__ void hist_range(const HistArgs& a, int begin, int end, int step, unsigned int* s_h) {
   for (int c = threadIdx.x; c < a.n_e_cells; c += blockDim.x) s_h[c] = 0u;
   __syncthreads();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+  for (int i = begin; i < end; i += step) {
     const float4 B = a.state[2 * i + 1];
     const float v2xy = B.x * B.x + B.y * B.y;
     const float v2 = v2xy + B.z * B.z;
@@ -543,6 +760,11 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(HistArgs a) {
       if (a.eedf_periodic_row) atomicAdd(&a.eedf_periodic_row[c], (double)h);
     }
   }
+}
+
+__global__ void __launch_bounds__(kHistThreads) k_hist(HistArgs a) {
+  __shared__ unsigned int s_h[kMaxEedfCells];
+  hist_range(a, blockIdx.x * blockDim.x + threadIdx.x, a.n, gridDim.x * blockDim.x, s_h);
 }
 
 // ------------------------------------------------------- population control
@@ -580,8 +802,7 @@ __device__ __forceinline__ float energy4(float4 B, float hme) { return (B.x * B.
 //      reference's sequential uniform removal (:1379-1407) - and the surviving
 //      secondaries take the removed slots; removed energies leave the growth term.
 constexpr int kPopThreads = 1024;
-__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
-  __shared__ int s_n[4];  // alive secondaries, removed slots, surviving secondaries
+__device__ __forceinline__ void pop_body(const PopArgs& a, int* s_n) {
   const int n_sec_all = min(*a.sec_count, 1 << 30);
   const int n_att = *a.att_count;
   if (n_sec_all == 0 && n_att == 0) return;
@@ -680,6 +901,83 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
+  __shared__ int s_n[4];  // alive secondaries, removed slots, surviving secondaries
+  pop_body(a, s_n);
+}
+
+// ---------------------------------------------------------- batch helpers
+// Before the advance: each slot's interval values to its control block, the
+// per-interval scalars cleared (and the moment sums of sampling slots), the
+// advance counter reset. One warp per slot.
+__global__ void k_batch_prep(BatchArgs b) {
+  const int n = b.hdr->n_slots;
+  if (blockIdx.x == 0 && threadIdx.x < kFieldModes) b.hdr->chunk_counter[threadIdx.x] = 0;
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= n) return;
+  const BatchSlot& sl = b.slots[s];
+  DevScalars* sc = sl.sc;
+  if (lane == 0) {
+    *sl.ctl_dst = sl.ctl;
+    sc->sec_count = 0;
+    sc->att_count = 0;
+    sc->spill_count = 0;
+    sc->error_flag = 0;
+    sc->max_energy_bits = 0u;
+    sc->work_counter = 0;
+  }
+  if (sl.flags & kSlotSample) {
+    if (lane < kMoments) sc->moments[lane] = 0.0;
+    if (lane == 0) sc->sample_max_bits = 0u;
+  }
+}
+
+// distribution tallies of the slots that sample them this interval
+__global__ void __launch_bounds__(kHistThreads) k_hist_batch(BatchArgs b) {
+  __shared__ unsigned int s_h[kMaxEedfCells];
+  const int n_slots = b.hdr->n_slots, total = b.hdr->hist_chunks;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    const int slot = slot_of_chunk(b.hist_prefix, n_slots, c);
+    const HistArgs& a = b.slots[slot].hist;
+    const int first = (c - b.hist_prefix[slot]) * kBatchHistChunk;
+    hist_range(a, first + threadIdx.x, min(first + kBatchHistChunk, a.n), blockDim.x, s_h);
+    __syncthreads();
+  }
+}
+
+// ensemble moments of the sampling slots
+__global__ void __launch_bounds__(kSampleThreads) k_sample_batch(BatchArgs b) {
+  __shared__ double s_m[kSampleThreads / 32][kMoments];
+  const int n_slots = b.hdr->n_slots, total = b.hdr->smp_chunks;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    const int slot = slot_of_chunk(b.smp_prefix, n_slots, c);
+    const SampleArgs& a = b.slots[slot].smp;
+    const int first = (c - b.smp_prefix[slot]) * kBatchSampleChunk;
+    sample_range(a, first + threadIdx.x, min(first + kBatchSampleChunk, a.n), blockDim.x, s_m);
+    __syncthreads();
+  }
+}
+
+// population control: one block per slot that ionizes or attaches
+__global__ void __launch_bounds__(kPopThreads) k_pop_batch(BatchArgs b) {
+  __shared__ int s_n[4];
+  const int slot = blockIdx.x;
+  if (slot >= b.hdr->n_slots || !(b.slots[slot].flags & kSlotIonAtt)) return;
+  pop_body(b.slots[slot].pop, s_n);
+}
+
+// every slot's scalars into one contiguous array for a single read-back
+__global__ void k_batch_gather(BatchArgs b) {
+  const int n = b.hdr->n_slots;
+  constexpr int kWords = (int)(sizeof(DevScalars) / sizeof(int));
+  for (int s = blockIdx.x; s < n; s += gridDim.x) {
+    const int* src = reinterpret_cast<const int*>(b.slots[s].sc);
+    int* dst = reinterpret_cast<int*>(&b.gather[s]);
+    for (int k = threadIdx.x; k < kWords; k += blockDim.x) dst[k] = src[k];
+  }
+}
+
 // --------------------------------------------------------------- replay
 __global__ void k_replay_flight(ReplayFlightArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -775,6 +1073,34 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
 }
 
 void launch_pop_control(const PopArgs& a, cudaStream_t s) { k_pop_all<<<1, kPopThreads, 0, s>>>(a); }
+
+size_t batch_prefix_offset() { return (sizeof(BatchHeader) + 15) / 16 * 16; }
+size_t batch_slots_offset() {
+  return (batch_prefix_offset() + 3 * (kBatchMaxSlots + 1) * sizeof(int) + 255) / 256 * 256;
+}
+
+void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
+  const int slots = max(1, min(max_slots, kBatchMaxSlots));
+  k_batch_prep<<<(slots + 7) / 8, 256, 0, s>>>(b);
+  k_hist_batch<<<sm_count * 2, kHistThreads, 0, s>>>(b);
+}
+
+void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s) {
+  const int grid = sm_count * kAdvanceBlocksPerSM;
+  k_advance_batch<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(b);
+  k_advance_batch<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(b);
+  k_advance_batch<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(b);
+  k_advance_batch<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(b);
+  k_advance_batch<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(b);
+}
+
+void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
+  const int slots = max(1, min(max_slots, kBatchMaxSlots));
+  k_advance_drain_batch<<<slots, 32, 0, s>>>(b);
+  k_pop_batch<<<slots, kPopThreads, 0, s>>>(b);
+  k_sample_batch<<<sm_count * 4, kSampleThreads, 0, s>>>(b);
+  k_batch_gather<<<min(slots, 64), 64, 0, s>>>(b);
+}
 
 void launch_replay_flight(const ReplayFlightArgs& a, cudaStream_t s) {
   if (a.n > 0) k_replay_flight<<<blocks_for(a.n, 128), 128, 0, s>>>(a);

@@ -13,6 +13,22 @@ constexpr int kMaxProcesses = 512;
 constexpr int kMaxGases = 16;
 constexpr int kMoments = 22;  // sum e, r(3), v(3), r r^T (6 unique), r v^T (9)
 
+// Device scalars of one condition, read back after every interval.
+// Per-interval fields first (cleared before every interval), cumulative after.
+struct DevScalars {
+  int sec_count, att_count, spill_count, error_flag;
+  unsigned int max_energy_bits;
+  int work_counter;
+  unsigned long long null_count;
+  unsigned long long real_count;
+  double field_gain;
+  double growth;
+  double time_adjust;   // electron-time beyond N x interval: + secondaries, - attachments (s)
+  unsigned int sample_max_bits;
+  int pad2;
+  double moments[kMoments];
+};
+
 // Arguments of one advance launch: every electron of the ensemble is pushed
 // from the start of the synchronisation interval to its end, colliding on the
 // way; secondaries created on the way are queued and pushed from their
@@ -143,6 +159,63 @@ struct PopArgs {
   int* error_flag;                 // set when a bounded retry loop gives up
 };
 void launch_pop_control(const PopArgs& a, cudaStream_t s);
+
+// ------------------------------------------------------------------ batches
+// Many swarm conditions (slots) advanced by one launch sequence per interval.
+// Each slot carries the same argument blocks a single-condition launch takes;
+// the kernels split every slot's ensemble into fixed-size chunks and find the
+// slot of a chunk by bisection over exclusive prefix sums of the chunk counts.
+enum SlotFlags : int { kSlotIonAtt = 1, kSlotSample = 2, kSlotHist = 4 };
+
+struct BatchSlot {
+  AdvanceArgs adv;        // adv.ctl points at ctl_dst
+  PopArgs pop;
+  SampleArgs smp;
+  HistArgs hist;
+  IntervalCtl ctl;        // this interval's values, copied to *ctl_dst by the prep kernel
+  IntervalCtl* ctl_dst;
+  DevScalars* sc;         // the condition's scalars; the per-interval part is cleared by prep
+  int flags;              // SlotFlags
+  int pad;
+};
+
+constexpr int kFieldModes = 5;
+
+// Slots are ordered by field mode; the advance runs one launch per mode over
+// that mode's chunks [mode_chunk[m], mode_chunk[m + 1]).
+struct BatchHeader {
+  int n_slots;
+  int adv_chunks, smp_chunks, hist_chunks;  // totals (last prefix entries)
+  int mode_chunk[kFieldModes + 1];          // first advance chunk of each mode's slots
+  int chunk_counter[kFieldModes];           // advance work counters, zeroed by prep
+  int pad;
+};
+
+constexpr int kBatchMaxSlots = 1024;
+constexpr int kBatchAdvanceChunk = 4096;   // electrons per block-chunk of the advance
+constexpr int kBatchSampleChunk = 4096;    // electrons per block of the moment sums
+constexpr int kBatchHistChunk = 16384;     // electrons per block of the histograms
+
+// Staging layout (host pinned mirror and device copy are identical):
+//   BatchHeader | adv_prefix | smp_prefix | hist_prefix (kBatchMaxSlots+1 ints each, padded) | BatchSlot[...]
+struct BatchArgs {
+  BatchHeader* hdr;
+  const BatchSlot* slots;
+  const int* adv_prefix;
+  const int* smp_prefix;
+  const int* hist_prefix;
+  DevScalars* gather;       // [kBatchMaxSlots]: each slot's scalars after the interval
+};
+size_t batch_prefix_offset();   // bytes from the staging start to adv_prefix
+size_t batch_slots_offset();    // bytes from the staging start to slots[0]
+// One batched interval is three launch groups on one stream:
+//   pre:     slot control blocks and per-interval scalars, deferred histograms
+//   advance: one persistent launch per field mode
+//   post:    drain of spilled secondaries, population control, moments, gather
+void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
+void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s);
+void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
+constexpr int kBatchLaunches = 11;  // kernels per batched interval
 
 // Replay kernels for the parity tests: the production device functions
 // driven by given inputs and recorded uniforms.

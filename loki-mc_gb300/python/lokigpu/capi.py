@@ -28,7 +28,13 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
             "lgpu_get_timing",
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
-            "lgpu_replay_flights_noalloc")
+            "lgpu_replay_flights_noalloc",
+            "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
+            "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
+            "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_report_get", "lgpu_server_last_error",
+            "lgpu_server_stop")
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
 
 
 class LokiGpuError(RuntimeError):
@@ -82,6 +88,28 @@ class Timing(ctypes.Structure):
                 ("h2d_bytes", D), ("d2h_bytes", D)]
 
 
+class BatchReport(ctypes.Structure):
+    _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
+                ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
+                ("d2h_bytes", D)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("config", Config), ("procs", P_(Process)), ("n_procs", I), ("gases", P_(Gas)), ("n_gases", I),
+                ("emax_elastic", D), ("conditions", Conditions)]
+
+
+class JobStatus(ctypes.Structure):
+    _fields_ = [("state", I), ("status", I), ("submit_time", D), ("start_time", D), ("end_time", D),
+                ("footprint_bytes", D), ("result", Result)]
+
+
+class ServerReport(ctypes.Structure):
+    _fields_ = [("submitted", LL), ("completed", LL), ("failed", LL), ("running", LL), ("queued", LL),
+                ("intervals", LL), ("real_collisions", D), ("null_collisions", D), ("busy_seconds", D),
+                ("peak_footprint_bytes", D)]
+
+
 _lib = None
 
 
@@ -121,6 +149,21 @@ def load(path: str | None = None):
     lib.lgpu_replay_flights.argtypes = [ctypes.c_void_p, I] + [P_(D)] * 8
     lib.lgpu_replay_collisions.argtypes = [ctypes.c_void_p, I, P_(D), P_(D), P_(D), P_(D), I, P_(D), P_(I)]
     lib.lgpu_replay_flights_noalloc.argtypes = [I, P_(D), D, D, D, I] + [P_(D)] * 8
+    VP = ctypes.c_void_p
+    lib.lgpu_batch_create.argtypes = [I, I, P_(VP)]
+    lib.lgpu_batch_destroy.argtypes = [VP]
+    lib.lgpu_batch_last_error.argtypes = [VP, ctypes.c_char_p, ctypes.c_size_t]
+    lib.lgpu_batch_add.argtypes = [VP, VP]
+    lib.lgpu_batch_run.argtypes = [VP, P_(Result), P_(I), I, P_(BatchReport)]
+    lib.lgpu_server_start.argtypes = [I, I, D, P_(VP)]
+    lib.lgpu_server_submit.argtypes = [VP, P_(Job), P_(LL)]
+    lib.lgpu_server_poll.argtypes = [VP, LL, P_(JobStatus)]
+    lib.lgpu_server_wait.argtypes = [VP, LL, D, P_(JobStatus)]
+    lib.lgpu_server_job_rates.argtypes = [VP, LL, P_(ctypes.c_ulonglong), P_(D), I]
+    lib.lgpu_server_cancel.argtypes = [VP, LL]
+    lib.lgpu_server_report_get.argtypes = [VP, P_(ServerReport)]
+    lib.lgpu_server_last_error.argtypes = [VP, ctypes.c_char_p, ctypes.c_size_t]
+    lib.lgpu_server_stop.argtypes = [VP]
     _lib = lib
     return lib
 
@@ -153,6 +196,42 @@ def replay_flights_noalloc(device, E, freq_hz, red_mag, cyclotron, t, dt, pos, v
     if rc != LGPU_OK:
         raise LokiGpuError(rc, "lgpu_replay_flights_noalloc failed")
     return po, vo, eo, go
+
+
+def process_arrays(ps, gas_first, gas_last, gas_fraction):
+    """lgpu_process / lgpu_gas arrays of a ProcessSet-like object (see
+    synth.ProcessSet); the third value holds the raw arrays the structs point to."""
+    n = ps.n
+    arr = (Process * n)()
+    keep = []
+    for p in range(n):
+        q = arr[p]
+        q.type = int(ps.ptype[p])
+        q.is_super = int(ps.is_super[p])
+        q.is_elastic = int(ps.is_elastic[p])
+        q.sampler = int(ps.sampler[p])
+        q.sampler_p0 = float(ps.sampler_p0[p])
+        q.sampler_p1 = float(ps.sampler_p1[p])
+        q.superw = float(ps.superw[p])
+        q.emin = float(ps.emin[p])
+        q.emax = float(ps.emax[p])
+        q.rel_dens = float(ps.rel_dens[p])
+        q.mass = float(ps.mass[p])
+        q.eloss = float(ps.eloss[p])
+        q.wparam = float(ps.wparam[p])
+        e = np.ascontiguousarray(ps.raw_e[p], dtype=np.float64)
+        v = np.ascontiguousarray(ps.raw_v[p], dtype=np.float64)
+        keep += [e, v]
+        q.raw_len = len(e) if not ps.is_super[p] else 0
+        q.raw_e = dptr(e)
+        q.raw_v = dptr(v)
+    G = len(gas_first)
+    gs = (Gas * G)()
+    for g in range(G):
+        gs[g].first = int(gas_first[g])
+        gs[g].last = int(gas_last[g])
+        gs[g].fraction = float(gas_fraction[g])
+    return arr, gs, keep
 
 
 class Context:
@@ -188,38 +267,10 @@ class Context:
 
     def set_processes(self, ps, gas_first, gas_last, gas_fraction):
         """ps: a ProcessSet-like object (see synth.ProcessSet)."""
-        n = ps.n
-        arr = (Process * n)()
-        keep = []
-        for p in range(n):
-            q = arr[p]
-            q.type = int(ps.ptype[p])
-            q.is_super = int(ps.is_super[p])
-            q.is_elastic = int(ps.is_elastic[p])
-            q.sampler = int(ps.sampler[p])
-            q.sampler_p0 = float(ps.sampler_p0[p])
-            q.sampler_p1 = float(ps.sampler_p1[p])
-            q.superw = float(ps.superw[p])
-            q.emin = float(ps.emin[p])
-            q.emax = float(ps.emax[p])
-            q.rel_dens = float(ps.rel_dens[p])
-            q.mass = float(ps.mass[p])
-            q.eloss = float(ps.eloss[p])
-            q.wparam = float(ps.wparam[p])
-            e = np.ascontiguousarray(ps.raw_e[p], dtype=np.float64)
-            v = np.ascontiguousarray(ps.raw_v[p], dtype=np.float64)
-            keep += [e, v]
-            q.raw_len = len(e) if not ps.is_super[p] else 0
-            q.raw_e = dptr(e)
-            q.raw_v = dptr(v)
-        G = len(gas_first)
-        gs = (Gas * G)()
-        for g in range(G):
-            gs[g].first = int(gas_first[g])
-            gs[g].last = int(gas_last[g])
-            gs[g].fraction = float(gas_fraction[g])
-        self.check(self.lib.lgpu_set_processes(self.h, arr, n, gs, G, float(ps.energy_max_elastic)))
-        self.P = n
+        arr, gs, keep = process_arrays(ps, gas_first, gas_last, gas_fraction)
+        self._keep = keep
+        self.check(self.lib.lgpu_set_processes(self.h, arr, ps.n, gs, len(gas_first), float(ps.energy_max_elastic)))
+        self.P = ps.n
 
     def set_conditions(self, N, Tg=300.0, red_field=0.0, angle=180.0, freq_hz=0.0, red_mag=0.0):
         c = Conditions(N, Tg, red_field, angle, freq_hz, red_mag)
@@ -316,3 +367,122 @@ class Context:
         self.check(self.lib.lgpu_replay_collisions(self.h, n, dptr(nu), dptr(vel), dptr(energy), dptr(u), u.shape[1],
                                                    dptr(out), used.ctypes.data_as(P_(I))))
         return out, used
+
+
+class Batch:
+    """Owns one lgpu_batch: many contexts solved with one launch sequence per
+    synchronisation interval."""
+
+    def __init__(self, device=0, max_slots=64):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        self.ctxs = []
+        rc = self.lib.lgpu_batch_create(int(device), int(max_slots), ctypes.byref(self.h))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        self.lib.lgpu_batch_last_error(self.h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def add(self, ctx: Context):
+        rc = self.lib.lgpu_batch_add(self.h, ctx.h)
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+        self.ctxs.append(ctx)
+
+    def run(self):
+        """Solves every added context: (results, status codes, BatchReport)."""
+        n = len(self.ctxs)
+        res = (Result * max(n, 1))()
+        st = (I * max(n, 1))()
+        rep = BatchReport()
+        rc = self.lib.lgpu_batch_run(self.h, res, st, n, ctypes.byref(rep))
+        self.ctxs = []
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+        return [res[i] for i in range(n)], [st[i] for i in range(n)], rep
+
+    def close(self):
+        if self.h:
+            self.lib.lgpu_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Owns one lgpu_server: continuous batching of submitted swarm jobs."""
+
+    def __init__(self, device=0, max_slots=64, memory_budget_bytes=0.0):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        rc = self.lib.lgpu_server_start(int(device), int(max_slots), float(memory_budget_bytes), ctypes.byref(self.h))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        self.lib.lgpu_server_last_error(self.h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def submit(self, cfg: Config, ps, gas_first, gas_last, gas_fraction, N, Tg=300.0, red_field=0.0, angle=180.0,
+               freq_hz=0.0, red_mag=0.0) -> int:
+        arr, gs, keep = process_arrays(ps, gas_first, gas_last, gas_fraction)
+        job = Job(cfg, ctypes.cast(arr, P_(Process)), ps.n, ctypes.cast(gs, P_(Gas)), len(gas_first),
+                  float(ps.energy_max_elastic), Conditions(N, Tg, red_field, angle, freq_hz, red_mag))
+        jid = LL()
+        rc = self.lib.lgpu_server_submit(self.h, ctypes.byref(job), ctypes.byref(jid))
+        del keep  # the server copied every array
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_submit failed")
+        return jid.value
+
+    def poll(self, jid) -> JobStatus:
+        st = JobStatus()
+        rc = self.lib.lgpu_server_poll(self.h, int(jid), ctypes.byref(st))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_poll failed")
+        return st
+
+    def wait(self, jid, timeout_s=0.0) -> JobStatus:
+        st = JobStatus()
+        rc = self.lib.lgpu_server_wait(self.h, int(jid), float(timeout_s), ctypes.byref(st))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_wait: job not finished")
+        return st
+
+    def rates(self, jid, n):
+        counts = np.zeros(n, np.uint64)
+        rate = np.zeros(n)
+        rc = self.lib.lgpu_server_job_rates(self.h, int(jid), counts.ctypes.data_as(P_(ctypes.c_ulonglong)),
+                                            dptr(rate), int(n))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_job_rates failed")
+        return counts, rate
+
+    def cancel(self, jid):
+        rc = self.lib.lgpu_server_cancel(self.h, int(jid))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_cancel failed")
+
+    def report(self) -> ServerReport:
+        r = ServerReport()
+        self.lib.lgpu_server_report_get(self.h, ctypes.byref(r))
+        return r
+
+    def stop(self):
+        if self.h:
+            self.lib.lgpu_server_stop(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass

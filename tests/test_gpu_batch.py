@@ -1,0 +1,207 @@
+"""Batched and served solves against the same solves run alone.
+
+A batch (lgpu_batch_*) advances many contexts with one launch sequence per
+synchronisation interval; a server (lgpu_server_*) does the same for jobs that
+arrive while others run. Neither may change a result:
+
+* without ionization and attachment nothing couples the electrons and every
+  electron's random stream is fixed by (seed, electron, interval), so a
+  batched solve repeats the solve alone: the collision counts are equal and
+  the swarm parameters agree to 1e-4 relative (only the order of the
+  floating-point moment sums differs, and with it the FP32 origin shifts);
+* with ionization and attachment the secondaries draw from streams named by
+  the warp that pushes them and population control claims slots with
+  atomics, so the runs are statistically equivalent: mean energy and drift
+  agree within four combined standard errors or 1%, and the rates of processes
+  with at least 2000 counts within five combined Poisson errors doubled for
+  autocorrelation, plus 2%.
+
+The cases use the reference's parsed inputs of tests/golden/kin_{atomic,mix}.npz
+(the mixture is 80/20 two-gas with ionization and attachment) under DC, AC and
+crossed-B fields with uneven electron counts.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import golden_util as gu
+
+pytestmark = pytest.mark.gpu
+KB_EV = 1.38064852e-23 / 1.6021766208e-19
+N_GAS = 3.22e22
+F_AC = N_GAS * 1e-16 / (2 * np.pi)  # omega/N = 1e-16 m^3/s
+
+# (case, electrons, E/N (Td), angle, frequency (Hz), B/N (Hx), seed)
+ATOMIC = [("atomic", 20000, 50.0, 180.0, 0.0, 0.0, 11), ("atomic", 50000, 100.0, 180.0, 0.0, 0.0, 12),
+          ("atomic", 30000, 100.0, 90.0, 0.0, 500.0, 13), ("atomic", 30000, 150.0, 180.0, F_AC, 0.0, 14)]
+MIX = [("mix", 50000, 100.0, 180.0, 0.0, 0.0, 21), ("mix", 20000, 300.0, 180.0, 0.0, 0.0, 22),
+       ("mix", 30000, 100.0, 90.0, 0.0, 500.0, 23), ("mix", 30000, 150.0, 180.0, F_AC, 0.0, 24)]
+
+
+def _inputs(case):
+    g = gu.load(case)
+    arrays = gu.proc_arrays(g)
+    return gu.processes(arrays), arrays
+
+
+def _config(n_e, seed):
+    from lokigpu import capi
+    return capi.default_config(n_electrons=float(n_e), n_interp=2000, seed=seed, init_temp_ratio=1.0 / (KB_EV * 300.0),
+                               req_integration_points=300.0, max_coll_before_ss=100.0, n_phases=16, max_seconds=300.0)
+
+
+def _context(spec):
+    from lokigpu import capi
+    case, n_e, red_field, angle, freq, red_mag, seed = spec
+    ps, arrays = _inputs(case)
+    ctx = capi.Context(_config(n_e, seed))
+    ctx.set_processes(ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
+    ctx.set_conditions(N_GAS, 300.0, red_field, angle, freq, red_mag)
+    return ctx
+
+
+def _alone(specs):
+    out = []
+    for spec in specs:
+        ctx = _context(spec)
+        r = ctx.solve()
+        counts, rate, _, _ = ctx.process_results()
+        out.append((r, counts, rate))
+        ctx.close()
+    return out
+
+
+def _batched(specs, max_slots=64):
+    from lokigpu import capi
+    b = capi.Batch(0, max_slots)
+    ctxs = [_context(s) for s in specs]
+    for c in ctxs:
+        b.add(c)
+    res, st, rep = b.run()
+    out = []
+    for c, r, s in zip(ctxs, res, st):
+        assert s == 0, c.last_error()
+        counts, rate, _, _ = c.process_results()
+        out.append((r, counts, rate))
+        c.close()
+    b.close()
+    return out, rep
+
+
+def _drift_axis(spec):
+    # the field axis: z at 180 degrees, x at 90 degrees (BoltzmannMC.C:465-474)
+    return 2 if spec[3] == 180.0 else 0
+
+
+def _statistically_equal(spec, a, b):
+    ra, ca, qa = a
+    rb, cb, qb = b
+    fails = []
+    k = _drift_axis(spec)
+    for label, va, ea, vb, eb in [("mean energy", ra.mean_energy, ra.mean_energy_err, rb.mean_energy, rb.mean_energy_err),
+                                  ("flux v", ra.flux_v[k], ra.flux_v_err[k], rb.flux_v[k], rb.flux_v_err[k])]:
+        tol = max(4.0 * np.hypot(ea, eb), 0.01 * abs(va))
+        if abs(va - vb) > tol:
+            fails.append(f"{spec}: {label} {va:.6g} +- {ea:.3g} vs {vb:.6g} +- {eb:.3g}")
+    for p in range(len(qa)):
+        if ca[p] < 2000 or cb[p] < 2000:
+            continue
+        rel = 2.0 * 5.0 * np.sqrt(1.0 / ca[p] + 1.0 / cb[p]) + 0.02
+        if abs(qb[p] / qa[p] - 1.0) > rel:
+            fails.append(f"{spec}: rate[{p}] {qa[p]:.6g} vs {qb[p]:.6g} (counts {ca[p]}, {cb[p]})")
+    return fails
+
+
+@pytest.fixture(scope="module")
+def mix_alone():
+    return _alone(MIX)
+
+
+def test_batch_repeats_alone_without_ionization():
+    alone = _alone(ATOMIC)
+    batched, rep = _batched(ATOMIC)
+    assert rep.intervals > 0 and rep.kernel_launches > 0 and rep.electron_steps > 0
+    for spec, (ra, ca, _), (rb, cb, _) in zip(ATOMIC, alone, batched):
+        assert ra.capped == 0 and rb.capped == 0
+        assert rb.sync_steps == ra.sync_steps, spec
+        assert rb.real_collisions == ra.real_collisions, spec
+        assert rb.null_collisions == ra.null_collisions, spec
+        assert np.array_equal(ca, cb), spec
+        assert abs(rb.mean_energy / ra.mean_energy - 1.0) < 1e-4, spec
+        k = _drift_axis(spec)
+        assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < 1e-4, spec
+        assert abs(rb.bulk_v[k] / ra.bulk_v[k] - 1.0) < 1e-3, spec
+
+
+def test_batch_matches_alone_with_ionization_and_attachment(mix_alone):
+    batched, rep = _batched(MIX)
+    fails = []
+    for spec, a, b in zip(MIX, mix_alone, batched):
+        assert b[0].capped == 0 and b[0].integration_points >= 300
+        fails += _statistically_equal(spec, a, b)
+    assert not fails, "\n".join(fails)
+
+
+def test_batch_with_fewer_slots_than_contexts(mix_alone):
+    # two slots for four contexts: the last two start as the first ones finish
+    batched, rep = _batched(MIX, max_slots=2)
+    fails = []
+    for spec, a, b in zip(MIX, mix_alone, batched):
+        fails += _statistically_equal(spec, a, b)
+    assert not fails, "\n".join(fails)
+
+
+def test_server_jobs_arriving_while_others_run(mix_alone):
+    from lokigpu import capi
+    srv = capi.Server(0, 16)
+    ids = []
+    for spec in MIX:
+        case, n_e, red_field, angle, freq, red_mag, seed = spec
+        ps, arrays = _inputs(case)
+        ids.append(srv.submit(_config(n_e, seed), ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"],
+                              N_GAS, 300.0, red_field, angle, freq, red_mag))
+        time.sleep(0.02)  # later jobs join a batch already on the device
+    fails = []
+    starts, ends = [], []
+    for spec, jid, a in zip(MIX, ids, mix_alone):
+        st = srv.wait(jid, 600.0)
+        assert st.state == capi.JOB_DONE, (spec, st.status, srv.last_error())
+        assert st.submit_time <= st.start_time <= st.end_time
+        starts.append(st.start_time)
+        ends.append(st.end_time)
+        ps, _ = _inputs(spec[0])
+        counts, rate = srv.rates(jid, ps.n)
+        fails += _statistically_equal(spec, a, (st.result, counts, rate))
+    rep = srv.report()
+    srv.stop()
+    assert not fails, "\n".join(fails)
+    assert rep.completed == len(MIX) and rep.failed == 0 and rep.intervals > 0
+    # the work overlapped: two jobs were on the device at the same time
+    assert any(starts[i] < ends[j] and starts[j] < ends[i] for i in range(len(ids)) for j in range(i))
+
+
+def test_server_admits_by_memory_footprint():
+    from lokigpu import capi
+    spec = ("atomic", 10000, 100.0, 180.0, 0.0, 0.0, 5)
+    ps, arrays = _inputs("atomic")
+    cfg = _config(10000, 5)
+    cfg.req_integration_points = 100.0
+    probe = capi.Server(0, 4)
+    jid = probe.submit(cfg, ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"], N_GAS, 300.0, 100.0)
+    fp = probe.wait(jid, 300.0).footprint_bytes
+    probe.stop()
+    assert fp > 10000 * 64
+    srv = capi.Server(0, 4, memory_budget_bytes=1.5 * fp)  # one job at a time
+    ids = [srv.submit(cfg, ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"], N_GAS, 300.0, 100.0)
+           for _ in range(3)]
+    big = capi.default_config(**{k: getattr(cfg, k) for k, _ in capi.Config._fields_})
+    big.n_electrons = 1e6  # larger than the whole budget
+    big_id = srv.submit(big, ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"], N_GAS, 300.0, 100.0)
+    sts = [srv.wait(j, 300.0) for j in ids]
+    st_big = srv.wait(big_id, 300.0)
+    srv.stop()
+    assert all(s.state == capi.JOB_DONE for s in sts)
+    for s0, s1 in zip(sts, sts[1:]):
+        assert s1.start_time >= s0.end_time - 1e-6  # never two at once
+    assert st_big.state == capi.JOB_FAILED and st_big.status == 2  # LGPU_ERR_OOM
