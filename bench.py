@@ -1,22 +1,36 @@
 #!/usr/bin/env python3
 """Benchmark of the electron Monte Carlo hot path on GB300.
 
-Workload: the synthetic N2-like molecular gas (elastic with screened-Coulomb
-anisotropy, 1 rotational and 8 vibrational <-> levels, 20 electronic levels,
-ionization at 15.6 eV with equal energy sharing; seeded smooth cross sections
-on 200-point log grids, Boltzmann populations at 300 K), DC E/N = 200 Td,
-N = 3.22e22 m^-3, 1e6 electrons, FP32 push with FP64 tallies.
+Default workload (--workload sweep): the 64-point E/N sweep. E/N log-spaced
+1..1000 Td over the synthetic N2-like gas mixed 80/20 with the synthetic
+O2-like gas (65 processes: ionization in both gases, dissociative attachment
+at 4.4 eV; 200-point log grids over 1e-3..1e4 eV), N = 3.22e22 m^-3, cold gas, uneven electron counts per condition
+(seeded log-uniform 1e4..2e6, 1.98e7 in all), FP32 push with FP64 tallies.
+Three forms of the same work are measured:
 
-A step is one synchronisation interval of the plain method over the whole
-ensemble: every electron flies and collides up to the synchronisation time,
-population control runs, and the ensemble is sampled (moments). The metric is
-real collisions per second. The ensemble is relaxed for a number of untimed
-intervals first, then W warm-up steps, then K timed steps; an L2 flush (a
-256 MiB write) precedes every timed step and is outside the timed region.
+* batched: all 64 conditions in one lgpu_batch - one launch sequence (CUDA
+  graph) per synchronisation interval advances every condition;
+* plain: one condition per launch sequence (lgpu_solve / lgpu_advance), the
+  drop-in path, one condition after the other;
+* served: the 64 conditions submitted to lgpu_server with Poisson arrivals,
+  admitted by device footprint as they arrive (continuous batching).
+
+`value` is real collisions per second of the batched form over K timed
+intervals of all 64 conditions (after R relaxation intervals and W warm-up
+intervals; each timed interval is bracketed by CUDA events on the batch's
+stream and preceded by a 256 MiB L2 flush outside the timed region). The plain
+form is timed the same way per condition (plain.value). `e2e` is the whole
+sweep solved to convergence (mean-energy standard error below 0.5%) through
+the C ABI from host arrays: contexts created, processes uploaded, solved,
+results and rate coefficients read back; the same for the plain form
+(plain.e2e) and the served form with its p50/p99 request latency.
+
+--workload n2_200td keeps the single-condition line: the synthetic N2-like gas
+at DC 200 Td with 1e6 electrons, one plain interval per step.
 
 --impl reference times the CPU implementation of the same path on the host
-cores: the reference built from its own sources when present (oracle/_ref),
-else the C restatement (oracle/), on a bounded sample of the same workload.
+cores (the C restatement of the reference's algorithm, oracle/) on a bounded
+sample of the same workload.
 """
 from __future__ import annotations
 
@@ -35,14 +49,23 @@ METRIC = "real collisions/s, batched+served vs plain, 1 GB300; sweep p50/p99 at 
 UNIT = "collisions/s"
 N_GAS = 3.22e22
 T_GAS = 300.0
+KT_INIT = 1.0 / (8.617333262e-5 * T_GAS)  # start Maxwellian at kT = 1 eV
+STATE_BYTES_PER_ELECTRON_STEP = 64  # 32 B state read + 32 B written per electron per interval
+
+# single-condition workload
 E_N = 200.0
 N_ELECTRONS = 1_000_000
-STATE_BYTES_PER_ELECTRON_STEP = 64  # 32 B state read + 32 B written per electron per interval
 # DRAM bytes per electron and interval of k_advance, from one ncu capture of the
 # same kernel on 4e6 electrons (profiles/k_advance_n2_dc200.md): 130.5 MB read +
 # 73.6 MB written; traffic grows in proportion to the electrons advanced
 DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
-WORKLOAD = "n2_like_dc200Td_1e6e"
+
+# sweep workload
+SWEEP_POINTS = 64
+SWEEP_SEED = 2024
+SWEEP_NE_RANGE = (1e4, 2e6)
+SWEEP_ERR = 0.005            # mean-energy relative standard error at convergence
+SWEEP_SS_CAP = 50.0          # maxCollisionsBeforeSteadyState (x nElectrons)
 
 
 def measured_peaks():
@@ -103,22 +126,57 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def workload_processes():
+# ------------------------------------------------------------------ workloads
+def n2_processes():
     from lokigpu import synth
 
     return synth.flatten([synth.n2_like_gas()])
 
 
+def sweep_processes():
+    from lokigpu import synth
+
+    # cross sections to 1e4 eV: at 1000 Td the electrons pass 1 keV, where tables
+    # ending at 1e3 eV stop the solve (BoltzmannMC.C:1426-1430)
+    return synth.flatten([synth.n2_like_gas(fraction=0.8, e_max=1e4), synth.o2_like_gas(fraction=0.2, e_max=1e4)])
+
+
+def sweep_conditions():
+    """(E/N in Td, electrons) of the 64 sweep points."""
+    import numpy as np
+
+    en = np.logspace(0.0, 3.0, SWEEP_POINTS)
+    rng = np.random.default_rng(SWEEP_SEED)
+    lo, hi = np.log10(SWEEP_NE_RANGE[0]), np.log10(SWEEP_NE_RANGE[1])
+    ne = np.round(10.0 ** rng.uniform(lo, hi, SWEEP_POINTS)).astype(int)
+    return [(float(e), int(n)) for e, n in zip(en, ne)]
+
+
+def sweep_config(capi, device, n_e, seed, converge):
+    """Numerics of a sweep condition: converged means the reference's stop
+    criteria with relError meanEnergy 0.5% (BoltzmannMC.C:1743-1767), else a
+    context that never stops by itself (timed intervals)."""
+    kw = dict(device=device, seed=seed, n_electrons=float(n_e), n_interp=10000, init_temp_ratio=KT_INIT)
+    if converge:
+        kw.update(errors_checked=1, req_err_mean_energy=SWEEP_ERR, req_integration_points=200.0,
+                  max_coll_before_ss=SWEEP_SS_CAP, max_seconds=300.0)
+    else:
+        kw.update(req_integration_points=1e15)
+    return capi.default_config(**kw)
+
+
 # --------------------------------------------------------------------- CPU arm
-def cpu_sample(seconds: float, threads: int, n_electrons: int = 100_000, warm_intervals: int = 300):
+def cpu_sample(seconds: float, threads: int, workload: str, n_electrons: int = 100_000, warm_intervals: int = 300):
     """Times the CPU restatement of the reference's path (oracle/) on the host
-    cores: the same gas and field, n_electrons electrons, rate measured after
-    warm_intervals intervals so it is taken near steady state like the GPU's."""
+    cores on a bounded sample of the workload: the sweep's mixture at 100 Td
+    (the sweep's midpoint decade), or the N2-like gas at 200 Td; n_electrons
+    electrons, rate measured after warm_intervals intervals."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
 
-    ps = workload_processes()
+    ps = sweep_processes() if workload == "sweep" else n2_processes()
+    en = 100.0 if workload == "sweep" else E_N
     off = np.concatenate([[0], np.cumsum([len(e) for e in ps.raw_e])]).astype(np.int32)
     arrays = dict(ptype=ps.ptype, is_super=ps.is_super, sampler=ps.sampler, sampler_p0=ps.sampler_p0,
                   sampler_p1=ps.sampler_p1, superw=ps.superw, emin=ps.emin, emax=ps.emax, rel_dens=ps.rel_dens,
@@ -127,18 +185,19 @@ def cpu_sample(seconds: float, threads: int, n_electrons: int = 100_000, warm_in
                   raw_v=np.concatenate(ps.raw_v), gas_first=ps.gas_first, gas_last=ps.gas_last,
                   gas_frac=ps.gas_fraction, energy_max_elastic=ps.energy_max_elastic)
     pr = O.OracleProcs(arrays, 10000)
-    f = O.make_fields(N_GAS, T_GAS, E=(0.0, 0.0, -E_N * 1e-21 * N_GAS))
+    f = O.make_fields(N_GAS, T_GAS, E=(0.0, 0.0, -en * 1e-21 * N_GAS))
     cfg = O.default_run_config(n_electrons, n_threads=threads, seed=3, max_seconds=seconds,
                                mark_sync_step=warm_intervals, req_integration_points=1e12)
     st, res, _ = O.run(pr, f, cfg)
+    what = "the sweep's mixture at 100 Td" if workload == "sweep" else "the N2-like gas at 200 Td"
     if res.mark_elapsed > 0 and res.elapsed > res.mark_elapsed:
         real = res.real_collisions - res.mark_real_collisions
         dt = res.elapsed - res.mark_elapsed
-        sample = (f"{n_electrons} electrons, same gas and field, intervals {warm_intervals + 1}..{res.sync_steps} "
+        sample = (f"{n_electrons} electrons, {what}, intervals {warm_intervals + 1}..{res.sync_steps} "
                   f"({dt:.1f} s of a {seconds:.0f} s run, C restatement of the reference path)")
     else:
         real, dt = res.real_collisions, res.elapsed
-        sample = f"{n_electrons} electrons, same gas and field, first {res.sync_steps} intervals ({dt:.1f} s)"
+        sample = f"{n_electrons} electrons, {what}, first {res.sync_steps} intervals ({dt:.1f} s)"
     return real / dt, sample, threads
 
 
@@ -152,24 +211,27 @@ def run_reference_arm(args):
     sample = ""
     per_step = max(3.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     for i in range(args.warmup + args.steps):
-        r, sample, _ = cpu_sample(per_step, threads, warm_intervals=100)
+        r, sample, _ = cpu_sample(per_step, threads, args.workload, warm_intervals=100)
         if i >= args.warmup:
             rates.append(r)
     v = sum(rates) / len(rates)
+    workload = "sweep64_n2o2_1-1000Td" if args.workload == "sweep" else "n2_like_dc200Td_1e6e"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (time.time() - t0) / (args.steps + args.warmup),
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * (time.time() - t0) / (args.steps + args.warmup),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "electrons": 100_000, "impl_detail": "C restatement of the reference path (oracle/), OpenMP"},
+            "config": {"workload": workload, "electrons": 100_000,
+                       "impl_detail": "C restatement of the reference path (oracle/), OpenMP"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-# --------------------------------------------------------------------- GPU arm
+# --------------------------------------------------------------------- GPU arms
 def aggregate_ranks(total_ms, real, null, device):
-    """Replicas only: every rank advances its own ensemble; the job time is the
-    slowest rank's, the collisions are summed over ranks."""
+    """Replicas only: every rank advances its own ensembles; the job time is
+    the slowest rank's, the collisions are summed over ranks."""
     import torch
     import torch.distributed as dist
 
@@ -180,13 +242,9 @@ def aggregate_ranks(total_ms, real, null, device):
     return float(t[0]), float(c[0]), float(c[1])
 
 
-def run_gpu_arm(args):
+def _init_ranks():
     import torch
 
-    from lokigpu import build as gbuild
-    from lokigpu import capi
-
-    rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
@@ -194,13 +252,311 @@ def run_gpu_arm(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
+    return int(os.environ.get("RANK", "0")), world, local
+
+
+def _percentile(xs, q):
+    import numpy as np
+
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
+
+
+def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
+    """value: K timed batched intervals of all conditions, after relaxation."""
+    import torch
+
+    b = capi.Batch(local, len(conds))
+    ctxs = []
+    for i, (en, ne) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False))
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, en)
+        b.add(c)
+        ctxs.append(c)
+    b.start()
+    b.step(args.relax)
+    for _ in range(args.warmup):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        b.step(1)
+    stream = torch.cuda.ExternalStream(b.stream(), device=local)
+    total_ms = real = null = adv_ms = steps = 0.0
+    launches = intervals = 0
+    h2d = d2h = host_ms = secondaries = spilled = 0.0
+    for _ in range(args.steps):
+        flush.add_(1.0)                    # L2 flush (256 MiB written), outside the timed region
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        running, rep = b.step(1)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        real += rep.real_collisions
+        null += rep.null_collisions
+        adv_ms += rep.advance_ms
+        steps += rep.electron_steps
+        launches += rep.kernel_launches
+        intervals += rep.intervals
+        h2d += rep.h2d_bytes
+        d2h += rep.d2h_bytes
+        host_ms += rep.host_ms
+        secondaries += rep.secondaries
+        spilled += rep.spilled
+        assert running == len(conds)
+    del b
+    for c in ctxs:
+        c.close()
+    return dict(total_ms=total_ms, real=real, null=null, adv_ms=adv_ms, electron_steps=steps, launches=launches,
+                intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled)
+
+
+def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
+    """plain.value: the same number of timed intervals per condition, one
+    condition per launch sequence."""
+    import torch
+
+    total_ms = real = null = 0.0
+    for i, (en, ne) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False))
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, en)
+        c.init_ensemble()
+        c.advance(args.relax)
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        c.advance(1)
+        stream = torch.cuda.ExternalStream(c.stream(), device=local)
+        r0 = c.advance(0)
+        for _ in range(args.plain_steps):
+            flush.add_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            c.advance(1)
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+        r1 = c.advance(0)
+        real += r1.real_collisions - r0.real_collisions
+        null += r1.null_collisions - r0.null_collisions
+        c.close()
+    return dict(total_ms=total_ms, real=real, null=null)
+
+
+def _sweep_e2e_batched(capi, ps, conds, local, rank):
+    import torch
+
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    b = capi.Batch(local, len(conds))
+    ctxs = []
+    for i, (en, ne) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True))
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, en)
+        b.add(c)
+        ctxs.append(c)
+    res, st, rep = b.run()
+    rates = [c.process_results()[:2] for c in ctxs]
+    w1 = time.perf_counter()
+    for c in ctxs:
+        c.close()
+    del b
+    return dict(wall=w1 - w0, results=res, status=st, rates=rates, report=rep)
+
+
+def _sweep_e2e_plain(capi, ps, conds, local, rank):
+    import torch
+
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    res, rates, h2d, d2h, steps = [], [], 0.0, 0.0, 0
+    for i, (en, ne) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True))
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, en)
+        r = c.solve()
+        rates.append(c.process_results()[:2])
+        tm = c.timing()
+        h2d += tm.h2d_bytes
+        d2h += tm.d2h_bytes
+        steps += r.sync_steps
+        res.append(r)
+        c.close()
+    w1 = time.perf_counter()
+    return dict(wall=w1 - w0, results=res, rates=rates, h2d=h2d, d2h=d2h, steps=steps)
+
+
+def _sweep_served(capi, ps, conds, local, rank, args):
+    import numpy as np
+
+    srv = capi.Server(local, len(conds))
+    rng = np.random.default_rng(SWEEP_SEED + 1)
+    order = rng.permutation(len(conds))
+    gaps = rng.exponential(args.arrival_ms * 1e-3, len(conds))
+    ids = {}
+    w0 = time.perf_counter()
+    for k, i in enumerate(order):
+        time.sleep(float(gaps[k]))
+        en, ne = conds[i]
+        ids[i] = srv.submit(sweep_config(capi, local, ne, 7000 + 100 * rank + int(i), converge=True), ps,
+                            ps.gas_first, ps.gas_last, ps.gas_fraction, N_GAS, T_GAS, en)
+    sts = {i: srv.wait(j, 600.0) for i, j in ids.items()}
+    w1 = time.perf_counter()
+    rep = srv.report()
+    srv.stop()
+    lat = [s.end_time - s.submit_time for s in sts.values()]
+    real = sum(s.result.real_collisions for s in sts.values())
+    span = max(s.end_time for s in sts.values()) - min(s.submit_time for s in sts.values())
+    errors = [f"E/N {conds[i][0]:.4g} Td, {conds[i][1]} electrons: status {s.status}: {s.error.decode(errors='replace')}"
+              for i, s in sts.items() if s.state != capi.JOB_DONE]
+    return dict(wall=w1 - w0, latencies=lat, real=real, span=span, errors=errors,
+                failed=sum(s.state != capi.JOB_DONE for s in sts.values()),
+                results=[sts[i].result for i in range(len(conds))], intervals=rep.intervals, busy=rep.busy_seconds,
+                peak_footprint=rep.peak_footprint_bytes)
+
+
+def _accuracy(conds, batched, plain):
+    """Convergence and agreement of the batched solves with the plain ones."""
+    import numpy as np
+
+    rel_err, zs, rate_dev = [], [], []
+    for i in range(len(conds)):
+        rb, rp = batched["results"][i], plain["results"][i]
+        rel_err.append(rb.mean_energy_err / rb.mean_energy)
+        zs.append(abs(rb.mean_energy - rp.mean_energy) / max(np.hypot(rb.mean_energy_err, rp.mean_energy_err), 1e-300))
+        cb, qb = batched["rates"][i]
+        cp, qp = plain["rates"][i]
+        for p in range(len(qb)):
+            if cb[p] >= 2000 and cp[p] >= 2000 and qp[p] > 0:
+                sig = np.sqrt(1.0 / cb[p] + 1.0 / cp[p])
+                rate_dev.append(abs(qb[p] / qp[p] - 1.0) / sig)
+    return {"max_mean_energy_rel_err": float(max(rel_err)),
+            "mean_energy_batched_vs_plain_max_sigmas": float(max(zs)),
+            "mean_energy_batched_vs_plain_median_sigmas": float(np.median(zs)),
+            "rates_batched_vs_plain_median_poisson_sigmas": float(np.median(rate_dev)) if rate_dev else None,
+            "rates_compared": len(rate_dev),
+            "criterion": f"each condition stops when its mean-energy standard error < {SWEEP_ERR:.1%} "
+                         "(50-block batch means, BoltzmannMC.C:1743-1767)"}
+
+
+def run_gpu_sweep(args):
+    import torch
+
+    from lokigpu import build as gbuild
+    from lokigpu import capi
+
+    rank, world, local = _init_ranks()
     if not os.path.exists(capi.library_path()):
         gbuild.build()
-    ps = workload_processes()
+    ps = sweep_processes()
+    conds = sweep_conditions()
+    clocks = ClockSampler(local)
+    clocks.start()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    tb = _sweep_timed_batched(capi, ps, conds, local, rank, args, flush)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    total_ms, real, null = tb["total_ms"], tb["real"], tb["null"]
+    if world > 1:
+        total_ms, real, null = aggregate_ranks(total_ms, real, null, torch.device("cuda", local))
+    value = real / (total_ms * 1e-3)
+    tp = _sweep_timed_plain(capi, ps, conds, local, rank, args, flush) if not args.no_plain else None
+    e2e_b = _sweep_e2e_batched(capi, ps, conds, local, rank) if not args.no_e2e else None
+    e2e_p = _sweep_e2e_plain(capi, ps, conds, local, rank) if not (args.no_e2e or args.no_plain) else None
+    srv = _sweep_served(capi, ps, conds, local, rank, args) if not args.no_served else None
+
+    peak, peak_kind = measured_peaks()
+    achieved = STATE_BYTES_PER_ELECTRON_STEP * tb["electron_steps"] / (tb["adv_ms"] * 1e-3) / 1e9 if tb["adv_ms"] > 0 else 0.0
+    electrons = sum(n for _, n in conds)
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, sample, cores = cpu_sample(args.cpu_seconds, os.cpu_count() or 1, "sweep")
+            cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        e2e = None
+        if e2e_b:
+            rep = e2e_b["report"]
+            real_b = sum(r.real_collisions for r in e2e_b["results"])
+            e2e = {"value": real_b / e2e_b["wall"], "unit": UNIT,
+                   "h2d_bytes_per_step": rep.h2d_bytes / max(rep.intervals, 1),
+                   "d2h_bytes_per_step": rep.d2h_bytes / max(rep.intervals, 1),
+                   "scope": f"64 contexts created, processes uploaded, lgpu_batch_run to convergence, rates read back; "
+                            f"{rep.intervals} batched intervals, {e2e_b['wall']:.2f} s wall",
+                   "failed": int(sum(1 for s in e2e_b["status"] if s != 0)),
+                   "max_energy_eV": max(r.max_eedf_energy for r in e2e_b["results"]) / 1.2}
+        plain = None
+        if tp:
+            plain = {"value": tp["real"] / (tp["total_ms"] * 1e-3), "unit": UNIT,
+                     "timed_intervals_per_condition": args.plain_steps,
+                     "ms_per_interval_avg": tp["total_ms"] / (args.plain_steps * len(conds))}
+            if e2e_p:
+                real_p = sum(r.real_collisions for r in e2e_p["results"])
+                plain["e2e"] = {"value": real_p / e2e_p["wall"], "unit": UNIT, "wall_s": e2e_p["wall"],
+                                "h2d_bytes_per_step": e2e_p["h2d"] / max(e2e_p["steps"], 1),
+                                "d2h_bytes_per_step": e2e_p["d2h"] / max(e2e_p["steps"], 1)}
+        served = None
+        if srv:
+            served = {"p50_s": _percentile(srv["latencies"], 50), "p99_s": _percentile(srv["latencies"], 99),
+                      "value": srv["real"] / srv["span"], "unit": UNIT, "jobs": len(conds), "failed": srv["failed"],
+                      "arrivals": f"Poisson, mean gap {args.arrival_ms} ms, seeded order",
+                      "latency": "submit to results on the host (lgpu_server_wait)", "span_s": srv["span"],
+                      "peak_footprint_gb": srv["peak_footprint"] / 1e9, "errors": srv["errors"]}
+        ratio = {}
+        if plain:
+            ratio["device_timed"] = value / plain["value"]
+            if e2e and "e2e" in plain:
+                ratio["e2e"] = e2e["value"] / plain["e2e"]["value"]
+                if served:
+                    ratio["served_over_plain_e2e"] = served["value"] / plain["e2e"]["value"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "sweep64_n2o2_1-1000Td", "conditions": len(conds), "electrons_total": electrons,
+                       "electrons_range": list(SWEEP_NE_RANGE), "E/N_Td": [1.0, 1000.0], "gas_density": N_GAS,
+                       "processes": int(ps.n), "mixture": "N2-like 0.8 + O2-like 0.2 (synthetic, seeded)",
+                       "method": "batched: one launch sequence per interval for all 64 conditions",
+                       "relax_intervals": args.relax, "l2": "256 MiB flush before every timed step",
+                       "null_collisions_per_s": null / (total_ms * 1e-3),
+                       "host_ms_per_step": tb["host_ms"] / args.steps,
+                       "secondaries_per_step": tb["secondaries"] / args.steps,
+                       "spilled_per_step": tb["spilled"] / args.steps},
+            "plain": plain, "batched_over_plain": ratio or None, "served": served,
+            "accuracy": _accuracy(conds, e2e_b, e2e_p) if (e2e_b and e2e_p) else None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "traffic_source": "no ncu capture of the batched advance yet",
+                         "kernel": "k_advance_batch", "peak_source": peak_kind,
+                         "algorithmic_bytes": f"{STATE_BYTES_PER_ELECTRON_STEP} B per electron-interval",
+                         "kernel_ms_per_interval": tb["adv_ms"] / max(tb["intervals"], 1)},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tb["launches"]), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_gpu_n2(args):
+    import torch
+
+    from lokigpu import build as gbuild
+    from lokigpu import capi
+
+    rank, world, local = _init_ranks()
+    if not os.path.exists(capi.library_path()):
+        gbuild.build()
+    ps = n2_processes()
 
     def make_ctx(seed):
         cfg = capi.default_config(device=local, seed=seed, n_electrons=float(args.electrons), n_interp=10000,
-                                  init_temp_ratio=1.0 / (8.617333262e-5 * T_GAS))  # start Maxwellian at kT = 1 eV
+                                  init_temp_ratio=KT_INIT)
         ctx = capi.Context(cfg)
         ctx.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
         ctx.set_conditions(N_GAS, T_GAS, E_N)
@@ -260,7 +616,7 @@ def run_gpu_arm(args):
         torch.cuda.synchronize()
         w0 = time.perf_counter()
         cfg = capi.default_config(device=local, seed=77 + rank, n_electrons=float(args.electrons), n_interp=10000,
-                                  init_temp_ratio=1.0 / (8.617333262e-5 * T_GAS), req_integration_points=200,
+                                  init_temp_ratio=KT_INIT, req_integration_points=200,
                                   max_coll_before_ss=20.0, max_seconds=120.0)
         c2 = capi.Context(cfg)
         c2.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
@@ -277,18 +633,18 @@ def run_gpu_arm(args):
                         f"{res.integration_points} integration points, {w1 - w0:.2f} s wall"}
         c2.close()
 
-    line = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample, cores = cpu_sample(args.cpu_seconds, os.cpu_count() or 1)
+            v, sample, cores = cpu_sample(args.cpu_seconds, os.cpu_count() or 1, "n2_200td")
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "electrons": args.electrons, "E/N_Td": E_N, "gas_density": N_GAS,
-                       "processes": int(ps.n), "method": "plain (one synchronisation interval per step)",
+            "config": {"workload": "n2_like_dc200Td_1e6e", "electrons": args.electrons, "E/N_Td": E_N,
+                       "gas_density": N_GAS, "processes": int(ps.n),
+                       "method": "plain (one synchronisation interval per step)",
                        "relax_intervals": args.relax, "l2": "256 MiB flush before every timed step",
                        "null_collisions_per_s": null / (total_ms * 1e-3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -310,20 +666,29 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--electrons", type=int, default=N_ELECTRONS)
-    ap.add_argument("--relax", type=int, default=400)
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "n2_200td"])
+    ap.add_argument("--electrons", type=int, default=N_ELECTRONS, help="n2_200td only")
+    ap.add_argument("--relax", type=int, default=None)
+    ap.add_argument("--plain-steps", type=int, default=20, help="sweep: timed plain intervals per condition")
+    ap.add_argument("--arrival-ms", type=float, default=20.0, help="sweep: mean gap of the served arrivals")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = 200 if args.workload == "sweep" else 2000
+    if args.relax is None:
+        args.relax = 200 if args.workload == "sweep" else 400
     if args.impl == "reference":
         return run_reference_arm(args)
-    return run_gpu_arm(args)
+    return run_gpu_sweep(args) if args.workload == "sweep" else run_gpu_n2(args)
 
 
 if __name__ == "__main__":

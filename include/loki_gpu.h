@@ -278,6 +278,10 @@ typedef struct lgpu_batch_report {
   double advance_ms;            /* device time of the advance launches */
   double electron_steps;        /* electrons x intervals advanced */
   double h2d_bytes, d2h_bytes;  /* host<->device copies of the batched intervals */
+  double host_ms;               /* host time of the intervals outside the wait for the device */
+  double secondaries;           /* ionization secondaries created */
+  double spilled;               /* of those, the ones a warp queue could not hold */
+  double attached;              /* electrons removed by attachment */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);
@@ -290,6 +294,16 @@ int lgpu_batch_add(lgpu_batch* batch, lgpu_ctx* ctx);
  * afterwards. Returns LGPU_OK when the batch itself ran, whatever the
  * contexts' own status. */
 int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, lgpu_batch_report* report);
+/* Interval-level control (benchmarks, callers with their own loop):
+ * lgpu_batch_start starts the queued contexts that fit the slots (their
+ * lgpu_init_ensemble), lgpu_batch_step advances every running context by n
+ * intervals (a context whose stop criteria hold finishes and leaves its slot
+ * to a waiting one; *running counts those still running), and a later
+ * lgpu_batch_run completes what is left. report counts only this call. */
+int lgpu_batch_start(lgpu_batch* batch);
+int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* report);
+/* The cudaStream_t all of the batch's work runs on. */
+void* lgpu_batch_stream(lgpu_batch* batch);
 
 /* ---- serving: continuous batching of swarm jobs ----
  *
@@ -328,6 +342,7 @@ typedef struct lgpu_job_status {
   double end_time;                /* results available */
   double footprint_bytes;         /* device memory the job held */
   lgpu_result result;
+  char error[256];                /* message of a failed job */
 } lgpu_job_status;
 
 typedef struct lgpu_server_report {

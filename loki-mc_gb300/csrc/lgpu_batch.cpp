@@ -38,12 +38,53 @@ int lgpu_batch_add(lgpu_batch* batch, lgpu_ctx* ctx) {
   return batch->b->add(ctx->e);
 }
 
+void* lgpu_batch_stream(lgpu_batch* batch) { return (batch && batch->b) ? (void*)batch->b->stream_ : nullptr; }
+
+int lgpu_batch_start(lgpu_batch* batch) {
+  if (!batch || !batch->b) return LGPU_ERR_BAD_ARG;
+  batch->b->admit();
+  return LGPU_OK;
+}
+
+int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* report) {
+  if (!batch || !batch->b || n < 0) return LGPU_ERR_BAD_ARG;
+  lgpu::Batch& b = *batch->b;
+  const long long i0 = b.intervals_, l0 = b.launches_;
+  const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_, r0 = b.real_,
+               n0 = b.null_, hm0 = b.host_ms_, se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_;
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = LGPU_OK;
+  for (int i = 0; i < n && rc == LGPU_OK; ++i) {
+    b.admit();
+    if (b.active_.empty()) break;
+    rc = b.step();
+  }
+  if (running) *running = (int)b.active_.size();
+  if (report) {
+    report->intervals = b.intervals_ - i0;
+    report->kernel_launches = b.launches_ - l0;
+    report->elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    report->real_collisions = b.real_ - r0;
+    report->null_collisions = b.null_ - n0;
+    report->advance_ms = b.adv_ms_ - a0;
+    report->electron_steps = b.electron_steps_ - s0;
+    report->h2d_bytes = b.h2d_bytes_ - u0;
+    report->d2h_bytes = b.d2h_bytes_ - d0;
+    report->host_ms = b.host_ms_ - hm0;
+    report->secondaries = b.secondaries_ - se0;
+    report->spilled = b.spilled_ - sp0;
+    report->attached = b.attached_ - at0;
+  }
+  return rc;
+}
+
 int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, lgpu_batch_report* report) {
   if (!batch || !batch->b) return LGPU_ERR_BAD_ARG;
   lgpu::Batch& b = *batch->b;
   if (n != (int)b.members_.size()) return b.fail(LGPU_ERR_BAD_ARG, "n must be the number of added contexts");
   const long long i0 = b.intervals_, l0 = b.launches_;
-  const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_;
+  const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_, hm0 = b.host_ms_,
+               se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_;
   const auto t0 = std::chrono::steady_clock::now();
   int rc = b.run();
   const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -73,6 +114,10 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->electron_steps = b.electron_steps_ - s0;
     report->h2d_bytes = b.h2d_bytes_ - u0;
     report->d2h_bytes = b.d2h_bytes_ - d0;
+    report->host_ms = b.host_ms_ - hm0;
+    report->secondaries = b.secondaries_ - se0;
+    report->spilled = b.spilled_ - sp0;
+    report->attached = b.attached_ - at0;
   }
   b.members_.clear();
   b.active_.clear();

@@ -41,6 +41,8 @@ class Batch {
   // totals since creation
   long long intervals_ = 0, launches_ = 0;
   double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
+  double real_ = 0, null_ = 0;  // collisions of the batched intervals
+  double host_ms_ = 0, secondaries_ = 0, spilled_ = 0, attached_ = 0;
 
   struct Member {
     Engine* e = nullptr;
@@ -76,6 +78,7 @@ class Batch {
     max_slots_ = max_slots;
     int rc;
     if ((rc = cuda(cudaSetDevice(device), "cudaSetDevice"))) return rc;
+    if ((rc = cuda(prepare_kernels(), "kernel attributes"))) return rc;
     if ((rc = cuda(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device), "attribute"))) return rc;
     if ((rc = cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream"))) return rc;
     if ((rc = cuda(cudaEventCreate(&ev0_), "event")) || (rc = cuda(cudaEventCreate(&ev1_), "event"))) return rc;
@@ -117,6 +120,7 @@ class Batch {
     b.adv_prefix = reinterpret_cast<const int*>(d_stage_ + batch_prefix_offset());
     b.smp_prefix = b.adv_prefix + (kBatchMaxSlots + 1);
     b.hist_prefix = b.smp_prefix + (kBatchMaxSlots + 1);
+    b.hist2_prefix = b.hist_prefix + (kBatchMaxSlots + 1);
     b.slots = reinterpret_cast<const BatchSlot*>(d_stage_ + batch_slots_offset());
     b.gather = d_gather_;
     return b;
@@ -196,6 +200,7 @@ class Batch {
   // One synchronisation interval of every running member. Members whose stop
   // criteria hold (or that fail) finish here; *finished lists them.
   int step(std::vector<int>* finished = nullptr) {
+    const auto h0 = std::chrono::steady_clock::now();
     std::vector<int> go;
     go.reserve(active_.size());
     for (int idx : active_) {
@@ -220,8 +225,9 @@ class Batch {
     int* ap = reinterpret_cast<int*>(h_stage_ + batch_prefix_offset());
     int* sp = ap + (kBatchMaxSlots + 1);
     int* hp = sp + (kBatchMaxSlots + 1);
+    int* vp = hp + (kBatchMaxSlots + 1);
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
-    int na = 0, ns = 0, nh = 0;
+    int na = 0, ns = 0, nh = 0, nv = 0;
     double electrons = 0;
     for (int s = 0; s < n; ++s) {
       Engine* e = members_[go[s]].e;
@@ -231,18 +237,24 @@ class Batch {
       ap[s] = na;
       sp[s] = ns;
       hp[s] = nh;
+      vp[s] = nv;
       na += (N + kBatchAdvanceChunk - 1) / kBatchAdvanceChunk;
       if (sl[s].flags & kSlotSample) ns += (N + kBatchSampleChunk - 1) / kBatchSampleChunk;
-      if (sl[s].flags & kSlotHist) nh += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+      if (sl[s].flags & kSlotHist) {
+        nh += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+        if (sl[s].hist.cylindrical) nv += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+      }
     }
     ap[n] = na;
     sp[n] = ns;
     hp[n] = nh;
+    vp[n] = nv;
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_slots = n;
     hdr->adv_chunks = na;
     hdr->smp_chunks = ns;
     hdr->hist_chunks = nh;
+    hdr->hist2_chunks = nv;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];
@@ -255,7 +267,9 @@ class Batch {
     if ((rc = cuda(cudaMemcpyAsync(d_stage_, h_stage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
     if ((rc = cuda(cudaGraphLaunch(ge, stream_), "graph launch"))) return rc;
     if ((rc = cuda(cudaMemcpyAsync(h_gather_, d_gather_, down, cudaMemcpyDeviceToHost, stream_), "gather"))) return rc;
+    const auto h1 = std::chrono::steady_clock::now();
     if ((rc = cuda(cudaStreamSynchronize(stream_), "batched interval"))) return rc;
+    const auto h2 = std::chrono::steady_clock::now();
     if ((rc = cuda(cudaGetLastError(), "batched interval"))) return rc;
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
@@ -269,6 +283,11 @@ class Batch {
     still.reserve(go.size());
     for (int s = 0; s < n; ++s) {
       Member& m = members_[go[s]];
+      real_ += (double)(h_gather_[s].real_count - m.e->h_sc_->real_count);
+      null_ += (double)(h_gather_[s].null_count - m.e->h_sc_->null_count);
+      secondaries_ += h_gather_[s].sec_count;
+      spilled_ += h_gather_[s].spill_count;
+      attached_ += h_gather_[s].att_count;
       std::memcpy(m.e->h_sc_, &h_gather_[s], sizeof(DevScalars));
       rc = m.e->interval_post();
       if (rc == LGPU_OK) rc = m.e->solve_post();
@@ -280,6 +299,8 @@ class Batch {
       }
     }
     active_ = still;
+    const auto h3 = std::chrono::steady_clock::now();
+    host_ms_ += 1e3 * (std::chrono::duration<double>(h1 - h0).count() + std::chrono::duration<double>(h3 - h2).count());
     return LGPU_OK;
   }
 

@@ -132,14 +132,17 @@ template <int MODE = -1>
 __device__ __forceinline__ void free_flight(const FieldF& f, float phi0, float dt, float3& p, float3& v) {
   switch (MODE >= 0 ? MODE : f.mode) {
     case kFieldDC: {
-      // x += v dt + a dt^2/2 ; v += a dt
-      const float hdt2 = 0.5f * dt * dt;
-      p.x += v.x * dt + f.ax * hdt2;
-      p.y += v.y * dt + f.ay * hdt2;
-      p.z += v.z * dt + f.az * hdt2;
-      v.x += f.ax * dt;
-      v.y += f.ay * dt;
-      v.z += f.az * dt;
+      // x += v dt + a dt^2/2 ; v += a dt. The DC, AC and B branches spell out
+      // every rounding (explicit _rn operations) so that each kernel that
+      // inlines them computes the same bits, whatever the compiler's choice
+      // of multiply-add contraction in the surrounding code.
+      const float hdt2 = __fmul_rn(__fmul_rn(0.5f, dt), dt);
+      p.x = __fadd_rn(p.x, __fmaf_rn(v.x, dt, __fmul_rn(f.ax, hdt2)));
+      p.y = __fadd_rn(p.y, __fmaf_rn(v.y, dt, __fmul_rn(f.ay, hdt2)));
+      p.z = __fadd_rn(p.z, __fmaf_rn(v.z, dt, __fmul_rn(f.az, hdt2)));
+      v.x = __fmaf_rn(f.ax, dt, v.x);
+      v.y = __fmaf_rn(f.ay, dt, v.y);
+      v.z = __fmaf_rn(f.az, dt, v.z);
       break;
     }
     case kFieldAC: {
@@ -147,37 +150,37 @@ __device__ __forceinline__ void free_flight(const FieldF& f, float phi0, float d
       const float w = f.w;
       float sPhi, cPhi, sPh, cPh;
       sincosf(phi0, &sPhi, &cPhi);
-      const float wdt = w * dt;
-      sincosf(phi0 + wdt, &sPh, &cPh);
-      const float k = f.e_me / w;  // e/(m w)
-      const float aux1 = k / w * (cPh + wdt * sPhi - cPhi);
-      const float aux2 = k * (sPhi - sPh);
-      p.x += v.x * dt + f.Ex * aux1;
-      p.y += v.y * dt;
-      p.z += v.z * dt + f.Ez * aux1;
-      v.x += f.Ex * aux2;
-      v.z += f.Ez * aux2;
+      const float wdt = __fmul_rn(w, dt);
+      sincosf(__fadd_rn(phi0, wdt), &sPh, &cPh);
+      const float k = __fdiv_rn(f.e_me, w);  // e/(m w)
+      const float aux1 = __fmul_rn(__fdiv_rn(k, w), __fsub_rn(__fmaf_rn(wdt, sPhi, cPh), cPhi));
+      const float aux2 = __fmul_rn(k, __fsub_rn(sPhi, sPh));
+      p.x = __fadd_rn(p.x, __fmaf_rn(v.x, dt, __fmul_rn(f.Ex, aux1)));
+      p.y = __fmaf_rn(v.y, dt, p.y);
+      p.z = __fadd_rn(p.z, __fmaf_rn(v.z, dt, __fmul_rn(f.Ez, aux1)));
+      v.x = __fmaf_rn(f.Ex, aux2, v.x);
+      v.z = __fmaf_rn(f.Ez, aux2, v.z);
       break;
     }
     case kFieldB: {
       // DC E in the x-z plane, B along z: BoltzmannMC.C:835-849
       const float W = f.W;
-      const float Wdt = W * dt;
+      const float Wdt = __fmul_rn(W, dt);
       float sW, cW;
       sincosf(Wdt, &sW, &cW);
-      const float sh = sinf(0.5f * Wdt);
-      const float cWm1 = -2.0f * sh * sh;  // cos(W dt) - 1 without cancellation
-      const float sW_W = sW / W;
-      const float aux2 = cWm1 / W;
-      const float vEx = f.e_me * f.Ex / W;
-      const float az = f.e_me * f.Ez;
+      const float sh = sinf(__fmul_rn(0.5f, Wdt));
+      const float cWm1 = __fmul_rn(__fmul_rn(-2.0f, sh), sh);  // cos(W dt) - 1 without cancellation
+      const float sW_W = __fdiv_rn(sW, W);
+      const float aux2 = __fdiv_rn(cWm1, W);
+      const float vEx = __fdiv_rn(__fmul_rn(f.e_me, f.Ex), W);
+      const float az = __fmul_rn(f.e_me, f.Ez);
       const float vx0 = v.x, vy0 = v.y, vz0 = v.z;
-      p.x += vx0 * sW_W + (vy0 + vEx) * aux2;
-      p.y += -vx0 * aux2 + vy0 * sW_W + vEx * (sW_W - dt);
-      p.z += vz0 * dt - 0.5f * az * dt * dt;
-      v.x = vx0 * cW - vy0 * sW - vEx * sW;
-      v.y = vx0 * sW + vy0 * cW + vEx * cWm1;
-      v.z = vz0 - az * dt;
+      p.x = __fadd_rn(p.x, __fmaf_rn(vx0, sW_W, __fmul_rn(__fadd_rn(vy0, vEx), aux2)));
+      p.y = __fadd_rn(p.y, __fmaf_rn(vEx, __fsub_rn(sW_W, dt), __fmaf_rn(vy0, sW_W, __fmul_rn(-vx0, aux2))));
+      p.z = __fadd_rn(p.z, __fsub_rn(__fmul_rn(vz0, dt), __fmul_rn(__fmul_rn(__fmul_rn(0.5f, az), dt), dt)));
+      v.x = __fsub_rn(__fmaf_rn(vx0, cW, __fmul_rn(-vy0, sW)), __fmul_rn(vEx, sW));
+      v.y = __fmaf_rn(vEx, cWm1, __fmaf_rn(vx0, sW, __fmul_rn(vy0, cW)));
+      v.z = __fsub_rn(vz0, __fmul_rn(az, dt));
       break;
     }
     case kFieldECR: {
@@ -327,8 +330,9 @@ struct CollResult {
   float3 ej_v;        // secondary velocity
 };
 
+// (rounding spelled out, as in the flights)
 __device__ __forceinline__ float energy_of(float3 v, float half_me_over_e) {
-  return (v.x * v.x + v.y * v.y + v.z * v.z) * half_me_over_e;
+  return __fmul_rn(__fmaf_rn(v.z, v.z, __fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x))), half_me_over_e);
 }
 
 // Collision kinematics of the chosen process (BoltzmannMC.C:1115-1280).
@@ -474,18 +478,26 @@ __device__ __forceinline__ int row_count_below(const float2* row, int P, int str
   return min(cnt, P - 1);
 }
 
-// Process choice for a cold gas (BoltzmannMC.C:1033-1097): null test on the
-// interpolated total frequency, the first interpolated cumulative sum that
-// reaches the random number, backward skip of zero-rate processes. Returns -1
-// for null.
+// Null test of a cold gas (BoltzmannMC.C:1033-1052): r = U nu_trial against
+// the interpolated total frequency. False for a null collision; r is kept
+// for the process choice.
 template <class Rng>
-__device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, float energy, float speed, Rng& rng) {
-  const float r = nu_trial * rng.oc();
+__device__ __forceinline__ bool cold_real(const TablesF& t, float nu_trial, float energy, Rng& rng, float& r) {
+  r = nu_trial * rng.oc();
   int i1;
   float w1, w2;
   row_weights(energy * t.inv_step, t.M, i1, w1, w2);
   const float2 nt = __ldg(&t.nu_pair[i1]);
-  if (r > w1 * nt.x + w2 * nt.y) return -1;
+  return !(r > w1 * nt.x + w2 * nt.y);
+}
+
+// Process of a real cold collision whose null test drew r (BoltzmannMC.C:1053-1097):
+// the first interpolated cumulative sum that reaches r/(N|v|), backward skip of
+// zero-rate processes.
+__device__ __forceinline__ int cold_choice(const TablesF& t, float energy, float speed, float r) {
+  int i1;
+  float w1, w2;
+  row_weights(energy * t.inv_step, t.M, i1, w1, w2);
   const float rcs = r * t.inv_N / speed;
   int chosen = row_count_below(t.cum_pair + (size_t)i1 * t.stride, t.P, t.stride, w1, w2, rcs);
   const float2* sig = t.sig_pair + (size_t)i1 * t.stride;
@@ -495,6 +507,14 @@ __device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, flo
     --chosen;
   }
   return chosen;
+}
+
+// Process choice for a cold gas: -1 for null.
+template <class Rng>
+__device__ __forceinline__ int choose_cold(const TablesF& t, float nu_trial, float energy, float speed, Rng& rng) {
+  float r;
+  if (!cold_real(t, nu_trial, energy, rng, r)) return -1;
+  return cold_choice(t, energy, speed, r);
 }
 
 // Process choice with thermal targets, gas by gas (BoltzmannMC.C:916-1031):
@@ -560,26 +580,47 @@ __device__ __forceinline__ int choose_thermal(const TablesF& t, const GasF* gase
   return chosen;
 }
 
-// One collision event at the end of a free flight (BoltzmannMC.C:907-1113).
+// Whether the event samples a thermal target (BoltzmannMC.C:916).
+__device__ __forceinline__ bool is_thermal(const Consts& c, float energy) {
+  return (c.gas_temp == kGasTempTrue) || (c.gas_temp == kGasTempSmart && energy < c.smart_energy);
+}
+
+// The rest of a collision event once a cold gas's null test said real (with
+// its r), or the whole event for a thermal target (r unused).
 template <class Rng>
-__device__ __forceinline__ void collide(const Consts& c, const TablesF& t, const ProcF* procs, const GasF* gases,
-                                        float nu_trial, float3& v, float& energy, Rng& rng, CollResult& out) {
+__device__ __forceinline__ void collide_pending(const Consts& c, const TablesF& t, const ProcF* procs,
+                                                const GasF* gases, float nu_trial, float r, float3& v,
+                                                float& energy, Rng& rng, CollResult& out) {
   out.chosen = -1;
   out.dE = 0.0f;
   out.ionized = 0;
-  const bool thermal = (c.gas_temp == kGasTempTrue) || (c.gas_temp == kGasTempSmart && energy < c.smart_energy);
+  const bool thermal = is_thermal(c, energy);
   float3 tv = make_float3(0.f, 0.f, 0.f);
   int ch;
   if (thermal) {
     ch = choose_thermal(t, gases, c.G, nu_trial, v, rng, tv, c.inv_qe);
   } else {
     const float speed = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-    ch = choose_cold(t, nu_trial, energy, speed, rng);
+    ch = cold_choice(t, energy, speed, r);
   }
   if (ch < 0) return;
   const ProcF pr = procs[ch];
   if (!apply_collision(c, pr, thermal, tv, v, energy, rng, out)) return;
   out.chosen = ch;
+}
+
+// One collision event at the end of a free flight (BoltzmannMC.C:907-1113).
+template <class Rng>
+__device__ __forceinline__ void collide(const Consts& c, const TablesF& t, const ProcF* procs, const GasF* gases,
+                                        float nu_trial, float3& v, float& energy, Rng& rng, CollResult& out) {
+  float r = 0.0f;
+  if (!is_thermal(c, energy) && !cold_real(t, nu_trial, energy, rng, r)) {
+    out.chosen = -1;
+    out.dE = 0.0f;
+    out.ionized = 0;
+    return;
+  }
+  collide_pending(c, t, procs, gases, nu_trial, r, v, energy, rng, out);
 }
 
 }  // namespace lgpu

@@ -108,6 +108,7 @@ class Engine {
     if (cfg_.n_energy_cells < 1 || cfg_.n_energy_cells > 4096) return fail(LGPU_ERR_BAD_ARG, "nEnergyCells must be 1..4096");
     if (cfg_.sync_oversampling < 1) return fail(LGPU_ERR_BAD_ARG, "synchronizationOverSampling must be >= 1");
     LGPU_CU(cudaSetDevice(cfg_.device));
+    LGPU_CU(prepare_kernels());
     LGPU_CU(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, cfg_.device));
     LGPU_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     LGPU_CU(cudaEventCreate(&ev0_));
@@ -566,6 +567,8 @@ class Engine {
     p.n_electrons = N_;
     p.sec = d_sec_;
     p.sec_count = &d_sc_->sec_count;
+    p.sec_cap = sec_cap_;
+    p.counts = d_sc_->pop_counts;
     p.att_list = d_att_;
     p.att_count = &d_sc_->att_count;
     p.claim = d_claim_;
@@ -599,7 +602,7 @@ class Engine {
       d.salt = 2;
       launch_advance(d, stream_);
       launch_pop_control(pop_args(), stream_);
-      launches_ += 2;
+      launches_ += 1 + kPopLaunches;
     }
     if (sample) enqueue_sample();
     copy(h_sc_, d_sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost);
@@ -720,6 +723,7 @@ class Engine {
     if (e == 0) return LGPU_OK;
     if (e == 2) return fail(LGPU_ERR_OVERFLOW, "secondary or spill buffer full within one interval");
     if (e == 3) return fail(LGPU_ERR_OVERFLOW, "collision budget of one interval exhausted");
+    if (e == 6) return fail(LGPU_ERR_STATE, "batched interval: chunk outside the ensemble");
     return fail(LGPU_ERR_OVERFLOW, "population control retry limit reached (code %d)", e);
   }
 
@@ -883,7 +887,7 @@ class Engine {
       return LGPU_OK;
     }
     launch_hist(h, stream_);
-    ++launches_;
+    launches_ += h.cylindrical ? 2 : 1;
     return LGPU_OK;
   }
 
@@ -1121,7 +1125,7 @@ class Engine {
     if (!hist_pending_) return LGPU_OK;
     hist_pending_ = false;
     launch_hist(pending_hist_, stream_);
-    ++launches_;
+    launches_ += pending_hist_.cylindrical ? 2 : 1;
     return LGPU_OK;
   }
   SampleArgs sample_args() const {

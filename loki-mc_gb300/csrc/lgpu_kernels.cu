@@ -129,9 +129,11 @@ __device__ __forceinline__ IntervalView interval_view(const AdvanceArgs& a) {
 // The electron a lane holds.
 struct Lane {
   bool have;
-  int slot;  // ensemble slot, -1 for a secondary
+  bool pending;  // a real collision waits for the warp's next collision turn
+  int slot;      // ensemble slot, -1 for a secondary
   float3 p, v;
   float s, t, energy;
+  float r;       // the pending collision's null-test draw (cold gas)
   int events;
   PcgStream rng;
 };
@@ -144,6 +146,8 @@ struct LaneTally {
 
 __device__ __forceinline__ void reset_lane(Lane& L) {
   L.have = false;
+  L.pending = false;
+  L.r = 0.0f;
   L.slot = 0;
   L.p = make_float3(0.f, 0.f, 0.f);
   L.v = make_float3(0.f, 0.f, 0.f);
@@ -186,6 +190,7 @@ __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const I
     L.rng.init((uint32_t)idx, iv.interval, a.seed, a.salt);
     L.energy = energy_of(L.v, a.c.half_me_over_e);
     L.events = 0;
+    L.pending = false;
     L.have = true;
   }
 }
@@ -202,6 +207,7 @@ __device__ __forceinline__ void lane_take_secondary(const AdvanceArgs& a, const 
   L.rng.init(id, iv.interval, a.seed, a.salt + 1u);
   L.energy = energy_of(L.v, a.c.half_me_over_e);
   L.events = 0;
+  L.pending = false;
   L.have = true;
 }
 
@@ -225,85 +231,127 @@ __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const Inte
   return qn;
 }
 
-// One event of a lane's electron: a free flight to the next collision or,
-// when that lies beyond the synchronisation time, to the synchronisation time
-// (BoltzmannMC.C:650-675); the flight code is the same for both so the lanes
-// stay converged.
+// A finished electron: an ensemble electron goes back to its slot (attached
+// ones flagged), a secondary to the list of secondaries at the
+// synchronisation time.
+__device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneTally& tl, bool dead) {
+  if (L.slot >= 0) {
+    a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
+    a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
+  } else if (!dead) {
+    const int k = append_slot(a.sec_count);
+    if (k < a.sec_cap) {
+      a.sec[2 * k] = make_float4(L.p.x, L.p.y, L.p.z, L.s);
+      a.sec[2 * k + 1] = make_float4(L.v.x, L.v.y, L.v.z, 0.0f);
+    } else {
+      atomicExch(a.error_flag, 2);
+    }
+  }
+  if (!dead) tl.e_max = fmaxf(tl.e_max, L.energy);
+  L.have = false;
+}
+
+// The flight turn of a lane's electron: a free flight to the next collision
+// or, when that lies beyond the synchronisation time, to the synchronisation
+// time (BoltzmannMC.C:650-675; the flight code is the same for both so the
+// lanes stay converged), then the null test of a cold gas. A real collision
+// (or any thermal-target event) is left pending for the collision turn, which
+// the warp takes once enough of its lanes have one: the long collision code
+// then runs on most of the warp's lanes instead of a few. Each electron draws
+// its random numbers in the same order either way.
 template <int MODE>
-__device__ __forceinline__ void lane_event(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
-                                           Lane& L, LaneTally& tl) {
+__device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const IntervalView& iv, Lane& L, LaneTally& tl) {
   if (L.s < 0.0f) L.s = -__logf(L.rng.oo());
   const float tau = L.s * iv.inv_nu;
   const bool partial = L.t + tau > iv.T;
   const float dt = partial ? iv.T - L.t : tau;
-  free_flight<MODE>(iv.field, iv.phi0 + iv.phase_rate * L.t, dt, L.p, L.v);
+  free_flight<MODE>(iv.field, __fmaf_rn(iv.phase_rate, L.t, iv.phi0), dt, L.p, L.v);
   {
     const float e1 = energy_of(L.v, a.c.half_me_over_e);
     tl.gain += e1 - L.energy;
     L.energy = e1;
   }
-  bool finished = partial, dead = false;
   if (partial) {
-    L.s = fmaxf(L.s - iv.nu * dt, 0.0f);
+    L.s = fmaxf(__fmaf_rn(-iv.nu, dt, L.s), 0.0f);
+    lane_finish(a, L, tl, false);
+    return;
+  }
+  L.t += tau;
+  if (is_thermal(a.c, L.energy) || cold_real(iv.tab, iv.nu, L.energy, L.rng, L.r)) {
+    L.pending = true;
+    return;
+  }
+  ++tl.null_n;
+  L.s = -__logf(L.rng.oo());  // next free flight (BoltzmannMC.C:670)
+  if (++L.events >= (1 << 20)) {
+    atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+    lane_finish(a, L, tl, false);
+  }
+}
+
+// The collision turn: process choice, kinematics, tallies, secondaries and
+// attachment (BoltzmannMC.C:907-1280).
+__device__ __forceinline__ void lane_real(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
+                                          Lane& L, LaneTally& tl) {
+  L.pending = false;
+  CollResult cr;
+  collide_pending(a.c, iv.tab, sh.proc, sh.gas, iv.nu, L.r, L.v, L.energy, L.rng, cr);
+  bool finished = false, dead = false;
+  if (cr.chosen < 0) {
+    ++tl.null_n;
   } else {
-    L.t += tau;
-    CollResult cr;
-    collide(a.c, iv.tab, sh.proc, sh.gas, iv.nu, L.v, L.energy, L.rng, cr);
-    if (cr.chosen < 0) {
-      ++tl.null_n;
-    } else {
-      ++tl.real_n;
-      atomicAdd(&sh.count[cr.chosen], 1u);
-      if (cr.dE >= 0.0f) atomicAdd(&sh.gain[cr.chosen], cr.dE);
-      else atomicAdd(&sh.loss[cr.chosen], cr.dE);
-      const int ptype = sh.proc[cr.chosen].type;
-      if (ptype == kIonization) {
-        const float4 A = make_float4(L.p.x, L.p.y, L.p.z, L.t);
-        const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
-        const int k = atomicAdd(&sh.qn[wid], 1);
-        if (k < kLocalQ) {
-          sh.qa[wid][k] = A;
-          sh.qb[wid][k] = B;
+    ++tl.real_n;
+    atomicAdd(&sh.count[cr.chosen], 1u);
+    if (cr.dE >= 0.0f) atomicAdd(&sh.gain[cr.chosen], cr.dE);
+    else atomicAdd(&sh.loss[cr.chosen], cr.dE);
+    const int ptype = sh.proc[cr.chosen].type;
+    if (ptype == kIonization) {
+      const float4 A = make_float4(L.p.x, L.p.y, L.p.z, L.t);
+      const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
+      const int k = atomicAdd(&sh.qn[wid], 1);
+      if (k < kLocalQ) {
+        sh.qa[wid][k] = A;
+        sh.qb[wid][k] = B;
+      } else {
+        const int g = append_slot(a.spill_count);
+        if (g < a.spill_cap) {
+          a.spill[2 * g] = A;
+          a.spill[2 * g + 1] = B;
         } else {
-          const int g = append_slot(a.spill_count);
-          if (g < a.spill_cap) {
-            a.spill[2 * g] = A;
-            a.spill[2 * g + 1] = B;
-          } else {
-            atomicExch(a.error_flag, 2);  // spill buffer full: the host reports it
-          }
-        }
-      } else if (ptype == kAttachment) {
-        dead = true;
-        finished = true;
-        tl.time_adj -= iv.T - L.t;  // electron-time the attached electron no longer spends
-        if (L.slot >= 0) {
-          const int k = append_slot(a.att_count);
-          a.att_list[k] = L.slot;
+          atomicExch(a.error_flag, 2);  // spill buffer full: the host reports it
         }
       }
-    }
-    L.s = -__logf(L.rng.oo());  // next free flight (BoltzmannMC.C:670)
-    if (++L.events >= (1 << 20) && !finished) {
-      atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+    } else if (ptype == kAttachment) {
+      dead = true;
       finished = true;
+      tl.time_adj -= iv.T - L.t;  // electron-time the attached electron no longer spends
+      if (L.slot >= 0) {
+        const int k = append_slot(a.att_count);
+        a.att_list[k] = L.slot;
+      }
     }
   }
-  if (finished) {
-    if (L.slot >= 0) {
-      a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
-      a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
-    } else if (!dead) {
-      const int k = append_slot(a.sec_count);
-      if (k < a.sec_cap) {
-        a.sec[2 * k] = make_float4(L.p.x, L.p.y, L.p.z, L.s);
-        a.sec[2 * k + 1] = make_float4(L.v.x, L.v.y, L.v.z, 0.0f);
-      } else {
-        atomicExch(a.error_flag, 2);
-      }
-    }
-    if (!dead) tl.e_max = fmaxf(tl.e_max, L.energy);
-    L.have = false;
+  L.s = -__logf(L.rng.oo());  // next free flight (BoltzmannMC.C:670)
+  if (++L.events >= (1 << 20) && !finished) {
+    atomicExch(a.error_flag, 3);  // collision budget of one interval exhausted
+    finished = true;
+  }
+  if (finished) lane_finish(a, L, tl, dead);
+}
+
+// Lanes with a pending collision that start the warp's collision turn.
+constexpr int kRealBatch = 20;
+
+// One turn of a warp: the collision turn when kRealBatch lanes (or every lane
+// with an electron) have a pending collision, else the flight turn.
+template <int MODE>
+__device__ __forceinline__ void warp_turn(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
+                                          Lane& L, LaneTally& tl, unsigned live) {
+  const unsigned pend = __ballot_sync(0xffffffffu, L.pending);
+  if (__popc(pend) >= kRealBatch || pend == live) {
+    if (L.pending) lane_real(a, sh, wid, iv, L, tl);
+  } else if (L.have && !L.pending) {
+    lane_flight<MODE>(a, iv, L, tl);
   }
 }
 
@@ -415,13 +463,13 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh
         sp_next += max(take2, 0);
       }
     }
-    if (!__any_sync(0xffffffffu, L.have)) {
+    const unsigned live = __ballot_sync(0xffffffffu, L.have);
+    if (!live) {
       const bool spill_left = drain && sp_next < min(*(volatile int*)a.spill_count, a.spill_cap);
       if (exhausted && qn == 0 && !spill_left) break;
       continue;
     }
-    if (!L.have) continue;
-    lane_event<MODE>(a, sh, wid, iv, L, tl);
+    warp_turn<MODE>(a, sh, wid, iv, L, tl, live);
   }
   block_flush(a, sh, tl, lane, wid);
 }
@@ -486,12 +534,12 @@ __device__ __forceinline__ void batch_chunk(const AdvanceArgs& a, AdvShared& sh,
     }
     int qn = min(sh.qn[wid], kLocalQ);
     if (exhausted) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, 0x3FFFFu);
-    if (!__any_sync(0xffffffffu, L.have)) {
+    const unsigned live = __ballot_sync(0xffffffffu, L.have);
+    if (!live) {
       if (exhausted && qn == 0) break;
       continue;
     }
-    if (!L.have) continue;
-    lane_event<MODE>(a, sh, wid, iv, L, tl);
+    warp_turn<MODE>(a, sh, wid, iv, L, tl, live);
   }
 }
 
@@ -527,7 +575,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
     }
     __syncthreads();
     const int slot = s_slot;
-    if (slot != cur) {
+    if (slot != cur || slot < 0) {  // a new slot, or no chunk left (also before the first)
       if (cur >= 0) block_flush(s_a, sh, tl, lane, wid);
       reset_tally(tl);
       __syncthreads();
@@ -541,7 +589,11 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
     }
     const int first = (s_chunk - b.adv_prefix[slot]) * kBatchAdvanceChunk;
     const int cnt = min(kBatchAdvanceChunk, s_a.n - first);
-    batch_chunk<MODE>(s_a, sh, s_iv, tl, first, cnt, &s_next, sec_id, id_hi);
+    if (first >= 0 && cnt > 0) {
+      batch_chunk<MODE>(s_a, sh, s_iv, tl, first, cnt, &s_next, sec_id, id_hi);
+    } else if (threadIdx.x == 0) {
+      atomicExch(s_a.error_flag, 6);  // inconsistent chunk table: the host reports it
+    }
     __syncthreads();  // every warp is done with the chunk before the counters are reused
   }
 }
@@ -686,7 +738,7 @@ __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int
   for (int i = begin; i < end; i += step) {
     const float4 A = a.state[2 * i];
     const float4 B = a.state[2 * i + 1];
-    const float e = (B.x * B.x + B.y * B.y + B.z * B.z) * a.half_me_over_e;
+    const float e = energy_of(make_float3(B.x, B.y, B.z), a.half_me_over_e);
     e_max = fmaxf(e_max, e);
     const float x = A.x, y = A.y, z = A.z, vx = B.x, vy = B.y, vz = B.z;
     m[0] += e;
@@ -722,49 +774,115 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
 }
 
 // ------------------------------------------------------------- histograms
-constexpr int kHistThreads = 512;
-constexpr int kMaxEedfCells = 4096;
+// The tallies of one sample in two passes over the electrons' velocities,
+// each in blocks of up to kHistChunk electrons that count in shared memory and
+// then add one atomic per occupied cell to the FP64 tallies:
+//   pass A: EEDF counts (32-bit) and EADF counts (16-bit, two per word),
+//   pass B: EVDF counts (16-bit, two per word), cylindrical conditions only.
+// A block's chunk is below 2^16 electrons, so no 16-bit count can carry into
+// its neighbour. A condition whose grid is larger than the block's shared
+// memory counts that tally with global atomics instead.
+constexpr int kHistChunk = 32768;
+constexpr int kHistAThreads = 1024;
+constexpr int kHistBThreads = 512;
+constexpr int kHistASmem = 224 * 1024;  // one block per SM
+constexpr int kHistBSmem = 96 * 1024;   // two blocks per SM
 
-// Tallies of electrons begin, begin+step, ... < end: the EEDF counts go
-// through a shared-memory histogram, EADF and EVDF straight to global memory.
-// Every thread of the block calls this; s_h is the block's scratch.
-__device__ __forceinline__ void hist_range(const HistArgs& a, int begin, int end, int step, unsigned int* s_h) {
-  for (int c = threadIdx.x; c < a.n_e_cells; c += blockDim.x) s_h[c] = 0u;
+__device__ __forceinline__ void hist_cells(const HistArgs& a, float4 B, int& c, int& cy, int& rx, int& ry) {
+  // MathFunctions.C:61-81 (energy) and 106-127 (energy x cos, radial x axial velocity)
+  const float v2xy = __fmaf_rn(B.y, B.y, __fmul_rn(B.x, B.x));
+  const float v2 = __fmaf_rn(B.z, B.z, v2xy);
+  const float e = __fmul_rn(v2, a.half_me_over_e);  // energy_of's rounding
+  c = (int)(e * a.inv_e_step);
+  cy = rx = ry = -1;
+  if (a.cylindrical) {
+    const float speed = sqrtf(v2);
+    const float cosang = B.z / speed;
+    cy = (int)((cosang + 1.0f) * (0.5f * (float)a.n_cos));
+    rx = (int)(sqrtf(v2xy) * a.inv_rad_step);
+    ry = (int)((B.z + a.max_speed) * a.inv_ax_step);
+  }
+}
+
+// pass A over electrons [first, last) of one condition
+__device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int last, unsigned int* sm, int sm_words) {
+  const int nE = a.n_e_cells;
+  const int nA = a.cylindrical ? nE * a.n_cos : 0;
+  const int nAw = (nA + 1) >> 1;
+  const bool a_shared = a.cylindrical && nE + nAw <= sm_words;
+  unsigned int* hE = sm;
+  unsigned int* hA = sm + nE;
+  const int zero_words = nE + (a_shared ? nAw : 0);
+  for (int w = threadIdx.x; w < zero_words; w += blockDim.x) sm[w] = 0u;
   __syncthreads();
-  for (int i = begin; i < end; i += step) {
-    const float4 B = a.state[2 * i + 1];
-    const float v2xy = B.x * B.x + B.y * B.y;
-    const float v2 = v2xy + B.z * B.z;
-    const float e = v2 * a.half_me_over_e;
-    // MathFunctions.C:61-81: cell = (x - x0) / step, counted when below the cell count
-    const int c = (int)(e * a.inv_e_step);
-    if (c < a.n_e_cells) atomicAdd(&s_h[c], 1u);
-    if (a.cylindrical) {
-      const float speed = sqrtf(v2);
-      const float cosang = B.z / speed;
-      // MathFunctions.C:106-127
-      const int cx = c;
-      const int cy = (int)((cosang + 1.0f) * (0.5f * (float)a.n_cos));
-      if (cx < a.n_e_cells && cx >= 0 && cy < a.n_cos && cy >= 0) atomicAdd(&a.eadf[(size_t)cx * a.n_cos + cy], 1.0);
-      const float vr = sqrtf(v2xy);
-      const int rx = (int)(vr * a.inv_rad_step);
-      const int ry = (int)((B.z + a.max_speed) * a.inv_ax_step);
-      if (rx < a.n_rad && rx >= 0 && ry < a.n_ax && ry >= 0) atomicAdd(&a.evdf[(size_t)rx * a.n_ax + ry], 1.0);
+  for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+    int c, cy, rx, ry;
+    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
+    if (c >= 0 && c < nE) atomicAdd(&hE[c], 1u);
+    if (a.cylindrical && c < nE && c >= 0 && cy < a.n_cos && cy >= 0) {
+      const int idx = c * a.n_cos + cy;
+      if (a_shared) atomicAdd(&hA[idx >> 1], 1u << ((idx & 1) << 4));
+      else atomicAdd(&a.eadf[idx], 1.0);
     }
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < a.n_e_cells; c += blockDim.x) {
-    const unsigned int h = s_h[c];
+  for (int c = threadIdx.x; c < nE; c += blockDim.x) {
+    const unsigned int h = hE[c];
     if (h) {
       atomicAdd(&a.eedf[c], (double)h);
       if (a.eedf_periodic_row) atomicAdd(&a.eedf_periodic_row[c], (double)h);
     }
   }
+  if (a_shared) {
+    for (int w = threadIdx.x; w < nAw; w += blockDim.x) {
+      const unsigned int h = hA[w];
+      if (h & 0xFFFFu) atomicAdd(&a.eadf[2 * w], (double)(h & 0xFFFFu));
+      if ((h >> 16) && 2 * w + 1 < nA) atomicAdd(&a.eadf[2 * w + 1], (double)(h >> 16));
+    }
+  }
+  __syncthreads();
 }
 
-__global__ void __launch_bounds__(kHistThreads) k_hist(HistArgs a) {
-  __shared__ unsigned int s_h[kMaxEedfCells];
-  hist_range(a, blockIdx.x * blockDim.x + threadIdx.x, a.n, gridDim.x * blockDim.x, s_h);
+// pass B over electrons [first, last) of one cylindrical condition
+__device__ __forceinline__ void hist_chunk_b(const HistArgs& a, int first, int last, unsigned int* sm, int sm_words) {
+  const int nV = a.n_rad * a.n_ax;
+  const int nVw = (nV + 1) >> 1;
+  const bool v_shared = nVw <= sm_words;
+  if (v_shared)
+    for (int w = threadIdx.x; w < nVw; w += blockDim.x) sm[w] = 0u;
+  __syncthreads();
+  for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+    int c, cy, rx, ry;
+    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
+    if (rx < a.n_rad && rx >= 0 && ry < a.n_ax && ry >= 0) {
+      const int idx = rx * a.n_ax + ry;
+      if (v_shared) atomicAdd(&sm[idx >> 1], 1u << ((idx & 1) << 4));
+      else atomicAdd(&a.evdf[idx], 1.0);
+    }
+  }
+  __syncthreads();
+  if (v_shared) {
+    for (int w = threadIdx.x; w < nVw; w += blockDim.x) {
+      const unsigned int h = sm[w];
+      if (h & 0xFFFFu) atomicAdd(&a.evdf[2 * w], (double)(h & 0xFFFFu));
+      if ((h >> 16) && 2 * w + 1 < nV) atomicAdd(&a.evdf[2 * w + 1], (double)(h >> 16));
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kHistAThreads) k_hist_a(HistArgs a) {
+  extern __shared__ unsigned int sm_hist[];
+  const int chunks = (a.n + kHistChunk - 1) / kHistChunk;
+  for (int c = blockIdx.x; c < chunks; c += gridDim.x)
+    hist_chunk_a(a, c * kHistChunk, min(a.n, (c + 1) * kHistChunk), sm_hist, kHistASmem / 4);
+}
+
+__global__ void __launch_bounds__(kHistBThreads) k_hist_b(HistArgs a) {
+  extern __shared__ unsigned int sm_hist[];
+  const int chunks = (a.n + kHistChunk - 1) / kHistChunk;
+  for (int c = blockIdx.x; c < chunks; c += gridDim.x)
+    hist_chunk_b(a, c * kHistChunk, min(a.n, (c + 1) * kHistChunk), sm_hist, kHistBSmem / 4);
 }
 
 // ------------------------------------------------------- population control
@@ -788,80 +906,108 @@ __device__ __forceinline__ void add_growth(double* growth, double e) {
   if (g.thread_rank() == 0) atomicAdd(growth, tot);
 }
 
-__device__ __forceinline__ float energy4(float4 B, float hme) { return (B.x * B.x + B.y * B.y + B.z * B.z) * hme; }
+__device__ __forceinline__ float energy4(float4 B, float hme) { return energy_of(make_float3(B.x, B.y, B.z), hme); }
 
-// Population control (BoltzmannMC.C:1282-1408) in one block, every phase
-// separated by a block barrier. All electrons and secondaries are at the
-// synchronisation time here.
-//  (0) secondaries that did not attach are compacted;
-//  (1) attached slots take secondaries, last secondary first (:1344-1359);
-//  (2) remaining attached slots clone a random non-attached electron, whose
-//      energy enters the growth term (:1360-1376);
-//  (3) excess secondaries: a uniformly random subset of size m is removed from
-//      the pool of N slots + m unplaced secondaries - the outcome of the
-//      reference's sequential uniform removal (:1379-1407) - and the surviving
-//      secondaries take the removed slots; removed energies leave the growth term.
-constexpr int kPopThreads = 1024;
-__device__ __forceinline__ void pop_body(const PopArgs& a, int* s_n) {
-  const int n_sec_all = min(*a.sec_count, 1 << 30);
-  const int n_att = *a.att_count;
-  if (n_sec_all == 0 && n_att == 0) return;
-  const uint64_t interval = a.ctl->interval;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const float hme = a.half_me_over_e;
-  if (tid < 4) s_n[tid] = 0;
-  __syncthreads();
-  // (0)
-  for (int j = tid; j < n_sec_all; j += nt)
-    if (a.sec[2 * j + 1].w == 0.0f) a.alive[atomicAdd(&s_n[0], 1)] = j;
-  __syncthreads();
-  const int n_sec = s_n[0];
-  // (1)
+// Population control (BoltzmannMC.C:1282-1408), when all electrons and
+// secondaries are at the synchronisation time. Five launches, each a grid of
+// blocks over one or many slots (blockIdx.y) whose threads stride over the
+// slot's items:
+//  (0) the secondaries that did not attach are listed (alive);
+//  (1) attached slots take secondaries, one per slot (:1344-1359); the slots
+//      that stay attached are marked in the claim bitmap, so that no clone is
+//      made from another clone;
+//  (2) the slots still attached clone a random non-attached electron, whose
+//      energy enters the growth term (:1360-1376); or, when secondaries are
+//      left over, a uniformly random subset of size m is drawn from the pool of
+//      N slots + m unplaced secondaries - the outcome of the reference's
+//      sequential uniform removal (:1379-1407) - by claiming pool bits;
+//  (3) clone marks are cleared; the removed ensemble slots and the unremoved
+//      secondaries are listed, removed energies leave the growth term;
+//  (4) the listed secondaries move into the removed slots; removal marks are
+//      cleared, so the bitmap is zero again.
+constexpr int kPopThreads = 256;
+constexpr int kPopBlocks = 64;           // blocks per slot, single condition
+constexpr int kPopBlocksPerSlot = 16;    // blocks per slot, batches
+
+// one condition, arguments by value
+struct PopOne {
+  PopArgs a;
+  __device__ const PopArgs* get(int s) const { return s == 0 ? &a : nullptr; }
+};
+// the slots of a batch that ionize or attach
+struct PopBatch {
+  const BatchHeader* hdr;
+  const BatchSlot* slots;
+  __device__ const PopArgs* get(int s) const {
+    return (s < hdr->n_slots && (slots[s].flags & kSlotIonAtt)) ? &slots[s].pop : nullptr;
+  }
+};
+
+__device__ __forceinline__ int pop_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int pop_stride() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ int pop_sec_total(const PopArgs& a) { return min(*a.sec_count, a.sec_cap); }
+__device__ __forceinline__ bool claimed(const unsigned int* claim, int i) { return (claim[i >> 5] >> (i & 31)) & 1u; }
+
+template <class Src>
+__global__ void __launch_bounds__(kPopThreads) k_pop_list(Src src) {
+  const PopArgs* ap = src.get(blockIdx.y);
+  if (!ap) return;
+  const PopArgs& a = *ap;
+  const int n = pop_sec_total(a);
+  for (int j = pop_tid(); j < n; j += pop_stride())
+    if (a.sec[2 * j + 1].w == 0.0f) a.alive[append_slot(&a.counts[0])] = j;
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kPopThreads) k_pop_fill(Src src) {
+  const PopArgs* ap = src.get(blockIdx.y);
+  if (!ap) return;
+  const PopArgs& a = *ap;
+  const int n_att = *a.att_count, n_sec = a.counts[0];
   const int k = min(n_att, n_sec);
-  for (int j = tid; j < k; j += nt) {
+  for (int j = pop_tid(); j < k; j += pop_stride()) {
     const int slot = a.att_list[j];
     const int sidx = a.alive[n_sec - 1 - j];
     a.state[2 * slot] = a.sec[2 * sidx];
     a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
-  __syncthreads();
-  // (2) the slots still attached are marked first, so that no clone is made
-  // from another clone
-  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
+  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
     const int dest = a.att_list[n_sec + jj];
     atomicOr(&a.claim[dest >> 5], 1u << (dest & 31));
   }
-  __syncthreads();
-  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
+  const PopArgs* ap = src.get(blockIdx.y);
+  if (!ap) return;
+  const PopArgs& a = *ap;
+  const int n_att = *a.att_count, n_sec = a.counts[0];
+  const uint64_t interval = a.ctl->interval;
+  const float hme = a.half_me_over_e;
+  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
     const int j = n_sec + jj;
     const int dest = a.att_list[j];
-    int src = -1;
+    int src_slot = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
       const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
-      if (!(a.claim[r >> 5] & (1u << (r & 31))) && a.state[2 * r + 1].w == 0.0f) {
-        src = r;
+      if (!claimed(a.claim, r) && a.state[2 * r + 1].w == 0.0f) {
+        src_slot = r;
         break;
       }
     }
-    if (src < 0) {
+    if (src_slot < 0) {
       atomicExch(a.error_flag, 4);
       continue;
     }
-    const float4 A = a.state[2 * src], B = a.state[2 * src + 1];
+    const float4 A = a.state[2 * src_slot], B = a.state[2 * src_slot + 1];
     a.state[2 * dest] = A;
     a.state[2 * dest + 1] = B;
     add_growth(a.growth, (double)energy4(B, hme));
   }
-  __syncthreads();
-  for (int jj = tid; jj < n_att - n_sec; jj += nt) {
-    const int dest = a.att_list[n_sec + jj];
-    atomicAnd(&a.claim[dest >> 5], ~(1u << (dest & 31)));
-  }
-  __syncthreads();
-  // (3)
   const int m = n_sec - n_att;
   const int pool = a.n_electrons + m;
-  for (int j = tid; j < m; j += nt) {
+  for (int j = pop_tid(); j < m; j += pop_stride()) {
     int got = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
       const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 2u, d), pool);
@@ -875,35 +1021,59 @@ __device__ __forceinline__ void pop_body(const PopArgs& a, int* s_n) {
     a.removed[j] = got;
     if (got < 0) atomicExch(a.error_flag, 5);
   }
-  __syncthreads();
-  for (int j = tid; j < m; j += nt) {
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kPopThreads) k_pop_sort(Src src) {
+  const PopArgs* ap = src.get(blockIdx.y);
+  if (!ap) return;
+  const PopArgs& a = *ap;
+  const int n_att = *a.att_count, n_sec = a.counts[0];
+  const float hme = a.half_me_over_e;
+  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
+    const int dest = a.att_list[n_sec + jj];
+    atomicAnd(&a.claim[dest >> 5], ~(1u << (dest & 31)));
+  }
+  const int m = n_sec - n_att;
+  for (int j = pop_tid(); j < m; j += pop_stride()) {
     const int r = a.removed[j];
     if (r >= 0 && r < a.n_electrons) {
-      a.pair_slot[atomicAdd(&s_n[1], 1)] = r;
+      a.pair_slot[append_slot(&a.counts[1])] = r;
       add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], hme));
     } else if (r >= a.n_electrons) {
       add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], hme));
     }
-    const int b = a.n_electrons + j;
-    if (!(a.claim[b >> 5] & (1u << (b & 31)))) a.pair_sec[atomicAdd(&s_n[2], 1)] = a.alive[j];
+    if (!claimed(a.claim, a.n_electrons + j)) a.pair_sec[append_slot(&a.counts[2])] = a.alive[j];
   }
-  __syncthreads();
-  const int np = min(s_n[1], s_n[2]);
-  for (int q = tid; q < np; q += nt) {
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kPopThreads) k_pop_place(Src src) {
+  const PopArgs* ap = src.get(blockIdx.y);
+  if (!ap) return;
+  const PopArgs& a = *ap;
+  const int n_att = *a.att_count, n_sec = a.counts[0];
+  const int np = min(a.counts[1], a.counts[2]);
+  for (int q = pop_tid(); q < np; q += pop_stride()) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
     a.state[2 * slot] = a.sec[2 * sidx];
     a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
-  for (int j = tid; j < m; j += nt) {
+  const int m = n_sec - n_att;
+  for (int j = pop_tid(); j < m; j += pop_stride()) {
     const int r = a.removed[j];
     if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
   }
 }
 
-__global__ void __launch_bounds__(kPopThreads) k_pop_all(PopArgs a) {
-  __shared__ int s_n[4];  // alive secondaries, removed slots, surviving secondaries
-  pop_body(a, s_n);
+template <class Src>
+void launch_pop_phases(const Src& src, dim3 grid, cudaStream_t s) {
+  k_pop_list<<<grid, kPopThreads, 0, s>>>(src);
+  k_pop_fill<<<grid, kPopThreads, 0, s>>>(src);
+  k_pop_draw<<<grid, kPopThreads, 0, s>>>(src);
+  k_pop_sort<<<grid, kPopThreads, 0, s>>>(src);
+  k_pop_place<<<grid, kPopThreads, 0, s>>>(src);
 }
 
 // ---------------------------------------------------------- batch helpers
@@ -926,6 +1096,7 @@ __global__ void k_batch_prep(BatchArgs b) {
     sc->error_flag = 0;
     sc->max_energy_bits = 0u;
     sc->work_counter = 0;
+    sc->pop_counts[0] = sc->pop_counts[1] = sc->pop_counts[2] = 0;
   }
   if (sl.flags & kSlotSample) {
     if (lane < kMoments) sc->moments[lane] = 0.0;
@@ -934,15 +1105,25 @@ __global__ void k_batch_prep(BatchArgs b) {
 }
 
 // distribution tallies of the slots that sample them this interval
-__global__ void __launch_bounds__(kHistThreads) k_hist_batch(BatchArgs b) {
-  __shared__ unsigned int s_h[kMaxEedfCells];
+__global__ void __launch_bounds__(kHistAThreads) k_hist_a_batch(BatchArgs b) {
+  extern __shared__ unsigned int sm_hist[];
   const int n_slots = b.hdr->n_slots, total = b.hdr->hist_chunks;
   for (int c = blockIdx.x; c < total; c += gridDim.x) {
     const int slot = slot_of_chunk(b.hist_prefix, n_slots, c);
     const HistArgs& a = b.slots[slot].hist;
-    const int first = (c - b.hist_prefix[slot]) * kBatchHistChunk;
-    hist_range(a, first + threadIdx.x, min(first + kBatchHistChunk, a.n), blockDim.x, s_h);
-    __syncthreads();
+    const int first = (c - b.hist_prefix[slot]) * kHistChunk;
+    hist_chunk_a(a, first, min(first + kHistChunk, a.n), sm_hist, kHistASmem / 4);
+  }
+}
+
+__global__ void __launch_bounds__(kHistBThreads) k_hist_b_batch(BatchArgs b) {
+  extern __shared__ unsigned int sm_hist[];
+  const int n_slots = b.hdr->n_slots, total = b.hdr->hist2_chunks;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    const int slot = slot_of_chunk(b.hist2_prefix, n_slots, c);
+    const HistArgs& a = b.slots[slot].hist;
+    const int first = (c - b.hist2_prefix[slot]) * kHistChunk;
+    hist_chunk_b(a, first, min(first + kHistChunk, a.n), sm_hist, kHistBSmem / 4);
   }
 }
 
@@ -957,14 +1138,6 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample_batch(BatchArgs b) {
     sample_range(a, first + threadIdx.x, min(first + kBatchSampleChunk, a.n), blockDim.x, s_m);
     __syncthreads();
   }
-}
-
-// population control: one block per slot that ionizes or attaches
-__global__ void __launch_bounds__(kPopThreads) k_pop_batch(BatchArgs b) {
-  __shared__ int s_n[4];
-  const int slot = blockIdx.x;
-  if (slot >= b.hdr->n_slots || !(b.slots[slot].flags & kSlotIonAtt)) return;
-  pop_body(b.slots[slot].pop, s_n);
 }
 
 // every slot's scalars into one contiguous array for a single read-back
@@ -1068,21 +1241,37 @@ void launch_sample(const SampleArgs& a, cudaStream_t s) {
 
 void launch_hist(const HistArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
-  const int grid = min(blocks_for(a.n, kHistThreads), 152 * 2);
-  k_hist<<<grid, kHistThreads, 0, s>>>(a);
+  const int chunks = (a.n + kHistChunk - 1) / kHistChunk;
+  k_hist_a<<<chunks, kHistAThreads, kHistASmem, s>>>(a);
+  if (a.cylindrical) k_hist_b<<<chunks, kHistBThreads, kHistBSmem, s>>>(a);
 }
 
-void launch_pop_control(const PopArgs& a, cudaStream_t s) { k_pop_all<<<1, kPopThreads, 0, s>>>(a); }
+void launch_pop_control(const PopArgs& a, cudaStream_t s) {
+  PopOne one;
+  one.a = a;
+  launch_pop_phases(one, dim3(kPopBlocks, 1), s);
+}
+
+cudaError_t prepare_kernels() {
+  cudaError_t e = cudaFuncSetAttribute(k_hist_a, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistASmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_b, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistBSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_hist_a_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistASmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_hist_b_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistBSmem);
+  return e;
+}
 
 size_t batch_prefix_offset() { return (sizeof(BatchHeader) + 15) / 16 * 16; }
 size_t batch_slots_offset() {
-  return (batch_prefix_offset() + 3 * (kBatchMaxSlots + 1) * sizeof(int) + 255) / 256 * 256;
+  return (batch_prefix_offset() + 4 * (kBatchMaxSlots + 1) * sizeof(int) + 255) / 256 * 256;
 }
 
 void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
   const int slots = max(1, min(max_slots, kBatchMaxSlots));
   k_batch_prep<<<(slots + 7) / 8, 256, 0, s>>>(b);
-  k_hist_batch<<<sm_count * 2, kHistThreads, 0, s>>>(b);
+  k_hist_a_batch<<<sm_count, kHistAThreads, kHistASmem, s>>>(b);
+  k_hist_b_batch<<<sm_count * 2, kHistBThreads, kHistBSmem, s>>>(b);
 }
 
 void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s) {
@@ -1097,7 +1286,10 @@ void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s) {
 void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
   const int slots = max(1, min(max_slots, kBatchMaxSlots));
   k_advance_drain_batch<<<slots, 32, 0, s>>>(b);
-  k_pop_batch<<<slots, kPopThreads, 0, s>>>(b);
+  PopBatch pb;
+  pb.hdr = b.hdr;
+  pb.slots = b.slots;
+  launch_pop_phases(pb, dim3(kPopBlocksPerSlot, slots), s);
   k_sample_batch<<<sm_count * 4, kSampleThreads, 0, s>>>(b);
   k_batch_gather<<<min(slots, 64), 64, 0, s>>>(b);
 }

@@ -19,6 +19,8 @@ struct DevScalars {
   int sec_count, att_count, spill_count, error_flag;
   unsigned int max_energy_bits;
   int work_counter;
+  int pop_counts[3];    // population control: alive secondaries, removed slots, surviving secondaries
+  int pad1;
   unsigned long long null_count;
   unsigned long long real_count;
   double field_gain;
@@ -76,6 +78,10 @@ struct AdvanceArgs {
 };
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);
+
+// Per-process kernel attributes (dynamic shared memory of the histogram
+// kernels); called on the current device before any launch or capture.
+cudaError_t prepare_kernels();
 
 struct InitArgs {
   float4* state;
@@ -144,7 +150,9 @@ struct PopArgs {
   float4* state;
   int n_electrons;
   const float4* sec;               // advanced secondaries (x, y, z, s), (vx, vy, vz, dead flag)
-  const int* sec_count;
+  const int* sec_count;            // may exceed sec_cap after an overflow (reported by the host)
+  int sec_cap;
+  int* counts;                     // [3] zero on entry: alive secondaries, removed slots, surviving secondaries
   const int* att_list;
   const int* att_count;
   unsigned int* claim;             // bitmap over n_electrons + sec_cap, all zero on entry and on exit
@@ -158,7 +166,10 @@ struct PopArgs {
   const IntervalCtl* ctl;
   int* error_flag;                 // set when a bounded retry loop gives up
 };
+// Five launches (compaction, filling of attached slots, clones or removal
+// draws, listing, pairing), each spread over many blocks.
 void launch_pop_control(const PopArgs& a, cudaStream_t s);
+constexpr int kPopLaunches = 5;
 
 // ------------------------------------------------------------------ batches
 // Many swarm conditions (slots) advanced by one launch sequence per interval.
@@ -188,22 +199,24 @@ struct BatchHeader {
   int adv_chunks, smp_chunks, hist_chunks;  // totals (last prefix entries)
   int mode_chunk[kFieldModes + 1];          // first advance chunk of each mode's slots
   int chunk_counter[kFieldModes];           // advance work counters, zeroed by prep
-  int pad;
+  int hist2_chunks;                         // velocity-distribution chunks (cylindrical slots)
 };
 
 constexpr int kBatchMaxSlots = 1024;
 constexpr int kBatchAdvanceChunk = 4096;   // electrons per block-chunk of the advance
 constexpr int kBatchSampleChunk = 4096;    // electrons per block of the moment sums
-constexpr int kBatchHistChunk = 16384;     // electrons per block of the histograms
+constexpr int kBatchHistChunk = 32768;     // electrons per block of the histograms
 
 // Staging layout (host pinned mirror and device copy are identical):
-//   BatchHeader | adv_prefix | smp_prefix | hist_prefix (kBatchMaxSlots+1 ints each, padded) | BatchSlot[...]
+//   BatchHeader | adv_prefix | smp_prefix | hist_prefix | hist2_prefix (kBatchMaxSlots+1 ints
+//   each, padded) | BatchSlot[...]
 struct BatchArgs {
   BatchHeader* hdr;
   const BatchSlot* slots;
   const int* adv_prefix;
   const int* smp_prefix;
-  const int* hist_prefix;
+  const int* hist_prefix;   // energy and energy-angle distributions
+  const int* hist2_prefix;  // velocity distribution (cylindrical slots)
   DevScalars* gather;       // [kBatchMaxSlots]: each slot's scalars after the interval
 };
 size_t batch_prefix_offset();   // bytes from the staging start to adv_prefix
@@ -215,7 +228,7 @@ size_t batch_slots_offset();    // bytes from the staging start to slots[0]
 void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
 void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s);
 void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
-constexpr int kBatchLaunches = 11;  // kernels per batched interval
+constexpr int kBatchLaunches = 16;  // kernels per batched interval
 
 // Replay kernels for the parity tests: the production device functions
 // driven by given inputs and recorded uniforms.

@@ -41,6 +41,7 @@ struct JobRec {
   double t_submit = 0, t_start = 0, t_end = 0, footprint = 0;
   bool cancel = false;
   bool holds = false;  // its footprint counts against the budget
+  std::string error;
   lgpu_result result{};
   std::vector<unsigned long long> counts;
   std::vector<double> rate;
@@ -137,6 +138,7 @@ class Server {
     st->end_time = r.t_end;
     st->footprint_bytes = r.footprint;
     st->result = r.result;
+    std::snprintf(st->error, sizeof(st->error), "%s", r.error.c_str());
   }
 
   static bool final_state(int s) { return s == LGPU_JOB_DONE || s == LGPU_JOB_FAILED || s == LGPU_JOB_CANCELLED; }
@@ -279,6 +281,7 @@ class Server {
           if (held_ + r->footprint > budget_) {
             if (running_.empty() && admit.empty()) {  // can never fit
               queue_.pop_front();
+              r->error = "device footprint above the server's memory budget";
               retire(r, LGPU_JOB_FAILED, LGPU_ERR_OOM);
               continue;
             }
@@ -297,8 +300,10 @@ class Server {
       for (JobRec* r : admit) {
         const int rc = create(r);
         if (rc != LGPU_OK) {
+          const std::string msg = r->engine ? r->engine->err_ : std::string("out of host memory");
           destroy_engine(r);
           std::lock_guard<std::mutex> lock(mu_);
+          r->error = msg.empty() ? batch_.err_ : msg;
           retire(r, LGPU_JOB_FAILED, rc);
         } else {
           running_.push_back(r);
@@ -357,8 +362,10 @@ class Server {
           status = r->engine->process_results(counts.data(), rate.data(), nullptr, nullptr, P);
         }
         const lgpu_result res = m.result;
+        const std::string msg = status == LGPU_OK ? std::string() : r->engine->err_;
         destroy_engine(r);
         std::lock_guard<std::mutex> lock(mu_);
+        r->error = msg;
         r->result = res;
         r->counts = std::move(counts);
         r->rate = std::move(rate);

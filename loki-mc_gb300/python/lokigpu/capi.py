@@ -30,6 +30,7 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
             "lgpu_replay_flights_noalloc",
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
+            "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
             "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_report_get", "lgpu_server_last_error",
             "lgpu_server_stop")
@@ -91,7 +92,7 @@ class Timing(ctypes.Structure):
 class BatchReport(ctypes.Structure):
     _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
-                ("d2h_bytes", D)]
+                ("d2h_bytes", D), ("host_ms", D), ("secondaries", D), ("spilled", D), ("attached", D)]
 
 
 class Job(ctypes.Structure):
@@ -101,7 +102,7 @@ class Job(ctypes.Structure):
 
 class JobStatus(ctypes.Structure):
     _fields_ = [("state", I), ("status", I), ("submit_time", D), ("start_time", D), ("end_time", D),
-                ("footprint_bytes", D), ("result", Result)]
+                ("footprint_bytes", D), ("result", Result), ("error", ctypes.c_char * 256)]
 
 
 class ServerReport(ctypes.Structure):
@@ -155,6 +156,10 @@ def load(path: str | None = None):
     lib.lgpu_batch_last_error.argtypes = [VP, ctypes.c_char_p, ctypes.c_size_t]
     lib.lgpu_batch_add.argtypes = [VP, VP]
     lib.lgpu_batch_run.argtypes = [VP, P_(Result), P_(I), I, P_(BatchReport)]
+    lib.lgpu_batch_start.argtypes = [VP]
+    lib.lgpu_batch_step.argtypes = [VP, I, P_(I), P_(BatchReport)]
+    lib.lgpu_batch_stream.argtypes = [VP]
+    lib.lgpu_batch_stream.restype = VP
     lib.lgpu_server_start.argtypes = [I, I, D, P_(VP)]
     lib.lgpu_server_submit.argtypes = [VP, P_(Job), P_(LL)]
     lib.lgpu_server_poll.argtypes = [VP, LL, P_(JobStatus)]
@@ -391,6 +396,23 @@ class Batch:
         if rc != LGPU_OK:
             raise LokiGpuError(rc, self.last_error())
         self.ctxs.append(ctx)
+
+    def start(self):
+        rc = self.lib.lgpu_batch_start(self.h)
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+
+    def step(self, n=1):
+        """n batched intervals: (contexts still running, BatchReport of the call)."""
+        running = I()
+        rep = BatchReport()
+        rc = self.lib.lgpu_batch_step(self.h, int(n), ctypes.byref(running), ctypes.byref(rep))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
+        return running.value, rep
+
+    def stream(self) -> int:
+        return self.lib.lgpu_batch_stream(self.h)
 
     def run(self):
         """Solves every added context: (results, status codes, BatchReport)."""

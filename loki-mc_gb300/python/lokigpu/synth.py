@@ -125,11 +125,13 @@ def _boltzmann(energies: Sequence[float], weights: Sequence[float], tg: float) -
 def molecular_gas(name: str, seed: int, *, mass_amu: float, n_vib: int, vib_lo: float, vib_hi: float,
                   n_ele: int, ele_lo: float, ele_hi: float, ion_thr: Optional[float],
                   rot_thr: Optional[float], att: Optional[tuple], n_points: int = 200,
-                  screen: bool = True, tg: float = 300.0, fraction: float = 1.0) -> Gas:
+                  screen: bool = True, tg: float = 300.0, fraction: float = 1.0, e_max: float = 1e3) -> Gas:
     """Seeded molecule with elastic, rotational/vibrational ``<->`` levels,
-    electronic levels, optional ionization and attachment."""
+    electronic levels, optional ionization and attachment; cross sections on
+    ``n_points`` log points over 1e-3..``e_max`` eV (the same seeded shapes for
+    any ``e_max``)."""
     rng = np.random.default_rng(seed)
-    e = log_grid(n_points)
+    e = log_grid(n_points, 1e-3, e_max)
     cols: List[Collision] = []
     states: Dict[str, State] = {f"{name}(X)": State(1.0, 1.0, 0.0)}
     ground = f"{name}(X)"
@@ -188,17 +190,17 @@ def molecular_gas(name: str, seed: int, *, mass_amu: float, n_vib: int, vib_lo: 
     return Gas(name, mass_amu * C.UNIFIED_ATOMIC_MASS, fraction, cols, states)
 
 
-def n2_like_gas(seed: int = 2, name: str = "X2", fraction: float = 1.0) -> Gas:
+def n2_like_gas(seed: int = 2, name: str = "X2", fraction: float = 1.0, e_max: float = 1e3) -> Gas:
     return molecular_gas(name, seed, mass_amu=28.0, n_vib=8, vib_lo=0.29, vib_hi=2.3, n_ele=20,
                          ele_lo=6.0, ele_hi=15.0, ion_thr=15.6, rot_thr=0.0012, att=None,
-                         fraction=fraction)
+                         fraction=fraction, e_max=e_max)
 
 
-def o2_like_gas(seed: int = 3, name: str = "Y2", fraction: float = 1.0) -> Gas:
+def o2_like_gas(seed: int = 3, name: str = "Y2", fraction: float = 1.0, e_max: float = 1e3) -> Gas:
     # 1 elastic + 1 rot (<->: 2) + 4 vib (<->: 8) + 1 attachment + 12 electronic + 1 ionization = 25
     return molecular_gas(name, seed, mass_amu=32.0, n_vib=4, vib_lo=0.19, vib_hi=0.75, n_ele=12,
                          ele_lo=0.98, ele_hi=14.0, ion_thr=12.07, rot_thr=0.0018,
-                         att=(4.4, 1.4e-22), fraction=fraction)
+                         att=(4.4, 1.4e-22), fraction=fraction, e_max=e_max)
 
 
 def random_gas(seed: int, name: str, fraction: float) -> Gas:

@@ -248,7 +248,9 @@ STAT_CASES = {
     "atomic_dc100": ("atomic", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "1E3"}),
     "n2_dc200": ("n2", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
     "mix_dc100": ("mix", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
-    "mix_ac150": ("mix", {"red_field": 150.0, "freq": 3.22e22 * 1e-16 / (2 * np.pi)},
+    # omega/N = 1e-14 m^3/s: a 20 ns field period, so the 3000 integration
+    # intervals (~0.1 ns each) average over some 15 periods
+    "mix_ac150": ("mix", {"red_field": 150.0, "freq": 3.22e22 * 1e-14 / (2 * np.pi)},
                   {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300", "nIntegrationPhases": "64"}),
     "mix_b100": ("mix", {"red_field": 100.0, "red_mag": 1000.0, "angle": 90.0},
                  {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
