@@ -60,6 +60,11 @@ N_ELECTRONS = 1_000_000
 # 73.6 MB written; traffic grows in proportion to the electrons advanced
 DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
 
+# DRAM bytes per electron and interval of the batched advance (DC launch), from
+# one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 739.2 MB
+# read + 584.3 MB written for 1.98e7 electrons
+SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (739.159040e6 + 584.292352e6) / 19795598
+
 # sweep workload
 SWEEP_POINTS = 64
 SWEEP_SEED = 2024
@@ -283,6 +288,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
     total_ms = real = null = adv_ms = steps = 0.0
     launches = intervals = 0
     h2d = d2h = host_ms = secondaries = spilled = 0.0
+    real_batch = 0
     for _ in range(args.steps):
         flush.add_(1.0)                    # L2 flush (256 MiB written), outside the timed region
         torch.cuda.synchronize()
@@ -305,11 +311,13 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         secondaries += rep.secondaries
         spilled += rep.spilled
         assert running == len(conds)
+        real_batch = rep.real_batch
     del b
     for c in ctxs:
         c.close()
     return dict(total_ms=total_ms, real=real, null=null, adv_ms=adv_ms, electron_steps=steps, launches=launches,
-                intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled)
+                intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled,
+                real_batch=real_batch)
 
 
 def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
@@ -526,12 +534,13 @@ def run_gpu_sweep(args):
                        "null_collisions_per_s": null / (total_ms * 1e-3),
                        "host_ms_per_step": tb["host_ms"] / args.steps,
                        "secondaries_per_step": tb["secondaries"] / args.steps,
-                       "spilled_per_step": tb["spilled"] / args.steps},
+                       "spilled_per_step": tb["spilled"] / args.steps,
+                       "collision_turn_threshold": tb["real_batch"]},
             "plain": plain, "batched_over_plain": ratio or None, "served": served,
             "accuracy": _accuracy(conds, e2e_b, e2e_p) if (e2e_b and e2e_p) else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "traffic_source": "no ncu capture of the batched advance yet",
+                         "frac": achieved / peak, "traffic": SWEEP_DRAM_BYTES_PER_ELECTRON_STEP * electrons,
+                         "traffic_source": "ncu dram__bytes_read+write of the batched DC advance, one sweep interval",
                          "kernel": "k_advance_batch", "peak_source": peak_kind,
                          "algorithmic_bytes": f"{STATE_BYTES_PER_ELECTRON_STEP} B per electron-interval",
                          "kernel_ms_per_interval": tb["adv_ms"] / max(tb["intervals"], 1)},

@@ -63,6 +63,9 @@ typedef struct lgpu_config {
   int sync_oversampling;            /* synchronizationOverSampling */
   double max_seconds;               /* wall-clock cap of one solve (<= 0: none) */
   long long max_sync_steps;         /* interval cap of one solve (<= 0: none) */
+  int advance_real_batch;           /* lanes of a warp with a pending real collision that start its
+                                       collision turn (1..32); 0: 20 alone, tuned on line in a batch.
+                                       Scheduling only: no result depends on it */
 } lgpu_config;
 
 /* Fills the reference's defaults (BoltzmannMC.h:50-76). */
@@ -282,6 +285,7 @@ typedef struct lgpu_batch_report {
   double secondaries;           /* ionization secondaries created */
   double spilled;               /* of those, the ones a warp queue could not hold */
   double attached;              /* electrons removed by attachment */
+  double real_batch;            /* collision-turn threshold in use (0 while it is being tuned) */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);

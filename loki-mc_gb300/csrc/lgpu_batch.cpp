@@ -74,6 +74,7 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
+    report->real_batch = b.tuned_;
   }
   return rc;
 }
@@ -118,6 +119,7 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
+    report->real_batch = b.tuned_;
   }
   b.members_.clear();
   b.active_.clear();

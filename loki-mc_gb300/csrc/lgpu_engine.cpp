@@ -33,6 +33,7 @@ void lgpu_config_default(lgpu_config* c) {
   c->sync_oversampling = 1;            // BoltzmannMC.h:73
   c->max_seconds = 0;
   c->max_sync_steps = 0;
+  c->advance_real_batch = 0;
 }
 
 #define CTX_CHECK(ctx)                          \

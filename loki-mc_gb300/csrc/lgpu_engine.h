@@ -107,6 +107,8 @@ class Engine {
     if (cfg_.n_interp < 2 || cfg_.n_interp > (1 << 24)) return fail(LGPU_ERR_BAD_ARG, "nInterpPoints out of range");
     if (cfg_.n_energy_cells < 1 || cfg_.n_energy_cells > 4096) return fail(LGPU_ERR_BAD_ARG, "nEnergyCells must be 1..4096");
     if (cfg_.sync_oversampling < 1) return fail(LGPU_ERR_BAD_ARG, "synchronizationOverSampling must be >= 1");
+    if (cfg_.advance_real_batch < 0 || cfg_.advance_real_batch > 32)
+      return fail(LGPU_ERR_BAD_ARG, "advance_real_batch must be 0..32");
     LGPU_CU(cudaSetDevice(cfg_.device));
     LGPU_CU(prepare_kernels());
     LGPU_CU(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, cfg_.device));
@@ -558,6 +560,7 @@ class Engine {
     a.work_counter = &d_sc_->work_counter;
     a.sm_count = sm_count_;
     a.ctl = d_ctl_;
+    a.real_batch = cfg_.advance_real_batch > 0 ? std::min(cfg_.advance_real_batch, 32) : kDefaultRealBatch;
     return a;
   }
 

@@ -339,16 +339,13 @@ __device__ __forceinline__ void lane_real(const AdvanceArgs& a, AdvShared& sh, i
   if (finished) lane_finish(a, L, tl, dead);
 }
 
-// Lanes with a pending collision that start the warp's collision turn.
-constexpr int kRealBatch = 20;
-
-// One turn of a warp: the collision turn when kRealBatch lanes (or every lane
-// with an electron) have a pending collision, else the flight turn.
+// One turn of a warp: the collision turn when a.real_batch lanes (or every
+// lane with an electron) have a pending collision, else the flight turn.
 template <int MODE>
 __device__ __forceinline__ void warp_turn(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
                                           Lane& L, LaneTally& tl, unsigned live) {
   const unsigned pend = __ballot_sync(0xffffffffu, L.pending);
-  if (__popc(pend) >= kRealBatch || pend == live) {
+  if (__popc(pend) >= a.real_batch || pend == live) {
     if (L.pending) lane_real(a, sh, wid, iv, L, tl);
   } else if (L.have && !L.pending) {
     lane_flight<MODE>(a, iv, L, tl);

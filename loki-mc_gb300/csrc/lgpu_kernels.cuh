@@ -75,7 +75,9 @@ struct AdvanceArgs {
   int sm_count;
   const IntervalCtl* ctl;          // when set: per-interval values are read from here
   int queue_only;                  // 1: only drain the spilled secondaries (one warp)
+  int real_batch;                  // pending real collisions that start a warp's collision turn (1..32)
 };
+constexpr int kDefaultRealBatch = 20;
 
 void launch_advance(const AdvanceArgs& a, cudaStream_t s);
 

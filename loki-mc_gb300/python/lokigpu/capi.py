@@ -51,7 +51,7 @@ class Config(ctypes.Structure):
                 ("errors_checked", I), ("req_err_mean_energy", D), ("req_err_flux_v", D), ("req_err_flux_d", D),
                 ("req_err_bulk_v", D), ("req_err_bulk_d", D), ("req_err_power", D), ("n_energy_cells", I),
                 ("n_cos_cells", I), ("n_radial_cells", I), ("n_axial_cells", I), ("n_phases", I), ("sync_x", D),
-                ("sync_oversampling", I), ("max_seconds", D), ("max_sync_steps", LL)]
+                ("sync_oversampling", I), ("max_seconds", D), ("max_sync_steps", LL), ("advance_real_batch", I)]
 
 
 class Process(ctypes.Structure):
@@ -92,7 +92,8 @@ class Timing(ctypes.Structure):
 class BatchReport(ctypes.Structure):
     _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
-                ("d2h_bytes", D), ("host_ms", D), ("secondaries", D), ("spilled", D), ("attached", D)]
+                ("d2h_bytes", D), ("host_ms", D), ("secondaries", D), ("spilled", D), ("attached", D),
+                ("real_batch", D)]
 
 
 class Job(ctypes.Structure):
