@@ -273,6 +273,7 @@ class Batch {
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];
+      hdr->mode_slot[m] = s;
     }
     cudaGraphExec_t ge;
     int rc;

@@ -392,33 +392,31 @@ __device__ __forceinline__ void block_flush(const AdvanceArgs& a, AdvShared& sh,
   }
 }
 
-// One condition: the ensemble in warp chunks from the global work counter
-// (or, drain, only the spilled secondaries).
+// The warps' work on one condition: the ensemble in 128-electron warp chunks
+// from the condition's work counter, then each warp's queued secondaries (or,
+// drain, only the spilled secondaries). Returns when the condition's counter
+// and the warp's queue are exhausted; the caller flushes the lane sums.
 template <int MODE>
-__device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh) {
-  load_block_consts(a, sh);
-  __syncthreads();
-  const IntervalView iv = interval_view<MODE>(a);
+__device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, const IntervalView& iv,
+                                          LaneTally& tl, uint32_t& sec_id, uint32_t id_hi, uint32_t id_mask) {
   const bool drain = a.queue_only != 0;
   const int n_el = drain ? 0 : a.n;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
-  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 12);
-
-  LaneTally tl;
-  reset_tally(tl);
   Lane L;
   reset_lane(L);
   // warp-uniform cursors: ensemble chunk, spill buffer (drain only)
   int next = 0, end = 0, sp_next = 0;
   bool exhausted = drain;
-  uint32_t sec_id = 0;
 
   for (;;) {
     __syncwarp();
     if (drain) __threadfence();
-    // ---- refill lanes without an electron: the warp's ensemble chunk first,
-    // then the warp's own secondaries, then (drain) the spilled ones
+    // ---- refill lanes without an electron: the warp's own queued secondaries
+    // first (the queue stays short, so it rarely spills), then the ensemble
+    // chunk, then (drain) the spilled secondaries
+    int qn = min(sh.qn[wid], kLocalQ);
+    if (qn > 0) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, id_mask);
     const unsigned need = __ballot_sync(0xffffffffu, !L.have);
     if (need && !exhausted) {
       const int n_need = __popc(need);
@@ -444,9 +442,7 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh
       }
       if (idx >= 0) lane_take_electron(a, iv, L, idx);
     }
-    int qn = min(sh.qn[wid], kLocalQ);
     if (exhausted) {
-      qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, 0xFFFu);
       if (drain) {
         const unsigned idle2 = __ballot_sync(0xffffffffu, !L.have);
         const int cnt = min(*(volatile int*)a.spill_count, a.spill_cap);
@@ -468,6 +464,20 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh
     }
     warp_turn<MODE>(a, sh, wid, iv, L, tl, live);
   }
+}
+
+// One condition per launch (or, drain, its spilled secondaries).
+template <int MODE>
+__device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh) {
+  load_block_consts(a, sh);
+  __syncthreads();
+  const IntervalView iv = interval_view<MODE>(a);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 12);
+  LaneTally tl;
+  reset_tally(tl);
+  uint32_t sec_id = 0;
+  warp_loop<MODE>(a, sh, iv, tl, sec_id, id_hi, 0xFFFu);
   block_flush(a, sh, tl, lane, wid);
 }
 
@@ -503,95 +513,60 @@ __device__ __forceinline__ void load_slot_args(const AdvanceArgs* src, AdvanceAr
   for (int k = threadIdx.x; k < (int)(sizeof(AdvanceArgs) / sizeof(int)); k += blockDim.x) d[k] = s[k];
 }
 
-// One block-chunk [first, first + cnt) of a slot: the warps take electrons
-// from the block counter *next, then push their queued secondaries. The field
-// branch is a template parameter so each instantiation keeps only its own
-// flight code live.
-template <int MODE>
-__device__ __forceinline__ void batch_chunk(const AdvanceArgs& a, AdvShared& sh, const IntervalView& iv,
-                                            LaneTally& tl, int first, int cnt, int* next, uint32_t& sec_id,
-                                            uint32_t id_hi) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned lt_mask = (1u << lane) - 1u;
-  Lane L;
-  reset_lane(L);
-  bool exhausted = false;
-  for (;;) {
-    __syncwarp();
-    const unsigned need = __ballot_sync(0xffffffffu, !L.have);
-    if (need && !exhausted) {
-      const int n_need = __popc(need);
-      int base = 0;
-      if (lane == 0) base = atomicAdd(next, n_need);
-      base = __shfl_sync(0xffffffffu, base, 0);
-      const int take = min(n_need, cnt - base);
-      if (base + n_need >= cnt) exhausted = true;
-      const int r = __popc(need & lt_mask);
-      if (!L.have && r < take) lane_take_electron(a, iv, L, first + base + r);
-    }
-    int qn = min(sh.qn[wid], kLocalQ);
-    if (exhausted) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, 0x3FFFFu);
-    const unsigned live = __ballot_sync(0xffffffffu, L.have);
-    if (!live) {
-      if (exhausted && qn == 0) break;
-      continue;
-    }
-    warp_turn<MODE>(a, sh, wid, iv, L, tl, live);
-  }
-}
-
-// Many conditions in one persistent grid. A block takes chunks of
-// kBatchAdvanceChunk electrons of one slot at a time from the batch counter,
-// its warps take the chunk's electrons from a block counter, and the warps'
-// queued secondaries are pushed before the block moves on, so that every
-// chunk ends with empty queues. The slot's constants and per-process tallies
-// stay in shared memory while the block's chunks belong to the same slot and
-// are flushed to that slot's tallies when it changes. One launch per field
-// branch, over the chunks of the slots with that branch.
+// Many conditions of one field branch in one persistent grid. A block works
+// on one condition (slot) at a time: its warps take 128-electron chunks from
+// that slot's own work counter, as in the single-condition kernel, and the
+// slot's constants and per-process tallies stay in the block's shared memory.
+// Blocks start spread over the branch's slots in proportion to their
+// electrons; a block whose slot runs dry flushes its tallies and moves to the
+// next slot of the branch that still has electrons, so the block synchronises
+// only when it changes slot and idle blocks help finish large slots.
 template <int MODE>
 __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance_batch(BatchArgs b) {
   __shared__ AdvShared sh;
   __shared__ AdvanceArgs s_a;
   __shared__ IntervalView s_iv;
-  __shared__ int s_chunk, s_slot, s_next;
+  __shared__ int s_slot;
+  const int s0 = b.hdr->mode_slot[MODE], s1 = b.hdr->mode_slot[MODE + 1];
+  if (s0 >= s1) return;  // no slot with this field branch (uniform over the grid)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // secondary ids: 13 bits of warp index (< 8192 warps), 18 bits of count
   const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 18);
   const int n_slots = b.hdr->n_slots;
-  const int c0 = b.hdr->mode_chunk[MODE], c1 = b.hdr->mode_chunk[MODE + 1];
-  int cur = -1;
+  if (threadIdx.x == 0) {
+    const int c0 = b.hdr->mode_chunk[MODE], c1 = b.hdr->mode_chunk[MODE + 1];
+    const int c = c0 + (int)(((long long)blockIdx.x * (c1 - c0)) / gridDim.x);
+    s_slot = slot_of_chunk(b.adv_prefix, n_slots, min(c, c1 - 1));
+  }
+  __syncthreads();
   LaneTally tl;
-  reset_tally(tl);
   uint32_t sec_id = 0;
   for (;;) {
+    const int slot = s_slot;
+    if (slot < 0) break;
+    load_slot_args(&b.slots[slot].adv, &s_a);
+    __syncthreads();
+    load_block_consts(s_a, sh);
+    if (threadIdx.x == 0) s_iv = interval_view<-1>(s_a);
+    __syncthreads();
+    reset_tally(tl);
+    warp_loop<MODE>(s_a, sh, s_iv, tl, sec_id, id_hi, 0x3FFFFu);
+    __syncthreads();  // every warp is done with the slot
+    block_flush(s_a, sh, tl, lane, wid);
+    __syncthreads();  // the flush has read the shared tallies and arguments
     if (threadIdx.x == 0) {
-      const int c = c0 + atomicAdd(&b.hdr->chunk_counter[MODE], 1);
-      s_chunk = c;
-      s_slot = c < c1 ? slot_of_chunk(b.adv_prefix, n_slots, c) : -1;
-      s_next = 0;
+      int nxt = -1;
+      for (int k = 1; k <= s1 - s0; ++k) {
+        const int s = s0 + (slot - s0 + k) % (s1 - s0);
+        const AdvanceArgs& o = b.slots[s].adv;
+        if (*(volatile int*)o.work_counter < o.n) {
+          nxt = s;
+          break;
+        }
+      }
+      s_slot = nxt;
     }
     __syncthreads();
-    const int slot = s_slot;
-    if (slot != cur || slot < 0) {  // a new slot, or no chunk left (also before the first)
-      if (cur >= 0) block_flush(s_a, sh, tl, lane, wid);
-      reset_tally(tl);
-      __syncthreads();
-      if (slot < 0) break;
-      load_slot_args(&b.slots[slot].adv, &s_a);
-      __syncthreads();
-      load_block_consts(s_a, sh);
-      if (threadIdx.x == 0) s_iv = interval_view<-1>(s_a);
-      __syncthreads();
-      cur = slot;
-    }
-    const int first = (s_chunk - b.adv_prefix[slot]) * kBatchAdvanceChunk;
-    const int cnt = min(kBatchAdvanceChunk, s_a.n - first);
-    if (first >= 0 && cnt > 0) {
-      batch_chunk<MODE>(s_a, sh, s_iv, tl, first, cnt, &s_next, sec_id, id_hi);
-    } else if (threadIdx.x == 0) {
-      atomicExch(s_a.error_flag, 6);  // inconsistent chunk table: the host reports it
-    }
-    __syncthreads();  // every warp is done with the chunk before the counters are reused
   }
 }
 
@@ -779,7 +754,7 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample(SampleArgs a) {
 // A block's chunk is below 2^16 electrons, so no 16-bit count can carry into
 // its neighbour. A condition whose grid is larger than the block's shared
 // memory counts that tally with global atomics instead.
-constexpr int kHistChunk = 32768;
+constexpr int kHistChunk = kBatchHistChunk;  // below 2^16: 16-bit counts cannot carry
 constexpr int kHistAThreads = 1024;
 constexpr int kHistBThreads = 512;
 constexpr int kHistASmem = 224 * 1024;  // one block per SM
@@ -801,12 +776,16 @@ __device__ __forceinline__ void hist_cells(const HistArgs& a, float4 B, int& c, 
   }
 }
 
+// Below this many electrons a chunk counts EADF and EVDF with global atomics:
+// clearing and scanning the whole shared-memory grid would cost more.
+constexpr int kHistSharedMin = 16384;
+
 // pass A over electrons [first, last) of one condition
 __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int last, unsigned int* sm, int sm_words) {
   const int nE = a.n_e_cells;
   const int nA = a.cylindrical ? nE * a.n_cos : 0;
   const int nAw = (nA + 1) >> 1;
-  const bool a_shared = a.cylindrical && nE + nAw <= sm_words;
+  const bool a_shared = a.cylindrical && last - first >= kHistSharedMin && nE + nAw <= sm_words;
   unsigned int* hE = sm;
   unsigned int* hA = sm + nE;
   const int zero_words = nE + (a_shared ? nAw : 0);
@@ -815,11 +794,13 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
   for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
     int c, cy, rx, ry;
     hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
-    if (c >= 0 && c < nE) atomicAdd(&hE[c], 1u);
-    if (a.cylindrical && c < nE && c >= 0 && cy < a.n_cos && cy >= 0) {
-      const int idx = c * a.n_cos + cy;
-      if (a_shared) atomicAdd(&hA[idx >> 1], 1u << ((idx & 1) << 4));
-      else atomicAdd(&a.eadf[idx], 1.0);
+    if (c >= 0 && c < nE) {
+      atomicAdd(&hE[c], 1u);
+      if (a.cylindrical && cy < a.n_cos && cy >= 0) {
+        const int idx = c * a.n_cos + cy;
+        if (a_shared) atomicAdd(&hA[idx >> 1], 1u << ((idx & 1) << 4));
+        else atomicAdd(&a.eadf[idx], 1.0);
+      }
     }
   }
   __syncthreads();
@@ -844,7 +825,7 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
 __device__ __forceinline__ void hist_chunk_b(const HistArgs& a, int first, int last, unsigned int* sm, int sm_words) {
   const int nV = a.n_rad * a.n_ax;
   const int nVw = (nV + 1) >> 1;
-  const bool v_shared = nVw <= sm_words;
+  const bool v_shared = last - first >= kHistSharedMin && nVw <= sm_words;
   if (v_shared)
     for (int w = threadIdx.x; w < nVw; w += blockDim.x) sm[w] = 0u;
   __syncthreads();
@@ -924,7 +905,7 @@ __device__ __forceinline__ float energy4(float4 B, float hme) { return energy_of
 //      cleared, so the bitmap is zero again.
 constexpr int kPopThreads = 256;
 constexpr int kPopBlocks = 64;           // blocks per slot, single condition
-constexpr int kPopBlocksPerSlot = 16;    // blocks per slot, batches
+constexpr int kPopBlocksPerSlot = 48;    // blocks per slot, batches
 
 // one condition, arguments by value
 struct PopOne {
@@ -1079,7 +1060,6 @@ void launch_pop_phases(const Src& src, dim3 grid, cudaStream_t s) {
 // advance counter reset. One warp per slot.
 __global__ void k_batch_prep(BatchArgs b) {
   const int n = b.hdr->n_slots;
-  if (blockIdx.x == 0 && threadIdx.x < kFieldModes) b.hdr->chunk_counter[threadIdx.x] = 0;
   const int lane = threadIdx.x & 31;
   const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (s >= n) return;

@@ -195,19 +195,19 @@ struct BatchSlot {
 constexpr int kFieldModes = 5;
 
 // Slots are ordered by field mode; the advance runs one launch per mode over
-// that mode's chunks [mode_chunk[m], mode_chunk[m + 1]).
+// that mode's slots [mode_slot[m], mode_slot[m + 1]).
 struct BatchHeader {
   int n_slots;
   int adv_chunks, smp_chunks, hist_chunks;  // totals (last prefix entries)
   int mode_chunk[kFieldModes + 1];          // first advance chunk of each mode's slots
-  int chunk_counter[kFieldModes];           // advance work counters, zeroed by prep
+  int mode_slot[kFieldModes + 1];           // first slot of each mode
   int hist2_chunks;                         // velocity-distribution chunks (cylindrical slots)
 };
 
 constexpr int kBatchMaxSlots = 1024;
-constexpr int kBatchAdvanceChunk = 4096;   // electrons per block-chunk of the advance
-constexpr int kBatchSampleChunk = 4096;    // electrons per block of the moment sums
-constexpr int kBatchHistChunk = 32768;     // electrons per block of the histograms
+constexpr int kBatchAdvanceChunk = 4096;   // granularity of the advance's initial spread of blocks over slots
+constexpr int kBatchSampleChunk = 8192;    // electrons per block of the moment sums
+constexpr int kBatchHistChunk = 65535;     // electrons per block of the histograms (16-bit counts)
 
 // Staging layout (host pinned mirror and device copy are identical):
 //   BatchHeader | adv_prefix | smp_prefix | hist_prefix | hist2_prefix (kBatchMaxSlots+1 ints
