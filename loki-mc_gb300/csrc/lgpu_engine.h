@@ -455,6 +455,7 @@ class Engine {
   int init_ensemble() {
     if (!have_procs_ || !have_cond_) return fail(LGPU_ERR_STATE, "set_processes and set_conditions come first");
     drop_graphs();  // kernel arguments (field, constants, sizes) may have changed
+    hist_pending_ = false;
     LGPU_TRY(upload_proc_consts());
     time_ = 0;
     ss_time_ = kNonDef;

@@ -6,13 +6,13 @@ arrive while others run. Neither may change a result:
 
 * without ionization and attachment nothing couples the electrons and every
   electron's random stream is fixed by (seed, electron, interval), so a
-  batched solve repeats the solve alone. Under DC and crossed-B fields the
-  collision counts are equal and the swarm parameters agree to 1e-4 relative
-  (only the order of the floating-point moment sums differs, and with it the
-  FP32 origin shifts). Under AC the compiler contracts some multiply-adds of
-  the collision kinematics differently in the batched kernel, so trajectories
-  part at a rounding difference now and then: collision counts and swarm
-  parameters agree to 1e-3 relative;
+  batched solve repeats the solve alone up to rounding: the flights and
+  energies spell out their rounding, but the compiler may contract some
+  multiply-adds of the collision kinematics differently in the batched and
+  single-condition kernels, so a trajectory can part at a rounding difference.
+  Under DC and crossed B the collision counts and swarm parameters agree to
+  1e-4 relative (with the present build they are the same bits), under AC to
+  1e-3;
 * with ionization and attachment the secondaries draw from streams named by
   the warp that pushes them and population control claims slots with
   atomics, so the runs are statistically equivalent: mean energy and drift
@@ -130,14 +130,11 @@ def test_batch_repeats_alone_without_ionization():
         assert ra.capped == 0 and rb.capped == 0
         assert rb.sync_steps == ra.sync_steps, spec
         k = _drift_axis(spec)
-        if spec[4] == 0.0:  # DC and crossed B: the same bits
-            assert rb.real_collisions == ra.real_collisions, spec
-            assert rb.null_collisions == ra.null_collisions, spec
-            assert np.array_equal(ca, cb), spec
-            tol = 1e-4
-        else:
-            assert abs(rb.real_collisions / ra.real_collisions - 1.0) < 1e-3, spec
-            tol = 1e-3
+        tol = 1e-4 if spec[4] == 0.0 else 1e-3  # DC and crossed B / AC
+        assert abs(rb.real_collisions / ra.real_collisions - 1.0) < tol, spec
+        assert abs(rb.null_collisions / ra.null_collisions - 1.0) < tol, spec
+        big = ca > 10000
+        assert np.all(np.abs(cb[big] / ca[big].astype(float) - 1.0) < 10 * tol), spec
         assert abs(rb.mean_energy / ra.mean_energy - 1.0) < tol, spec
         assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < tol, spec
         if spec[4] == 0.0:

@@ -12,7 +12,9 @@ of its standard errors) are skipped. The batch-means errors of a 1e4-electron
 run understate its scatter (seeded reference runs of the atomic case differ by
 about 2 of their own errors), hence 0.5% as the floor. Rate coefficients
 of processes with at least 2000 reference counts agree within three combined
-Poisson errors doubled for autocorrelation, plus 1%.
+Poisson errors doubled for autocorrelation, plus 1%. The time-averaged EEDF
+agrees in 20 coarse energy bins (bins holding more than 1 % within 5 % +
+0.003) and in the mean energy it implies (1 %).
 """
 import glob
 import json
@@ -51,8 +53,20 @@ def run_gpu(rec, n_electrons=100_000):
                        meta.get("red_mag", 0.0))
     r = ctx.solve()
     counts, rate, _, _ = ctx.process_results()
+    dist = ctx.distributions()
     ctx.close()
-    return r, counts, rate, ps
+    return r, counts, rate, ps, dist
+
+
+def coarse_probabilities(cells, eedf, edges):
+    """Probability of each coarse energy bin from a normalised EEDF on uniform
+    cells: sum of f(e) sqrt(e) de over the cells whose centre lies in the bin
+    (BoltzmannMC.C:1574-1605 normalises f so that the full sum is 1)."""
+    cells = np.asarray(cells)
+    de = cells[1] - cells[0]
+    w = np.asarray(eedf) * np.sqrt(cells) * de
+    idx = np.digitize(cells, edges) - 1
+    return np.array([w[idx == k].sum() for k in range(len(edges) - 1)])
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -60,7 +74,7 @@ def test_swarm_parameters_match_reference(name):
     with open(os.path.join(gu.GOLDEN, f"stats_{name}.json")) as f:
         rec = json.load(f)
     ref = np.array(rec["result"])
-    r, counts, rate, ps = run_gpu(rec)
+    r, counts, rate, ps, dist = run_gpu(rec)
     assert r.capped == 0 and r.integration_points >= float(rec["numerics"]["nIntegrationPoints"]) - 1
     pairs = [("mean energy", r.mean_energy, r.mean_energy_err, ref[0], ref[1])]
     for k in range(3):
@@ -90,4 +104,18 @@ def test_swarm_parameters_match_reference(name):
         rel = 2.0 * 3.0 * np.sqrt(1.0 / c_ref + 1.0 / counts[p]) + 0.01
         if abs(rate[p] / ref_rate[p] - 1.0) > rel:
             failures.append(f"rate[{p}]: gpu {rate[p]:.6g}, reference {ref_rate[p]:.6g} (counts {counts[p]}, {c_ref:.0f})")
+    # time-averaged EEDF (BoltzmannMC.C:1492-1580): 20 coarse bins over the
+    # common energy range, bins holding > 1 % within 5 % + 0.003; the mean
+    # energy of the distribution within 1 %
+    cg, fg = dist["eedf_cells"], dist["eedf"]
+    cr, fr = np.array(rec["eedf_cells"]), np.array(rec["eedf"])
+    edges = np.linspace(0.0, min(cg[-1], cr[-1]), 21)
+    pg, pr = coarse_probabilities(cg, fg, edges), coarse_probabilities(cr, fr, edges)
+    for k in range(20):
+        if pr[k] > 0.01 and abs(pg[k] - pr[k]) > 0.05 * pr[k] + 0.003:
+            failures.append(f"EEDF bin {edges[k]:.3g}-{edges[k + 1]:.3g} eV: gpu {pg[k]:.4f}, reference {pr[k]:.4f}")
+    mg = np.sum(fg * cg ** 1.5) * (cg[1] - cg[0])
+    mr = np.sum(fr * cr ** 1.5) * (cr[1] - cr[0])
+    if abs(mg / mr - 1.0) > 0.01:
+        failures.append(f"EEDF mean energy: gpu {mg:.5g}, reference {mr:.5g}")
     assert not failures, "\n".join(failures)
