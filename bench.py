@@ -289,6 +289,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
     launches = intervals = 0
     h2d = d2h = host_ms = secondaries = spilled = 0.0
     real_batch = 0
+    coarse = -1
     for _ in range(args.steps):
         flush.add_(1.0)                    # L2 flush (256 MiB written), outside the timed region
         torch.cuda.synchronize()
@@ -312,12 +313,13 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         spilled += rep.spilled
         assert running == len(conds)
         real_batch = rep.real_batch
+        coarse = rep.coarse_null_test
     del b
     for c in ctxs:
         c.close()
     return dict(total_ms=total_ms, real=real, null=null, adv_ms=adv_ms, electron_steps=steps, launches=launches,
                 intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled,
-                real_batch=real_batch)
+                real_batch=real_batch, coarse=coarse)
 
 
 def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
@@ -535,7 +537,7 @@ def run_gpu_sweep(args):
                        "host_ms_per_step": tb["host_ms"] / args.steps,
                        "secondaries_per_step": tb["secondaries"] / args.steps,
                        "spilled_per_step": tb["spilled"] / args.steps,
-                       "collision_turn_threshold": tb["real_batch"]},
+                       "collision_turn_threshold": tb["real_batch"], "coarse_null_test": tb["coarse"]},
             "plain": plain, "batched_over_plain": ratio or None, "served": served,
             "accuracy": _accuracy(conds, e2e_b, e2e_p) if (e2e_b and e2e_p) else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

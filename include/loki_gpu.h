@@ -286,6 +286,7 @@ typedef struct lgpu_batch_report {
   double spilled;               /* of those, the ones a warp queue could not hold */
   double attached;              /* electrons removed by attachment */
   double real_batch;            /* collision-turn threshold in use (0 while it is being tuned) */
+  double coarse_null_test;      /* 1: null tests try the block bounds first, 0: not, -1: being tuned */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);

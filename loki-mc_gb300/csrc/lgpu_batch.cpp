@@ -74,7 +74,8 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
-    report->real_batch = b.tuned_;
+    report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
+    report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
   }
   return rc;
 }
@@ -119,7 +120,8 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
-    report->real_batch = b.tuned_;
+    report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
+    report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
   }
   b.members_.clear();
   b.active_.clear();

@@ -44,16 +44,21 @@ class Batch {
   double real_ = 0, null_ = 0;  // collisions of the batched intervals
   double host_ms_ = 0, secondaries_ = 0, spilled_ = 0, attached_ = 0;
 
-  // On-line tuning of the collision-turn threshold (AdvanceArgs::real_batch)
-  // for members whose config leaves it at 0. It changes how lanes are
-  // scheduled, never what an electron draws, so tuning intervals are ordinary
-  // intervals: the candidates take turns, kTuneRounds times each, and the one
-  // with the least advance time per electron-interval (median) is kept.
-  static constexpr int kTuneCandidates[5] = {12, 16, 20, 24, 28};
+  // On-line tuning of two scheduling choices of the advance for members whose
+  // config leaves the threshold at 0: the collision-turn threshold
+  // (AdvanceArgs::real_batch) and whether the null test tries the block
+  // bounds first (AdvanceArgs::coarse). Neither changes what an electron
+  // draws or decides, so tuning intervals are ordinary intervals: the
+  // candidates take turns, kTuneRounds times each, and the one with the least
+  // advance time per electron-interval (median) is kept.
+  static constexpr int kTuneThresholds[5] = {12, 16, 20, 24, 28};
+  static constexpr int kTuneCandidates = 10;  // thresholds x coarse test off / on
   static constexpr int kTuneRounds = 3;
   int tune_next_ = 0;   // intervals measured so far
-  int tuned_ = 0;       // chosen threshold, 0 while tuning
-  std::vector<double> tune_cost_[5];
+  int tuned_ = -1;      // chosen candidate, -1 while tuning
+  std::vector<double> tune_cost_[kTuneCandidates];
+  static int tune_threshold(int c) { return kTuneThresholds[c % 5]; }
+  static int tune_coarse(int c) { return c / 5; }
 
   struct Member {
     Engine* e = nullptr;
@@ -240,13 +245,14 @@ class Batch {
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
     int na = 0, ns = 0, nh = 0, nv = 0;
     double electrons = 0;
-    const int ncand = (int)(sizeof(kTuneCandidates) / sizeof(int));
-    const int cand = tuned_ ? -1 : tune_next_ % ncand;
-    const int real_batch = tuned_ ? tuned_ : kTuneCandidates[cand];
+    const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
     for (int s = 0; s < n; ++s) {
       Engine* e = members_[go[s]].e;
       e->fill_slot(&sl[s]);
-      if (e->cfg_.advance_real_batch == 0) sl[s].adv.real_batch = real_batch;
+      if (e->cfg_.advance_real_batch == 0) {
+        sl[s].adv.real_batch = tune_threshold(cand);
+        sl[s].adv.coarse = tune_coarse(cand);
+      }
       const int N = e->n_electrons();
       electrons += N;
       ap[s] = na;
@@ -290,19 +296,21 @@ class Batch {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     adv_ms_ += ms;
-    if (!tuned_ && electrons > 0) {
+    if (tuned_ < 0 && electrons > 0) {
       tune_cost_[cand].push_back(ms / electrons);
-      if (++tune_next_ >= ncand * kTuneRounds) {
+      if (++tune_next_ >= kTuneCandidates * kTuneRounds) {
         double best = 0;
-        for (int k = 0; k < ncand; ++k) {
+        int pick = 0;
+        for (int k = 0; k < kTuneCandidates; ++k) {
           std::vector<double> v = tune_cost_[k];
           std::sort(v.begin(), v.end());
           const double med = v[v.size() / 2];
-          if (!tuned_ || med < best) {
+          if (k == 0 || med < best) {
             best = med;
-            tuned_ = kTuneCandidates[k];
+            pick = k;
           }
         }
+        tuned_ = pick;
       }
     }
     electron_steps_ += electrons;

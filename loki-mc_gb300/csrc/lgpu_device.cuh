@@ -481,12 +481,17 @@ __device__ __forceinline__ int row_count_below(const float2* row, int P, int str
 // Null test of a cold gas (BoltzmannMC.C:1033-1052): r = U nu_trial against
 // the interpolated total frequency. False for a null collision; r is kept
 // for the process choice.
+// With `coarse` (a copy of the table's block bounds, e.g. in shared memory)
+// most null collisions are decided without loading the table row: r above the
+// bound of the row's block is above the interpolated frequency too.
 template <class Rng>
-__device__ __forceinline__ bool cold_real(const TablesF& t, float nu_trial, float energy, Rng& rng, float& r) {
+__device__ __forceinline__ bool cold_real(const TablesF& t, float nu_trial, float energy, Rng& rng, float& r,
+                                          const float* coarse = nullptr) {
   r = nu_trial * rng.oc();
   int i1;
   float w1, w2;
   row_weights(energy * t.inv_step, t.M, i1, w1, w2);
+  if (coarse && r > coarse[i1 >> t.coarse_shift]) return false;
   const float2 nt = __ldg(&t.nu_pair[i1]);
   return !(r > w1 * nt.x + w2 * nt.y);
 }

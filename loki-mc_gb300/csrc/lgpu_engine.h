@@ -138,6 +138,10 @@ class Engine {
     LGPU_TRY(dalloc(&d_nu_pair_, (size_t)M_));
     LGPU_TRY(dalloc(&d_nu_tot_, (size_t)M_));
     LGPU_TRY(dalloc(&d_nu_max_, (size_t)M_));
+    LGPU_TRY(dalloc(&d_nu_coarse_, (size_t)kMaxCoarse));
+    coarse_shift_ = 0;
+    while (((M_ + (1 << coarse_shift_) - 1) >> coarse_shift_) > kMaxCoarse) ++coarse_shift_;
+    n_coarse_ = (M_ + (1 << coarse_shift_) - 1) >> coarse_shift_;
     h_nu_max_.assign(M_, 0.0);
     const int nEC = cfg_.n_energy_cells;
     LGPU_TRY(dalloc(&d_eedf_, (size_t)nEC));
@@ -157,7 +161,7 @@ class Engine {
     d_ctl_ = nullptr;
     h_ctl_ = nullptr;
     void* ptrs[] = {d_state_, d_alive_, d_spill_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
-                    d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_cum_pair_, d_sig_pair_, d_procf_,
+                    d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_nu_coarse_, d_cum_pair_, d_sig_pair_, d_procf_,
                     d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
                     d_raw_e_, d_raw_v_, d_proc_count_, d_proc_gain_, d_proc_loss_, d_eedf_, d_eedf_per_, d_eadf_,
                     d_evdf_, d_rp_in_, d_rp_out_};
@@ -372,6 +376,9 @@ class Engine {
     t.stride = stride_;
     t.inv_step = (float)(1.0 / step_);
     t.inv_N = (float)(1.0 / Ngas_);
+    t.nu_coarse = d_nu_coarse_;
+    t.coarse_shift = coarse_shift_;
+    t.n_coarse = n_coarse_;
     return t;
   }
 
@@ -403,8 +410,11 @@ class Engine {
     a.nu_max = d_nu_max_;
     a.sig64 = sig64;
     a.cum64 = cum64;
+    a.nu_coarse = d_nu_coarse_;
+    a.coarse_shift = coarse_shift_;
+    a.n_coarse = n_coarse_;
     launch_build_tables(a, stream_);
-    launches_ += 2;
+    launches_ += 3;
     LGPU_CU(copy(h_nu_max_.data(), d_nu_max_, M_ * sizeof(double), cudaMemcpyDeviceToHost));
     return sync("build_tables");
   }
@@ -562,6 +572,7 @@ class Engine {
     a.sm_count = sm_count_;
     a.ctl = d_ctl_;
     a.real_batch = cfg_.advance_real_batch > 0 ? std::min(cfg_.advance_real_batch, 32) : kDefaultRealBatch;
+    a.coarse = 1;
     return a;
   }
 
@@ -1026,6 +1037,7 @@ class Engine {
   // sequence per interval.
   int solve_begin() {
     solve_t0_ = std::chrono::steady_clock::now();
+    ++solve_serial_;
     LGPU_TRY(init_ensemble());
     solve_good_ = false;
     solve_capped_ = 0;
@@ -1141,15 +1153,21 @@ class Engine {
     s.max_energy_bits = &d_sc_->sample_max_bits;
     return s;
   }
-  // this context's slot of the next batched interval (after interval_pre)
+  // this context's slot of the next batched interval (after interval_pre);
+  // the argument blocks are fixed once the ensemble starts, so they are
+  // built once per solve and only the control block and flags change
   void fill_slot(BatchSlot* sl) {
-    std::memset(sl, 0, sizeof(*sl));
-    sl->adv = advance_args();
-    sl->pop = pop_args();
-    sl->smp = sample_args();
+    if (slot_built_ != solve_serial_) {
+      std::memset(&slot_, 0, sizeof(slot_));
+      slot_.adv = advance_args();
+      slot_.pop = pop_args();
+      slot_.smp = sample_args();
+      slot_.ctl_dst = d_ctl_;
+      slot_.sc = d_sc_;
+      slot_built_ = solve_serial_;
+    }
+    std::memcpy(sl, &slot_, sizeof(*sl));
     sl->ctl = *h_ctl_;
-    sl->ctl_dst = d_ctl_;
-    sl->sc = d_sc_;
     sl->flags = (have_ion_att_ ? kSlotIonAtt : 0) | (sampling_ ? kSlotSample : 0);
     if (hist_pending_) {
       sl->hist = pending_hist_;
@@ -1505,6 +1523,8 @@ class Engine {
   double pending_dt_ = 0;
   // batch mode
   bool batch_ = false, hist_pending_ = false;
+  BatchSlot slot_{};                            // cached argument blocks of this solve's batch slot
+  long long solve_serial_ = 0, slot_built_ = -1;
   cudaStream_t own_stream_ = nullptr;
   HistArgs pending_hist_{};
   // timing
@@ -1526,6 +1546,8 @@ class Engine {
   long long graph_launches_[2] = {0, 0};
   float2 *d_nu_pair_ = nullptr, *d_cum_pair_ = nullptr, *d_sig_pair_ = nullptr;
   double *d_nu_tot_ = nullptr, *d_nu_max_ = nullptr;
+  float* d_nu_coarse_ = nullptr;
+  int coarse_shift_ = 0, n_coarse_ = 1;
   ProcF* d_procf_ = nullptr;
   GasF* d_gasf_ = nullptr;
   int *d_is_super_ = nullptr, *d_raw_off_ = nullptr, *d_raw_len_ = nullptr;

@@ -76,6 +76,7 @@ constexpr int kLocalQ = 32;
 // Shared memory of an advance block: constants and per-process tallies of the
 // block's current condition, the warps' secondary queues, reduction scratch.
 struct AdvShared {
+  float nu_coarse[kMaxCoarse];  // block bounds of the total frequency of the current condition
   unsigned int count[kMaxProcesses];
   float gain[kMaxProcesses];
   float loss[kMaxProcesses];
@@ -175,12 +176,14 @@ __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, AdvShare
   }
   if (threadIdx.x < a.c.G) sh.gas[threadIdx.x] = a.gases[threadIdx.x];
   if (threadIdx.x < kAdvanceWarps) sh.qn[threadIdx.x] = 0;
+  if (a.t.nu_coarse)
+    for (int b = threadIdx.x; b < a.t.n_coarse; b += blockDim.x) sh.nu_coarse[b] = a.t.nu_coarse[b];
 }
 
 // an ensemble electron (left alone when its slot is attached)
 __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const IntervalView& iv, Lane& L, int idx) {
-  const float4 A = a.state[2 * idx];
-  const float4 B = a.state[2 * idx + 1];
+  const float4 A = a.state[idx];
+  const float4 B = a.state[a.n + idx];
   if (B.w == 0.0f) {
     L.slot = idx;
     L.p = make_float3(A.x - iv.shift.x, A.y - iv.shift.y, A.z - iv.shift.z);
@@ -236,8 +239,8 @@ __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const Inte
 // synchronisation time.
 __device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneTally& tl, bool dead) {
   if (L.slot >= 0) {
-    a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
-    a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
+    a.state[L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
+    a.state[a.n + L.slot] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
   } else if (!dead) {
     const int k = append_slot(a.sec_count);
     if (k < a.sec_cap) {
@@ -260,7 +263,8 @@ __device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneT
 // then runs on most of the warp's lanes instead of a few. Each electron draws
 // its random numbers in the same order either way.
 template <int MODE>
-__device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const IntervalView& iv, Lane& L, LaneTally& tl) {
+__device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const AdvShared& sh, const IntervalView& iv, Lane& L,
+                                            LaneTally& tl) {
   if (L.s < 0.0f) L.s = -__logf(L.rng.oo());
   const float tau = L.s * iv.inv_nu;
   const bool partial = L.t + tau > iv.T;
@@ -277,7 +281,8 @@ __device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const Interval
     return;
   }
   L.t += tau;
-  if (is_thermal(a.c, L.energy) || cold_real(iv.tab, iv.nu, L.energy, L.rng, L.r)) {
+  if (is_thermal(a.c, L.energy) ||
+      cold_real(iv.tab, iv.nu, L.energy, L.rng, L.r, (a.coarse && iv.tab.nu_coarse) ? sh.nu_coarse : nullptr)) {
     L.pending = true;
     return;
   }
@@ -348,7 +353,7 @@ __device__ __forceinline__ void warp_turn(const AdvanceArgs& a, AdvShared& sh, i
   if (__popc(pend) >= a.real_batch || pend == live) {
     if (L.pending) lane_real(a, sh, wid, iv, L, tl);
   } else if (L.have && !L.pending) {
-    lane_flight<MODE>(a, iv, L, tl);
+    lane_flight<MODE>(a, sh, iv, L, tl);
   }
 }
 
@@ -599,8 +604,8 @@ __global__ void k_init(InitArgs a) {
     float sb, cb;
     sincosf(kTwoPiF * r2, &sb, &cb);
     const float3 v = make_float3(aa * cb * a.sd, aa * sb * a.sd, sqrtf(-2.0f * logf(r3)) * cosf(kTwoPiF * r4) * a.sd);
-    a.state[2 * i] = make_float4(0.f, 0.f, 0.f, -1.0f);
-    a.state[2 * i + 1] = make_float4(v.x, v.y, v.z, 0.0f);
+    a.state[i] = make_float4(0.f, 0.f, 0.f, -1.0f);
+    a.state[a.n + i] = make_float4(v.x, v.y, v.z, 0.0f);
     e = energy_of(v, a.half_me_over_e);
   }
   e = warp_max(e);
@@ -695,6 +700,21 @@ __global__ void k_prefix_max(const double* nu_tot, double* nu_max, int M) {
   }
 }
 
+// block bounds of the total frequency for the coarse null test: the largest
+// FP32 value of rows [b R, (b+1) R] (row pairs cover the next row), raised
+// by 2^-20 relative against the rounding of the interpolation
+__global__ void k_coarse_max(const float2* nu_pair, int M, int shift, float* coarse, int n_coarse) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_coarse) return;
+  const int i0 = b << shift, i1 = min((b + 1) << shift, M);
+  float m = 0.0f;
+  for (int i = i0; i < i1; ++i) {
+    const float2 v = nu_pair[i];
+    m = fmaxf(m, fmaxf(v.x, v.y));
+  }
+  coarse[b] = m * (1.0f + 9.5367431640625e-7f);
+}
+
 // ---------------------------------------------------------------- sample
 constexpr int kSampleThreads = 256;
 
@@ -707,9 +727,7 @@ __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int
 #pragma unroll
   for (int k = 0; k < kMoments; ++k) m[k] = 0.0f;
   float e_max = 0.0f;
-  for (int i = begin; i < end; i += step) {
-    const float4 A = a.state[2 * i];
-    const float4 B = a.state[2 * i + 1];
+  auto add = [&](float4 A, float4 B) {
     const float e = energy_of(make_float3(B.x, B.y, B.z), a.half_me_over_e);
     e_max = fmaxf(e_max, e);
     const float x = A.x, y = A.y, z = A.z, vx = B.x, vy = B.y, vz = B.z;
@@ -720,7 +738,20 @@ __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int
     m[13] += x * vx; m[14] += x * vy; m[15] += x * vz;
     m[16] += y * vx; m[17] += y * vy; m[18] += y * vz;
     m[19] += z * vx; m[20] += z * vy; m[21] += z * vz;
+  };
+  // four electrons' loads in flight before their sums (memory-level parallelism)
+  int i = begin;
+  for (; i + 3 * step < end; i += 4 * step) {
+    float4 A[4], B[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      A[u] = a.state[i + u * step];
+      B[u] = a.state[a.n + i + u * step];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) add(A[u], B[u]);
   }
+  for (; i < end; i += step) add(a.state[i], a.state[a.n + i]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // FP32 tree reduction inside the warp (32 partials), FP64 across warps and blocks
 #pragma unroll
@@ -791,21 +822,35 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
   const int zero_words = nE + (a_shared ? nAw : 0);
   for (int w = threadIdx.x; w < zero_words; w += blockDim.x) sm[w] = 0u;
   __syncthreads();
+  // With the EADF in shared memory the EEDF count of a cell is its EADF row
+  // sum, so only electrons outside the cos cells (cos rounding to 1, zero
+  // speed) are counted into hE: one shared-memory atomic per electron.
   for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
     int c, cy, rx, ry;
-    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
+    hist_cells(a, a.state[a.n + i], c, cy, rx, ry);
     if (c >= 0 && c < nE) {
-      atomicAdd(&hE[c], 1u);
       if (a.cylindrical && cy < a.n_cos && cy >= 0) {
         const int idx = c * a.n_cos + cy;
-        if (a_shared) atomicAdd(&hA[idx >> 1], 1u << ((idx & 1) << 4));
-        else atomicAdd(&a.eadf[idx], 1.0);
+        if (a_shared) {
+          atomicAdd(&hA[idx >> 1], 1u << ((idx & 1) << 4));
+        } else {
+          atomicAdd(&hE[c], 1u);
+          atomicAdd(&a.eadf[idx], 1.0);
+        }
+      } else {
+        atomicAdd(&hE[c], 1u);
       }
     }
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nE; c += blockDim.x) {
-    const unsigned int h = hE[c];
+    unsigned int h = hE[c];
+    if (a_shared) {
+      for (int k = 0; k < a.n_cos; ++k) {
+        const int idx = c * a.n_cos + k;
+        h += (hA[idx >> 1] >> ((idx & 1) << 4)) & 0xFFFFu;
+      }
+    }
     if (h) {
       atomicAdd(&a.eedf[c], (double)h);
       if (a.eedf_periodic_row) atomicAdd(&a.eedf_periodic_row[c], (double)h);
@@ -831,7 +876,7 @@ __device__ __forceinline__ void hist_chunk_b(const HistArgs& a, int first, int l
   __syncthreads();
   for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
     int c, cy, rx, ry;
-    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
+    hist_cells(a, a.state[a.n + i], c, cy, rx, ry);
     if (rx < a.n_rad && rx >= 0 && ry < a.n_ax && ry >= 0) {
       const int idx = rx * a.n_ax + ry;
       if (v_shared) atomicAdd(&sm[idx >> 1], 1u << ((idx & 1) << 4));
@@ -946,8 +991,8 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_fill(Src src) {
   for (int j = pop_tid(); j < k; j += pop_stride()) {
     const int slot = a.att_list[j];
     const int sidx = a.alive[n_sec - 1 - j];
-    a.state[2 * slot] = a.sec[2 * sidx];
-    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
+    a.state[slot] = a.sec[2 * sidx];
+    a.state[a.n_electrons + slot] = a.sec[2 * sidx + 1];
   }
   for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
     const int dest = a.att_list[n_sec + jj];
@@ -969,7 +1014,7 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
     int src_slot = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
       const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
-      if (!claimed(a.claim, r) && a.state[2 * r + 1].w == 0.0f) {
+      if (!claimed(a.claim, r) && a.state[a.n_electrons + r].w == 0.0f) {
         src_slot = r;
         break;
       }
@@ -978,9 +1023,9 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
       atomicExch(a.error_flag, 4);
       continue;
     }
-    const float4 A = a.state[2 * src_slot], B = a.state[2 * src_slot + 1];
-    a.state[2 * dest] = A;
-    a.state[2 * dest + 1] = B;
+    const float4 A = a.state[src_slot], B = a.state[a.n_electrons + src_slot];
+    a.state[dest] = A;
+    a.state[a.n_electrons + dest] = B;
     add_growth(a.growth, (double)energy4(B, hme));
   }
   const int m = n_sec - n_att;
@@ -1017,7 +1062,7 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_sort(Src src) {
     const int r = a.removed[j];
     if (r >= 0 && r < a.n_electrons) {
       a.pair_slot[append_slot(&a.counts[1])] = r;
-      add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], hme));
+      add_growth(a.growth, -(double)energy4(a.state[a.n_electrons + r], hme));
     } else if (r >= a.n_electrons) {
       add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], hme));
     }
@@ -1035,8 +1080,8 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_place(Src src) {
   for (int q = pop_tid(); q < np; q += pop_stride()) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
-    a.state[2 * slot] = a.sec[2 * sidx];
-    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
+    a.state[slot] = a.sec[2 * sidx];
+    a.state[a.n_electrons + slot] = a.sec[2 * sidx + 1];
   }
   const int m = n_sec - n_att;
   for (int j = pop_tid(); j < m; j += pop_stride()) {
@@ -1208,6 +1253,7 @@ void launch_init(const InitArgs& a, cudaStream_t s) {
 void launch_build_tables(const TableBuildArgs& a, cudaStream_t s) {
   k_build_tables<<<blocks_for(a.M, 128), 128, 0, s>>>(a);
   k_prefix_max<<<1, 1024, 0, s>>>(a.nu_tot, a.nu_max, a.M);
+  if (a.nu_coarse) k_coarse_max<<<1, kMaxCoarse, 0, s>>>(a.nu_pair, a.M, a.coarse_shift, a.nu_coarse, a.n_coarse);
 }
 
 void launch_sample(const SampleArgs& a, cudaStream_t s) {

@@ -36,7 +36,7 @@ struct DevScalars {
 // way; secondaries created on the way are queued and pushed from their
 // creation time to the end of the interval by the same launch.
 struct AdvanceArgs {
-  float4* state;            // [2*N]: (x, y, z, s) and (vx, vy, vz, dead flag)
+  float4* state;            // structure of arrays: [N] (x, y, z, s), then [N] (vx, vy, vz, dead flag)
   int n;                    // electrons of the ensemble
   float dt_sync;            // interval length (s)
   float phi0;               // phase at the interval start (rad), FP64-reduced on the host
@@ -76,6 +76,7 @@ struct AdvanceArgs {
   const IntervalCtl* ctl;          // when set: per-interval values are read from here
   int queue_only;                  // 1: only drain the spilled secondaries (one warp)
   int real_batch;                  // pending real collisions that start a warp's collision turn (1..32)
+  int coarse;                      // 1: null test against the block bounds first (t.nu_coarse)
 };
 constexpr int kDefaultRealBatch = 20;
 
@@ -115,6 +116,8 @@ struct TableBuildArgs {
   double* nu_max;     // FP64 running maximum
   double* sig64;      // optional FP64 sigma*n [M*P] (tests), may be null
   double* cum64;      // optional FP64 cumulative [M*P] (tests), may be null
+  float* nu_coarse;   // block bounds for the coarse null test [n_coarse], may be null
+  int coarse_shift, n_coarse;
 };
 void launch_build_tables(const TableBuildArgs& a, cudaStream_t s);
 

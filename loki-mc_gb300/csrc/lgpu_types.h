@@ -62,7 +62,13 @@ struct TablesF {
   int stride;              // row stride in pairs: P rounded up to even (16-byte rows), padded with +inf / 0
   float inv_step;          // 1 / energy step (1/eV)
   float inv_N;             // 1 / gas density
+  // bound of the total frequency over blocks of 2^coarse_shift rows (one
+  // block also covers the row after it), slightly raised so that rounding in
+  // the interpolation cannot exceed it: r above it is a null collision
+  const float* nu_coarse;  // [n_coarse], or null
+  int coarse_shift, n_coarse;
 };
+constexpr int kMaxCoarse = 256;
 
 // Per-condition constants used by the kernels.
 struct Consts {
