@@ -182,8 +182,8 @@ __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, AdvShare
 
 // an ensemble electron (left alone when its slot is attached)
 __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const IntervalView& iv, Lane& L, int idx) {
-  const float4 A = a.state[idx];
-  const float4 B = a.state[a.n + idx];
+  const float4 A = a.state[2 * idx];
+  const float4 B = a.state[2 * idx + 1];
   if (B.w == 0.0f) {
     L.slot = idx;
     L.p = make_float3(A.x - iv.shift.x, A.y - iv.shift.y, A.z - iv.shift.z);
@@ -239,8 +239,8 @@ __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const Inte
 // synchronisation time.
 __device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneTally& tl, bool dead) {
   if (L.slot >= 0) {
-    a.state[L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
-    a.state[a.n + L.slot] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
+    a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
+    a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
   } else if (!dead) {
     const int k = append_slot(a.sec_count);
     if (k < a.sec_cap) {
@@ -604,8 +604,8 @@ __global__ void k_init(InitArgs a) {
     float sb, cb;
     sincosf(kTwoPiF * r2, &sb, &cb);
     const float3 v = make_float3(aa * cb * a.sd, aa * sb * a.sd, sqrtf(-2.0f * logf(r3)) * cosf(kTwoPiF * r4) * a.sd);
-    a.state[i] = make_float4(0.f, 0.f, 0.f, -1.0f);
-    a.state[a.n + i] = make_float4(v.x, v.y, v.z, 0.0f);
+    a.state[2 * i] = make_float4(0.f, 0.f, 0.f, -1.0f);
+    a.state[2 * i + 1] = make_float4(v.x, v.y, v.z, 0.0f);
     e = energy_of(v, a.half_me_over_e);
   }
   e = warp_max(e);
@@ -745,13 +745,13 @@ __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int
     float4 A[4], B[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      A[u] = a.state[i + u * step];
-      B[u] = a.state[a.n + i + u * step];
+      A[u] = a.state[2 * (i + u * step)];
+      B[u] = a.state[2 * (i + u * step) + 1];
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) add(A[u], B[u]);
   }
-  for (; i < end; i += step) add(a.state[i], a.state[a.n + i]);
+  for (; i < end; i += step) add(a.state[2 * i], a.state[2 * i + 1]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // FP32 tree reduction inside the warp (32 partials), FP64 across warps and blocks
 #pragma unroll
@@ -827,7 +827,7 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
   // speed) are counted into hE: one shared-memory atomic per electron.
   for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
     int c, cy, rx, ry;
-    hist_cells(a, a.state[a.n + i], c, cy, rx, ry);
+    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
     if (c >= 0 && c < nE) {
       if (a.cylindrical && cy < a.n_cos && cy >= 0) {
         const int idx = c * a.n_cos + cy;
@@ -876,7 +876,7 @@ __device__ __forceinline__ void hist_chunk_b(const HistArgs& a, int first, int l
   __syncthreads();
   for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
     int c, cy, rx, ry;
-    hist_cells(a, a.state[a.n + i], c, cy, rx, ry);
+    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
     if (rx < a.n_rad && rx >= 0 && ry < a.n_ax && ry >= 0) {
       const int idx = rx * a.n_ax + ry;
       if (v_shared) atomicAdd(&sm[idx >> 1], 1u << ((idx & 1) << 4));
@@ -991,8 +991,8 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_fill(Src src) {
   for (int j = pop_tid(); j < k; j += pop_stride()) {
     const int slot = a.att_list[j];
     const int sidx = a.alive[n_sec - 1 - j];
-    a.state[slot] = a.sec[2 * sidx];
-    a.state[a.n_electrons + slot] = a.sec[2 * sidx + 1];
+    a.state[2 * slot] = a.sec[2 * sidx];
+    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
   for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
     const int dest = a.att_list[n_sec + jj];
@@ -1014,7 +1014,7 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
     int src_slot = -1;
     for (uint32_t d = 0; d < 4096u; ++d) {
       const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
-      if (!claimed(a.claim, r) && a.state[a.n_electrons + r].w == 0.0f) {
+      if (!claimed(a.claim, r) && a.state[2 * r + 1].w == 0.0f) {
         src_slot = r;
         break;
       }
@@ -1023,9 +1023,9 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
       atomicExch(a.error_flag, 4);
       continue;
     }
-    const float4 A = a.state[src_slot], B = a.state[a.n_electrons + src_slot];
-    a.state[dest] = A;
-    a.state[a.n_electrons + dest] = B;
+    const float4 A = a.state[2 * src_slot], B = a.state[2 * src_slot + 1];
+    a.state[2 * dest] = A;
+    a.state[2 * dest + 1] = B;
     add_growth(a.growth, (double)energy4(B, hme));
   }
   const int m = n_sec - n_att;
@@ -1062,7 +1062,7 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_sort(Src src) {
     const int r = a.removed[j];
     if (r >= 0 && r < a.n_electrons) {
       a.pair_slot[append_slot(&a.counts[1])] = r;
-      add_growth(a.growth, -(double)energy4(a.state[a.n_electrons + r], hme));
+      add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], hme));
     } else if (r >= a.n_electrons) {
       add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], hme));
     }
@@ -1080,8 +1080,8 @@ __global__ void __launch_bounds__(kPopThreads) k_pop_place(Src src) {
   for (int q = pop_tid(); q < np; q += pop_stride()) {
     const int slot = a.pair_slot[q];
     const int sidx = a.pair_sec[q];
-    a.state[slot] = a.sec[2 * sidx];
-    a.state[a.n_electrons + slot] = a.sec[2 * sidx + 1];
+    a.state[2 * slot] = a.sec[2 * sidx];
+    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
   }
   const int m = n_sec - n_att;
   for (int j = pop_tid(); j < m; j += pop_stride()) {

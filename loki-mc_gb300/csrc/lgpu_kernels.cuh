@@ -36,7 +36,7 @@ struct DevScalars {
 // way; secondaries created on the way are queued and pushed from their
 // creation time to the end of the interval by the same launch.
 struct AdvanceArgs {
-  float4* state;            // structure of arrays: [N] (x, y, z, s), then [N] (vx, vy, vz, dead flag)
+  float4* state;            // [2*N]: (x, y, z, s) and (vx, vy, vz, dead flag) per electron
   int n;                    // electrons of the ensemble
   float dt_sync;            // interval length (s)
   float phi0;               // phase at the interval start (rad), FP64-reduced on the host
