@@ -41,6 +41,9 @@ ATOMIC = [("atomic", 20000, 50.0, 180.0, 0.0, 0.0, 11), ("atomic", 50000, 100.0,
           ("atomic", 30000, 100.0, 90.0, 0.0, 500.0, 13), ("atomic", 30000, 150.0, 180.0, F_AC, 0.0, 14)]
 MIX = [("mix", 50000, 100.0, 180.0, 0.0, 0.0, 21), ("mix", 20000, 300.0, 180.0, 0.0, 0.0, 22),
        ("mix", 30000, 100.0, 90.0, 0.0, 500.0, 23), ("mix", 30000, 150.0, 180.0, F_AC, 0.0, 24)]
+# different mixtures (2, 40 and 65 processes) in one batch
+MIXTURES = [("atomic", 20000, 100.0, 180.0, 0.0, 0.0, 31), ("n2", 40000, 200.0, 180.0, 0.0, 0.0, 32),
+            ("mix", 30000, 100.0, 180.0, 0.0, 0.0, 33), ("n2", 25000, 150.0, 90.0, 0.0, 800.0, 34)]
 
 
 def _inputs(case):
@@ -212,3 +215,29 @@ def test_server_admits_by_memory_footprint():
     for s0, s1 in zip(sts, sts[1:]):
         assert s1.start_time >= s0.end_time - 1e-6  # never two at once
     assert st_big.state == capi.JOB_FAILED and st_big.status == 2  # LGPU_ERR_OOM
+
+
+def test_batch_and_server_with_different_mixtures():
+    # each slot carries its own process set, tables and gases: a block that
+    # moves between slots reloads them
+    from lokigpu import capi
+    alone = _alone(MIXTURES)
+    batched, rep = _batched(MIXTURES)
+    fails = []
+    for spec, a, b in zip(MIXTURES, alone, batched):
+        fails += _statistically_equal(spec, a, b)
+    srv = capi.Server(0, 8)
+    ids = []
+    for spec in MIXTURES:
+        case, n_e, red_field, angle, freq, red_mag, seed = spec
+        ps, arrays = _inputs(case)
+        ids.append(srv.submit(_config(n_e, seed), ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"],
+                              N_GAS, 300.0, red_field, angle, freq, red_mag))
+    for spec, jid, a in zip(MIXTURES, ids, alone):
+        st = srv.wait(jid, 600.0)
+        assert st.state == capi.JOB_DONE, (spec, st.status, st.error)
+        ps, _ = _inputs(spec[0])
+        counts, rate = srv.rates(jid, ps.n)
+        fails += _statistically_equal(spec, a, (st.result, counts, rate))
+    srv.stop()
+    assert not fails, "\n".join(fails)
