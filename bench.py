@@ -28,6 +28,12 @@ results and rate coefficients read back; the same for the plain form
 --workload n2_200td keeps the single-condition line: the synthetic N2-like gas
 at DC 200 Td with 1e6 electrons, one plain interval per step.
 
+--workload serve runs a request stream through lgpu_server: seeded requests of
+1-5 random gases (10-40 processes on 100-400-point grids), E/N 1..1000 Td, DC,
+crossed B or AC, 1e4..4e6 electrons, Poisson arrivals; each converged to 0.5 %
+mean-energy error; p50/p99 latency and throughput, and the plain path on the
+first requests.
+
 --impl reference times the CPU implementation of the same path on the host
 cores (the C restatement of the reference's algorithm, oracle/) on a bounded
 sample of the same workload.
@@ -61,9 +67,9 @@ N_ELECTRONS = 1_000_000
 DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch), from
-# one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 739.2 MB
-# read + 584.3 MB written for 1.98e7 electrons
-SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (739.159040e6 + 584.292352e6) / 19795598
+# one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 852.6 MB
+# read + 586.6 MB written for 1.98e7 electrons
+SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (852.604928e6 + 586.584320e6) / 19795598
 
 # sweep workload
 SWEEP_POINTS = 64
@@ -554,6 +560,121 @@ def run_gpu_sweep(args):
     return 0
 
 
+# ------------------------------------------------------------ serving stream
+def serve_requests(n, seed=SWEEP_SEED + 7):
+    """A seeded request stream: each request a mixture of 1-5 random gases
+    (10-40 processes on 100-400-point grids, to 1e4 eV), E/N log-uniform in
+    1..1000 Td, DC (60 %), crossed DC B with B/N 100..2000 Hx (20 %) or AC with
+    omega/N log-uniform 1e-16..1e-14 m^3/s (20 %), electrons log-uniform in
+    1e4..max_electrons."""
+    import numpy as np
+    from lokigpu import synth
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ng = int(rng.integers(1, 6))
+        fr = rng.dirichlet(np.ones(ng))
+        gases = [synth.random_gas(int(seed * 1000 + 10 * i + g), f"R{i}G{g}", float(fr[g]), e_max=1e4)
+                 for g in range(ng)]
+        en = float(10 ** rng.uniform(0.0, 3.0))
+        kind = rng.random()
+        angle, freq, red_mag = 180.0, 0.0, 0.0
+        if kind < 0.2:
+            angle, red_mag = 90.0, float(rng.uniform(100.0, 2000.0))
+        elif kind < 0.4:
+            freq = float(10 ** rng.uniform(-16.0, -14.0)) * N_GAS / (2.0 * np.pi)
+        ne = int(round(10 ** rng.uniform(4.0, np.log10(SERVE_MAX_ELECTRONS))))
+        out.append(dict(gases=gases, en=en, angle=angle, freq=freq, red_mag=red_mag, ne=ne, seed=9000 + i))
+    return out
+
+
+SERVE_MAX_ELECTRONS = 4e6
+
+
+def run_gpu_serve(args):
+    """Served request stream: latency percentiles, throughput, and the plain
+    sequential path on the first requests for comparison."""
+    import numpy as np
+    import torch
+
+    from lokigpu import build as gbuild
+    from lokigpu import capi, synth
+
+    rank, world, local = _init_ranks()
+    if not os.path.exists(capi.library_path()):
+        gbuild.build()
+    reqs = serve_requests(args.requests)
+    sets = [synth.flatten(r["gases"]) for r in reqs]
+    rng = np.random.default_rng(SWEEP_SEED + 11)
+    gaps = rng.exponential(args.arrival_ms * 1e-3, len(reqs))
+    clocks = ClockSampler(local)
+    clocks.start()
+    srv = capi.Server(local, args.slots)
+    ids = []
+    w0 = time.perf_counter()
+    for r, ps, gap in zip(reqs, sets, gaps):
+        time.sleep(float(gap))
+        cfg = sweep_config(capi, local, r["ne"], r["seed"], converge=True)
+        cfg.n_phases = 16
+        cfg.max_seconds = args.request_cap_s
+        ids.append(srv.submit(cfg, ps, ps.gas_first, ps.gas_last, ps.gas_fraction, N_GAS, T_GAS, r["en"],
+                              r["angle"], r["freq"], r["red_mag"]))
+    sts = [srv.wait(j, 1800.0) for j in ids]
+    w1 = time.perf_counter()
+    rep = srv.report()
+    srv.stop()
+    clk = clocks.stop()
+    done = [s for s in sts if s.state == capi.JOB_DONE]
+    capped = sum(1 for s in done if s.result.capped)
+    lat = [s.end_time - s.submit_time for s in done]
+    real = sum(s.result.real_collisions for s in done)
+    span = max(s.end_time for s in sts) - min(s.submit_time for s in sts)
+    errors = [f"request {i}: status {s.status}: {s.error.decode(errors='replace')}"
+              for i, s in enumerate(sts) if s.state != capi.JOB_DONE]
+    # the plain path, one request after the other, on the first requests
+    torch.cuda.synchronize()
+    k = min(args.plain_requests, len(reqs))
+    p0 = time.perf_counter()
+    real_p = 0.0
+    for r, ps in zip(reqs[:k], sets[:k]):
+        cfg = sweep_config(capi, local, r["ne"], r["seed"], converge=True)
+        cfg.n_phases = 16
+        cfg.max_seconds = args.request_cap_s
+        c = capi.Context(cfg)
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, r["en"], r["angle"], r["freq"], r["red_mag"])
+        real_p += c.solve().real_collisions
+        c.close()
+    p1 = time.perf_counter()
+    real_k = sum(s.result.real_collisions for s in sts[:k] if s.state == capi.JOB_DONE)
+    if rank == 0:
+        value = real / span
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(reqs), "warmup": 0,
+            "ms_per_step": 1e3 * span / len(reqs), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serve_random_mixtures", "requests": len(reqs),
+                       "arrivals": f"Poisson, mean gap {args.arrival_ms} ms", "slots": args.slots,
+                       "mixtures": "1-5 random gases, 10-40 processes each on 100-400-point grids",
+                       "E/N_Td": [1.0, 1000.0], "electrons_range": [1e4, SERVE_MAX_ELECTRONS],
+                       "convergence": f"mean-energy standard error < {SWEEP_ERR:.1%}"},
+            "served": {"p50_s": _percentile(lat, 50), "p99_s": _percentile(lat, 99), "completed": len(done),
+                       "capped": capped, "cap_s": args.request_cap_s,
+                       "failed": len(reqs) - len(done), "errors": errors[:10], "span_s": span,
+                       "intervals": rep.intervals, "busy_s": rep.busy_seconds,
+                       "peak_footprint_gb": rep.peak_footprint_bytes / 1e9},
+            "plain_first_requests": {"requests": k, "value": real_p / (p1 - p0), "unit": UNIT,
+                                     "wall_s": p1 - p0,
+                                     "note": "the same requests solved one after the other with lgpu_solve"},
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def run_gpu_n2(args):
     import torch
 
@@ -680,7 +801,11 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "n2_200td"])
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "n2_200td", "serve"])
+    ap.add_argument("--requests", type=int, default=100, help="serve: requests in the stream")
+    ap.add_argument("--request-cap-s", type=float, default=60.0, help="serve: wall-time cap of one request")
+    ap.add_argument("--slots", type=int, default=64, help="serve: jobs advanced together")
+    ap.add_argument("--plain-requests", type=int, default=16, help="serve: requests also solved one by one")
     ap.add_argument("--electrons", type=int, default=N_ELECTRONS, help="n2_200td only")
     ap.add_argument("--relax", type=int, default=None)
     ap.add_argument("--plain-steps", type=int, default=20, help="sweep: timed plain intervals per condition")
@@ -699,6 +824,8 @@ def main():
         args.relax = 200 if args.workload == "sweep" else 400
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "serve":
+        return run_gpu_serve(args)
     return run_gpu_sweep(args) if args.workload == "sweep" else run_gpu_n2(args)
 
 

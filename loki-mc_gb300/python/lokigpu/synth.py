@@ -203,7 +203,7 @@ def o2_like_gas(seed: int = 3, name: str = "Y2", fraction: float = 1.0, e_max: f
                          att=(4.4, 1.4e-22), fraction=fraction, e_max=e_max)
 
 
-def random_gas(seed: int, name: str, fraction: float) -> Gas:
+def random_gas(seed: int, name: str, fraction: float, e_max: float = 1e3) -> Gas:
     """Request-stream gas: 10-40 processes on a 100-400 point grid."""
     rng = np.random.default_rng(seed)
     n_pts = int(rng.integers(100, 401))
@@ -216,7 +216,7 @@ def random_gas(seed: int, name: str, fraction: float) -> Gas:
                          vib_lo=0.15, vib_hi=0.15 + 0.3 * max(n_vib, 1), n_ele=n_ele,
                          ele_lo=float(rng.uniform(5.0, 8.0)), ele_hi=float(rng.uniform(10.0, 16.0)),
                          ion_thr=float(rng.uniform(12.0, 16.0)), rot_thr=0.002, att=att,
-                         n_points=n_pts, fraction=fraction)
+                         n_points=n_pts, fraction=fraction, e_max=e_max)
 
 
 # ---------------------------------------------------------------------------
