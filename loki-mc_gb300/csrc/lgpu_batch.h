@@ -263,7 +263,7 @@ class Batch {
       if (sl[s].flags & kSlotSample) ns += (N + kBatchSampleChunk - 1) / kBatchSampleChunk;
       if (sl[s].flags & kSlotHist) {
         nh += (N + kBatchHistChunk - 1) / kBatchHistChunk;
-        if (sl[s].hist.cylindrical) nv += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+        if (sl[s].hist.cylindrical && !sl[s].hist.evdf_done) nv += (N + kBatchHistChunk - 1) / kBatchHistChunk;
       }
     }
     ap[n] = na;

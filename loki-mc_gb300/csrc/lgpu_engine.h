@@ -686,6 +686,9 @@ class Engine {
     c.shift_y = (float)shift_[1];
     c.shift_z = (float)shift_[2];
     c.interval = interval_;
+    // in a batch the sample of this interval counts its EVDF in the moment
+    // pass when it will record distributions (grid fixed since the steady state)
+    evdf_fused_ = batch_ && sampling_ && ss_time_ != kNonDef && cylindrical_;
     return LGPU_OK;
   }
 
@@ -896,6 +899,8 @@ class Engine {
     h.inv_ax_step = (float)(1.0 / ax_step_);
     h.max_speed = (float)max_speed_;
     h.evdf = d_evdf_;
+    h.evdf_done = evdf_fused_ ? 1 : 0;
+    evdf_fused_ = false;
     if (batch_) {
       pending_hist_ = h;
       hist_pending_ = true;
@@ -1169,6 +1174,17 @@ class Engine {
     std::memcpy(sl, &slot_, sizeof(*sl));
     sl->ctl = *h_ctl_;
     sl->flags = (have_ion_att_ ? kSlotIonAtt : 0) | (sampling_ ? kSlotSample : 0);
+    if (evdf_fused_) {
+      sl->flags |= kSlotEvdf;
+      HistArgs& v = sl->vhist;
+      v.n_rad = cfg_.n_radial_cells;
+      v.n_ax = cfg_.n_axial_cells;
+      v.inv_rad_step = (float)(1.0 / rad_step_);
+      v.inv_ax_step = (float)(1.0 / ax_step_);
+      v.max_speed = (float)max_speed_;
+      v.evdf = d_evdf_;
+      v.cylindrical = 1;
+    }
     if (hist_pending_) {
       sl->hist = pending_hist_;
       sl->flags |= kSlotHist;
@@ -1522,7 +1538,7 @@ class Engine {
   long long solve_steps_ = 0;
   double pending_dt_ = 0;
   // batch mode
-  bool batch_ = false, hist_pending_ = false;
+  bool batch_ = false, hist_pending_ = false, evdf_fused_ = false;
   BatchSlot slot_{};                            // cached argument blocks of this solve's batch slot
   long long solve_serial_ = 0, slot_built_ = -1;
   cudaStream_t own_stream_ = nullptr;

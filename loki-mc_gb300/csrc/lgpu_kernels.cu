@@ -721,13 +721,21 @@ constexpr int kSampleThreads = 256;
 // Moment sums of electrons begin, begin+step, ... < end into a.moments: per
 // thread in FP32 (a handful of electrons each), FP64 from the warp reduction on.
 // Every thread of the block calls this; s_m is the block's scratch.
+struct NoExtra {
+  __device__ __forceinline__ void operator()(float4) const {}
+};
+
+// `extra` sees every electron's (vx, vy, vz, flag) in the same pass (the
+// batched kernel counts the EVDF with it)
+template <class Extra = NoExtra>
 __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int end, int step,
-                                             double (*s_m)[kMoments]) {
+                                             double (*s_m)[kMoments], Extra extra = Extra()) {
   float m[kMoments];
 #pragma unroll
   for (int k = 0; k < kMoments; ++k) m[k] = 0.0f;
   float e_max = 0.0f;
   auto add = [&](float4 A, float4 B) {
+    extra(B);
     const float e = energy_of(make_float3(B.x, B.y, B.z), a.half_me_over_e);
     e_max = fmaxf(e_max, e);
     const float x = A.x, y = A.y, z = A.z, vx = B.x, vy = B.y, vz = B.z;
@@ -1149,16 +1157,55 @@ __global__ void __launch_bounds__(kHistBThreads) k_hist_b_batch(BatchArgs b) {
   }
 }
 
-// ensemble moments of the sampling slots
-__global__ void __launch_bounds__(kSampleThreads) k_sample_batch(BatchArgs b) {
-  __shared__ double s_m[kSampleThreads / 32][kMoments];
+// Ensemble moments of the sampling slots; for the slots whose sample records
+// distributions (kSlotEvdf) the same pass counts the EVDF (BoltzmannMC.C:
+// 1550-1571; 16-bit counts in shared memory per chunk, global atomics for
+// small chunks), saving its separate pass over the velocities.
+constexpr int kSampleBatchThreads = 512;
+constexpr int kSampleBatchSmem = 80 * 1024;  // EVDF counts, two blocks per SM
+
+__global__ void __launch_bounds__(kSampleBatchThreads) k_sample_batch(BatchArgs b) {
+  __shared__ double s_m[kSampleBatchThreads / 32][kMoments];
+  extern __shared__ unsigned int sm_evdf[];
   const int n_slots = b.hdr->n_slots, total = b.hdr->smp_chunks;
   for (int c = blockIdx.x; c < total; c += gridDim.x) {
     const int slot = slot_of_chunk(b.smp_prefix, n_slots, c);
-    const SampleArgs& a = b.slots[slot].smp;
+    const BatchSlot& sl = b.slots[slot];
+    const SampleArgs& a = sl.smp;
     const int first = (c - b.smp_prefix[slot]) * kBatchSampleChunk;
-    sample_range(a, first + threadIdx.x, min(first + kBatchSampleChunk, a.n), blockDim.x, s_m);
+    const int last = min(first + kBatchSampleChunk, a.n);
+    const bool evdf = (sl.flags & kSlotEvdf) != 0;
+    const HistArgs& h = sl.vhist;
+    const int nV = evdf ? h.n_rad * h.n_ax : 0;
+    const int nVw = (nV + 1) >> 1;
+    const bool v_shared = evdf && last - first >= kHistSharedMin && nVw <= kSampleBatchSmem / 4;
+    if (v_shared)
+      for (int w = threadIdx.x; w < nVw; w += blockDim.x) sm_evdf[w] = 0u;
     __syncthreads();
+    if (evdf) {
+      auto bin = [&](float4 B) {
+        const float v2xy = __fmaf_rn(B.y, B.y, __fmul_rn(B.x, B.x));
+        const int rx = (int)(sqrtf(v2xy) * h.inv_rad_step);
+        const int ry = (int)((B.z + h.max_speed) * h.inv_ax_step);
+        if (rx < h.n_rad && rx >= 0 && ry < h.n_ax && ry >= 0) {
+          const int idx = rx * h.n_ax + ry;
+          if (v_shared) atomicAdd(&sm_evdf[idx >> 1], 1u << ((idx & 1) << 4));
+          else atomicAdd(&h.evdf[idx], 1.0);
+        }
+      };
+      sample_range(a, first + threadIdx.x, last, blockDim.x, s_m, bin);
+    } else {
+      sample_range(a, first + threadIdx.x, last, blockDim.x, s_m);
+    }
+    __syncthreads();
+    if (v_shared) {
+      for (int w = threadIdx.x; w < nVw; w += blockDim.x) {
+        const unsigned int v = sm_evdf[w];
+        if (v & 0xFFFFu) atomicAdd(&h.evdf[2 * w], (double)(v & 0xFFFFu));
+        if ((v >> 16) && 2 * w + 1 < nV) atomicAdd(&h.evdf[2 * w + 1], (double)(v >> 16));
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -1266,7 +1313,7 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
   const int chunks = (a.n + kHistChunk - 1) / kHistChunk;
   k_hist_a<<<chunks, kHistAThreads, kHistASmem, s>>>(a);
-  if (a.cylindrical) k_hist_b<<<chunks, kHistBThreads, kHistBSmem, s>>>(a);
+  if (a.cylindrical && !a.evdf_done) k_hist_b<<<chunks, kHistBThreads, kHistBSmem, s>>>(a);
 }
 
 void launch_pop_control(const PopArgs& a, cudaStream_t s) {
@@ -1282,6 +1329,8 @@ cudaError_t prepare_kernels() {
     e = cudaFuncSetAttribute(k_hist_a_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistASmem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_hist_b_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kHistBSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sample_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kSampleBatchSmem);
   return e;
 }
 
@@ -1313,7 +1362,7 @@ void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStre
   pb.hdr = b.hdr;
   pb.slots = b.slots;
   launch_pop_phases(pb, dim3(kPopBlocksPerSlot, slots), s);
-  k_sample_batch<<<sm_count * 4, kSampleThreads, 0, s>>>(b);
+  k_sample_batch<<<sm_count * 2, kSampleBatchThreads, kSampleBatchSmem, s>>>(b);
   k_batch_gather<<<min(slots, 64), 64, 0, s>>>(b);
 }
 

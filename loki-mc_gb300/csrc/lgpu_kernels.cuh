@@ -146,6 +146,8 @@ struct HistArgs {
   int n_rad, n_ax;                 // EVDF: [n_rad x n_ax]
   float inv_rad_step, inv_ax_step, max_speed;
   double* evdf;
+  int evdf_done;                   // the EVDF of this sample was counted with its moments (batches)
+  int pad;
 };
 void launch_hist(const HistArgs& a, cudaStream_t s);
 
@@ -181,13 +183,17 @@ constexpr int kPopLaunches = 5;
 // Each slot carries the same argument blocks a single-condition launch takes;
 // the kernels split every slot's ensemble into fixed-size chunks and find the
 // slot of a chunk by bisection over exclusive prefix sums of the chunk counts.
-enum SlotFlags : int { kSlotIonAtt = 1, kSlotSample = 2, kSlotHist = 4 };
+// kSlotHist: the previous sample's distributions are tallied at the head of
+// this interval; kSlotEvdf: this interval's sample also counts the EVDF (its
+// grid is fixed from the steady state on, so it needs no re-binning check)
+enum SlotFlags : int { kSlotIonAtt = 1, kSlotSample = 2, kSlotHist = 4, kSlotEvdf = 8 };
 
 struct BatchSlot {
   AdvanceArgs adv;        // adv.ctl points at ctl_dst
   PopArgs pop;
   SampleArgs smp;
-  HistArgs hist;
+  HistArgs hist;          // deferred tallies of the previous sample (kSlotHist)
+  HistArgs vhist;         // EVDF counted with this interval's sample (kSlotEvdf)
   IntervalCtl ctl;        // this interval's values, copied to *ctl_dst by the prep kernel
   IntervalCtl* ctl_dst;
   DevScalars* sc;         // the condition's scalars; the per-interval part is cleared by prep
@@ -209,7 +215,7 @@ struct BatchHeader {
 
 constexpr int kBatchMaxSlots = 1024;
 constexpr int kBatchAdvanceChunk = 4096;   // granularity of the advance's initial spread of blocks over slots
-constexpr int kBatchSampleChunk = 8192;    // electrons per block of the moment sums
+constexpr int kBatchSampleChunk = 32768;   // electrons per block of the moment sums (and EVDF: < 2^16)
 constexpr int kBatchHistChunk = 65535;     // electrons per block of the histograms (16-bit counts)
 
 // Staging layout (host pinned mirror and device copy are identical):
