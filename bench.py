@@ -293,7 +293,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
     stream = torch.cuda.ExternalStream(b.stream(), device=local)
     total_ms = real = null = adv_ms = steps = 0.0
     launches = intervals = 0
-    h2d = d2h = host_ms = secondaries = spilled = 0.0
+    h2d = d2h = host_ms = secondaries = spilled = regrids = 0.0
     real_batch = 0
     coarse = -1
     for _ in range(args.steps):
@@ -317,6 +317,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         host_ms += rep.host_ms
         secondaries += rep.secondaries
         spilled += rep.spilled
+        regrids += rep.regrids
         assert running == len(conds)
         real_batch = rep.real_batch
         coarse = rep.coarse_null_test
@@ -325,7 +326,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         c.close()
     return dict(total_ms=total_ms, real=real, null=null, adv_ms=adv_ms, electron_steps=steps, launches=launches,
                 intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled,
-                real_batch=real_batch, coarse=coarse)
+                real_batch=real_batch, coarse=coarse, regrids=regrids)
 
 
 def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
@@ -543,7 +544,8 @@ def run_gpu_sweep(args):
                        "host_ms_per_step": tb["host_ms"] / args.steps,
                        "secondaries_per_step": tb["secondaries"] / args.steps,
                        "spilled_per_step": tb["spilled"] / args.steps,
-                       "collision_turn_threshold": tb["real_batch"], "coarse_null_test": tb["coarse"]},
+                       "collision_turn_threshold": tb["real_batch"], "coarse_null_test": tb["coarse"],
+                       "regrids_per_step": tb["regrids"] / max(args.steps, 1)},
             "plain": plain, "batched_over_plain": ratio or None, "served": served,
             "accuracy": _accuracy(conds, e2e_b, e2e_p) if (e2e_b and e2e_p) else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

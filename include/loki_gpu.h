@@ -287,6 +287,8 @@ typedef struct lgpu_batch_report {
   double attached;              /* electrons removed by attachment */
   double real_batch;            /* collision-turn threshold in use (0 while it is being tuned) */
   double coarse_null_test;      /* 1: null tests try the block bounds first, 0: not, -1: being tuned */
+  double regrids;               /* energy-grid re-builds, each overlapped with a batched interval the
+                                   context sat out */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);

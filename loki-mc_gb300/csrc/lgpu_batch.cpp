@@ -51,7 +51,7 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
   lgpu::Batch& b = *batch->b;
   const long long i0 = b.intervals_, l0 = b.launches_;
   const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_, r0 = b.real_,
-               n0 = b.null_, hm0 = b.host_ms_, se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_;
+               n0 = b.null_, hm0 = b.host_ms_, se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_, rg0 = b.regrids_;
   const auto t0 = std::chrono::steady_clock::now();
   int rc = LGPU_OK;
   for (int i = 0; i < n && rc == LGPU_OK; ++i) {
@@ -74,6 +74,7 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
+    report->regrids = b.regrids_ - rg0;
     report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
   }
@@ -86,7 +87,7 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
   if (n != (int)b.members_.size()) return b.fail(LGPU_ERR_BAD_ARG, "n must be the number of added contexts");
   const long long i0 = b.intervals_, l0 = b.launches_;
   const double a0 = b.adv_ms_, s0 = b.electron_steps_, u0 = b.h2d_bytes_, d0 = b.d2h_bytes_, hm0 = b.host_ms_,
-               se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_;
+               se0 = b.secondaries_, sp0 = b.spilled_, at0 = b.attached_, rg0 = b.regrids_;
   const auto t0 = std::chrono::steady_clock::now();
   int rc = b.run();
   const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -120,6 +121,7 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->secondaries = b.secondaries_ - se0;
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
+    report->regrids = b.regrids_ - rg0;
     report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
   }

@@ -42,7 +42,7 @@ class Batch {
   long long intervals_ = 0, launches_ = 0;
   double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
   double real_ = 0, null_ = 0;  // collisions of the batched intervals
-  double host_ms_ = 0, secondaries_ = 0, spilled_ = 0, attached_ = 0;
+  double host_ms_ = 0, secondaries_ = 0, spilled_ = 0, attached_ = 0, regrids_ = 0;
 
   // On-line tuning of two scheduling choices of the advance for members whose
   // config leaves the threshold at 0: the collision-turn threshold
@@ -214,25 +214,36 @@ class Batch {
   }
 
   // One synchronisation interval of every running member. Members whose stop
-  // criteria hold (or that fail) finish here; *finished lists them.
+  // criteria hold (or that fail) finish here; *finished lists them. A member
+  // whose energy grid is being re-built (on its own stream, concurrently with
+  // this interval) sits the interval out and goes on at the next step.
   int step(std::vector<int>* finished = nullptr) {
     const auto h0 = std::chrono::steady_clock::now();
-    std::vector<int> go;
+    std::vector<int> go, wait;
     go.reserve(active_.size());
     for (int idx : active_) {
       Member& m = members_[idx];
-      bool done = false;
+      bool done = false, ready = true;
       int rc = m.e->solve_next(&done);
-      if (rc == LGPU_OK && !done) rc = m.e->interval_pre();
+      if (rc == LGPU_OK && !done) rc = m.e->interval_pre(&ready);
       if (rc != LGPU_OK || done) {
         finish(m, rc);
         if (finished) finished->push_back(idx);
+      } else if (!ready) {
+        wait.push_back(idx);
+        ++regrids_;
       } else {
         go.push_back(idx);
       }
     }
     active_ = go;
-    if (go.empty()) return LGPU_OK;
+    active_.insert(active_.end(), wait.begin(), wait.end());
+    if (go.empty()) {
+      // only re-grids in flight: let them finish before the next step
+      for (int idx : wait)
+        if (int rc = members_[idx].e->settle_tables()) return rc;
+      return LGPU_OK;
+    }
     // slots ordered by field branch: one advance launch per branch
     std::stable_sort(go.begin(), go.end(),
                      [&](int a, int b) { return members_[a].e->field_mode() < members_[b].e->field_mode(); });
@@ -337,6 +348,10 @@ class Batch {
         still.push_back(go[s]);
       }
     }
+    // re-grids end within the step that launched them (they ran beside it)
+    for (int idx : wait)
+      if ((rc = members_[idx].e->settle_tables())) return rc;
+    still.insert(still.end(), wait.begin(), wait.end());
     active_ = still;
     const auto h3 = std::chrono::steady_clock::now();
     host_ms_ += 1e3 * (std::chrono::duration<double>(h1 - h0).count() + std::chrono::duration<double>(h3 - h2).count());

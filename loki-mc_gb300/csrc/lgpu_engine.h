@@ -115,6 +115,7 @@ class Engine {
     LGPU_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     LGPU_CU(cudaEventCreate(&ev0_));
     LGPU_CU(cudaEventCreate(&ev1_));
+    LGPU_CU(cudaEventCreateWithFlags(&tables_ev_, cudaEventDisableTiming));
     N_ = (int)cfg_.n_electrons;
     sec_cap_ = std::max(N_, 4096);
     LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
@@ -142,7 +143,8 @@ class Engine {
     coarse_shift_ = 0;
     while (((M_ + (1 << coarse_shift_) - 1) >> coarse_shift_) > kMaxCoarse) ++coarse_shift_;
     n_coarse_ = (M_ + (1 << coarse_shift_) - 1) >> coarse_shift_;
-    h_nu_max_.assign(M_, 0.0);
+    LGPU_CU(cudaMallocHost((void**)&h_nu_max_, (size_t)M_ * sizeof(double)));
+    std::memset(h_nu_max_, 0, (size_t)M_ * sizeof(double));
     const int nEC = cfg_.n_energy_cells;
     LGPU_TRY(dalloc(&d_eedf_, (size_t)nEC));
     LGPU_TRY(dalloc(&d_eedf_per_, (size_t)std::max(cfg_.n_phases, 1) * nEC));
@@ -168,6 +170,9 @@ class Engine {
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_sc_) cudaFreeHost(h_sc_);
+    if (h_nu_max_) cudaFreeHost(h_nu_max_);
+    h_nu_max_ = nullptr;
+    if (tables_ev_) cudaEventDestroy(tables_ev_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -384,7 +389,12 @@ class Engine {
 
   // ------------------------------------------------------------ tables
   // interpolateCrossSections (BoltzmannMC.C:561-615), on the device
-  int build_tables(double max_energy, double* sig64 = nullptr, double* cum64 = nullptr) {
+  // With `async` (a context in a batch) the tables are built on the context's
+  // own stream and the running maximum comes back into pinned memory behind
+  // tables_ev_; the context sits out batched intervals until that event has
+  // completed (settle_tables), so no batched launch reads half-built tables.
+  int build_tables(double max_energy, double* sig64 = nullptr, double* cum64 = nullptr, bool async = false) {
+    LGPU_TRY(settle_tables());
     if (max_energy == max_interp_) return LGPU_OK;
     max_interp_ = max_energy;
     step_ = max_energy / (double)(M_ - 1);
@@ -413,11 +423,28 @@ class Engine {
     a.nu_coarse = d_nu_coarse_;
     a.coarse_shift = coarse_shift_;
     a.n_coarse = n_coarse_;
-    launch_build_tables(a, stream_);
+    cudaStream_t st = async && batch_ ? own_stream_ : stream_;
+    launch_build_tables(a, st);
     launches_ += 3;
-    LGPU_CU(copy(h_nu_max_.data(), d_nu_max_, M_ * sizeof(double), cudaMemcpyDeviceToHost));
-    return sync("build_tables");
+    d2h_bytes_ += (double)M_ * sizeof(double);
+    LGPU_CU(cudaMemcpyAsync(h_nu_max_, d_nu_max_, M_ * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (async) {
+      LGPU_CU(cudaEventRecord(tables_ev_, st));
+      tables_inflight_ = true;
+      return cuda(cudaGetLastError(), "build_tables");
+    }
+    LGPU_CU(cudaStreamSynchronize(st));
+    return cuda(cudaGetLastError(), "build_tables");
   }
+
+  // waits for tables built asynchronously (a no-op once they are done)
+  int settle_tables() {
+    if (!tables_inflight_) return LGPU_OK;
+    tables_inflight_ = false;
+    LGPU_CU(cudaEventSynchronize(tables_ev_));
+    return cuda(cudaGetLastError(), "build_tables");
+  }
+  bool tables_ready() const { return !tables_inflight_ || cudaEventQuery(tables_ev_) != cudaErrorNotReady; }
 
   // maximizationAccelerationEnergy (BoltzmannMC.C:765-802)
   double max_accel_energy(double e0, double dt) const {
@@ -444,12 +471,23 @@ class Engine {
   }
 
   // checkMaxCollisionFrequency (BoltzmannMC.C:716-763)
-  int check_max_frequency(double max_energy_before) {
+  // With `ready` the check returns *ready = false after launching a table
+  // re-grid asynchronously; calling it again once the tables are built
+  // resumes it with the same decisions (max_interp_ now matches maxE).
+  int check_max_frequency(double max_energy_before, bool* ready = nullptr) {
+    LGPU_TRY(settle_tables());
+    if (ready) *ready = true;
     const double thermal = (cfg_.gas_temperature_effect == 1 || cfg_.gas_temperature_effect == 2) ? 10.0 * gas_energy_ : 0.0;
     for (int it = 0; it < 100000; ++it) {
       const double maxE = max_accel_energy(max_energy_before, 10.0 / nu_trial_) + thermal;
       if (maxE > max_interp_ || 2.5 * maxE < max_interp_) {
-        LGPU_TRY(build_tables(2.0 * maxE < emax_elastic_ ? 2.0 * maxE : emax_elastic_));
+        const double target = 2.0 * maxE < emax_elastic_ ? 2.0 * maxE : emax_elastic_;
+        if (ready && target != max_interp_) {
+          LGPU_TRY(build_tables(target, nullptr, nullptr, true));
+          *ready = false;
+          return LGPU_OK;
+        }
+        LGPU_TRY(build_tables(target));
       }
       const int idx = (int)std::fmin(std::ceil(maxE / step_), M_ - 1);
       if (nu_trial_ < h_nu_max_[idx]) {
@@ -665,8 +703,12 @@ class Engine {
 
   // The first half of a synchronisation interval (BoltzmannMC.C:617-688):
   // the trial-frequency check and the interval's control block in h_ctl_.
-  int interval_pre() {
-    LGPU_TRY(check_max_frequency(cur_max_energy_));
+  // In a batch (`ready` given) a table re-grid is launched asynchronously and
+  // *ready = false: the context sits this batched interval out and calls
+  // again at the next one.
+  int interval_pre(bool* ready = nullptr) {
+    LGPU_TRY(check_max_frequency(cur_max_energy_, ready));
+    if (ready && !*ready) return LGPU_OK;
     pending_dt_ = cfg_.sync_x / nu_trial_;
     double phi0 = 0.0, rate = 0.0;
     if (field_.mode == kFieldAC || field_.mode == kFieldACB) {
@@ -1480,7 +1522,7 @@ class Engine {
     max_interp_ = -1.0;
     LGPU_TRY(build_tables(max_energy));
     if (nu_tot) LGPU_CU(copy(nu_tot, d_nu_tot_, M_ * sizeof(double), cudaMemcpyDeviceToHost));
-    if (nu_max) std::copy(h_nu_max_.begin(), h_nu_max_.end(), nu_max);
+    if (nu_max) std::copy(h_nu_max_, h_nu_max_ + M_, nu_max);
     std::vector<float2> pairs((size_t)M_ * stride_);
     if (sig) {
       LGPU_CU(copy(pairs.data(), d_sig_pair_, pairs.size() * sizeof(float2), cudaMemcpyDeviceToHost));
@@ -1509,7 +1551,9 @@ class Engine {
   bool cylindrical_ = true;
   FieldF field_{};
   double max_interp_ = -1, step_ = 0, nu_trial_ = 0;
-  std::vector<double> h_nu_max_;
+  double* h_nu_max_ = nullptr;  // pinned: the asynchronous re-grid reads it back
+  cudaEvent_t tables_ev_ = nullptr;
+  bool tables_inflight_ = false;
   double time_ = 0, ss_time_ = kNonDef;
   uint64_t interval_ = 0;
   double origin_[3] = {0, 0, 0}, shift_[3] = {0, 0, 0};

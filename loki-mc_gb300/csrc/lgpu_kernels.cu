@@ -626,77 +626,112 @@ __device__ double interp_raw(const double* xs, const double* ys, int n, double x
   return __dadd_rn(ys[lo], __dmul_rn(__ddiv_rn(__dsub_rn(x, xs[lo]), dx), __dsub_rn(ys[lo + 1], ys[lo])));
 }
 
-__global__ void k_build_tables(TableBuildArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.M) return;
-  const int P = a.P;
-  const double energy = __dmul_rn((double)i, a.step);
-  double cur = 0.0;
-  for (int p = 0; p < P; ++p) {
-    double value = 0.0;
-    if (a.is_super[p]) {
-      if (energy > a.emin[p] && energy <= a.emax[p]) {
-        const double thr = a.emin[p - 1];
-        const double sg = interp_raw(a.raw_e + a.raw_off[p - 1], a.raw_v + a.raw_off[p - 1], a.raw_len[p - 1],
-                                     __dadd_rn(energy, thr));
-        value = __dmul_rn(__dmul_rn(__dmul_rn(a.superw[p], __dadd_rn(1.0, __ddiv_rn(thr, energy))), sg), a.rel_dens[p]);
-      }
-    } else if (energy >= a.emin[p] && energy <= a.emax[p]) {
-      value = __dmul_rn(interp_raw(a.raw_e + a.raw_off[p], a.raw_v + a.raw_off[p], a.raw_len[p], energy), a.rel_dens[p]);
+// sigma*n of process p at `energy` (a superelastic process reads its
+// inelastic partner's raw table at energy + threshold)
+__device__ double table_value(const TableBuildArgs& a, int p, double energy) {
+  if (a.is_super[p]) {
+    if (energy > a.emin[p] && energy <= a.emax[p]) {
+      const double thr = a.emin[p - 1];
+      const double sg = interp_raw(a.raw_e + a.raw_off[p - 1], a.raw_v + a.raw_off[p - 1], a.raw_len[p - 1],
+                                   __dadd_rn(energy, thr));
+      return __dmul_rn(__dmul_rn(__dmul_rn(a.superw[p], __dadd_rn(1.0, __ddiv_rn(thr, energy))), sg), a.rel_dens[p]);
     }
-    cur = __dadd_rn(cur, value);
-    if (a.sig64) a.sig64[(size_t)i * P + p] = value;
-    if (a.cum64) a.cum64[(size_t)i * P + p] = cur;
-    const size_t k = (size_t)i * a.stride + p;
-    const float vf = (float)value, cf = (float)cur;
-    a.sig_pair[k].x = vf;
-    a.cum_pair[k].x = cf;
-    if (i > 0) {
-      a.sig_pair[k - a.stride].y = vf;
-      a.cum_pair[k - a.stride].y = cf;
-    }
-    if (i == a.M - 1) {
-      a.sig_pair[k].y = vf;
-      a.cum_pair[k].y = cf;
-    }
+  } else if (energy >= a.emin[p] && energy <= a.emax[p]) {
+    return __dmul_rn(interp_raw(a.raw_e + a.raw_off[p], a.raw_v + a.raw_off[p], a.raw_len[p], energy), a.rel_dens[p]);
   }
-  // row padding: a cumulative value no random number reaches, zero rate
-  for (int p = P; p < a.stride; ++p) {
-    const size_t k = (size_t)i * a.stride + p;
-    a.cum_pair[k] = make_float2(3.0e38f, 3.0e38f);
-    a.sig_pair[k] = make_float2(0.0f, 0.0f);
-  }
-  const double kq = 1.6021766208e-19, km = 9.10938356e-31;
-  const double nu = __dmul_rn(cur, __dmul_rn(a.N, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(energy, 2.0), kq), km))));
-  a.nu_tot[i] = nu;
-  a.nu_pair[i].x = (float)nu;
-  if (i > 0) a.nu_pair[i - 1].y = (float)nu;
-  if (i == a.M - 1) a.nu_pair[i].y = (float)nu;
+  return 0.0;
 }
 
-// running maximum of nu_tot (single block)
-__global__ void k_prefix_max(const double* nu_tot, double* nu_max, int M) {
-  __shared__ double s_part[1024];
-  const int t = threadIdx.x, nt = blockDim.x;
-  const int chunk = (M + nt - 1) / nt;
-  const int b = t * chunk, e = min(M, b + chunk);
-  double m = 0.0;
-  for (int i = b; i < e; ++i) m = fmax(nu_tot[i], m);
-  s_part[t] = m;
-  __syncthreads();
-  if (t == 0) {
-    double run = 0.0;
-    for (int k = 0; k < nt; ++k) {
-      const double v = s_part[k];
-      s_part[k] = run;  // exclusive prefix max
-      run = fmax(run, v);
+// One warp per energy row: the lanes interpolate the processes of the row in
+// parallel, then the cumulative row is summed in process order (the order
+// fixes the FP64 rounding) and written as FP32 row pairs.
+constexpr int kTableWarps = 4;
+
+__global__ void __launch_bounds__(32 * kTableWarps) k_build_tables(TableBuildArgs a) {
+  __shared__ double s_val[kTableWarps][kMaxProcesses];
+  __shared__ double s_cum[kTableWarps][kMaxProcesses];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kTableWarps + w;
+  if (i >= a.M) return;  // whole warps
+  const int P = a.P;
+  const double energy = __dmul_rn((double)i, a.step);
+  for (int p = lane; p < P; p += 32) s_val[w][p] = table_value(a, p, energy);
+  __syncwarp();
+  if (lane == 0) {
+    double cur = 0.0;
+    for (int p = 0; p < P; ++p) {
+      cur = __dadd_rn(cur, s_val[w][p]);
+      s_cum[w][p] = cur;
     }
   }
-  __syncthreads();
-  double run = s_part[t];
-  for (int i = b; i < e; ++i) {
-    run = fmax(nu_tot[i], run);
-    nu_max[i] = run;
+  __syncwarp();
+  for (int p = lane; p < a.stride; p += 32) {
+    const size_t k = (size_t)i * a.stride + p;
+    if (p < P) {
+      const double value = s_val[w][p], cur = s_cum[w][p];
+      if (a.sig64) a.sig64[(size_t)i * P + p] = value;
+      if (a.cum64) a.cum64[(size_t)i * P + p] = cur;
+      const float vf = (float)value, cf = (float)cur;
+      a.sig_pair[k].x = vf;
+      a.cum_pair[k].x = cf;
+      if (i > 0) {
+        a.sig_pair[k - a.stride].y = vf;
+        a.cum_pair[k - a.stride].y = cf;
+      }
+      if (i == a.M - 1) {
+        a.sig_pair[k].y = vf;
+        a.cum_pair[k].y = cf;
+      }
+    } else {
+      // row padding: a cumulative value no random number reaches, zero rate
+      a.cum_pair[k] = make_float2(3.0e38f, 3.0e38f);
+      a.sig_pair[k] = make_float2(0.0f, 0.0f);
+    }
+  }
+  if (lane == 0) {
+    const double cur = s_cum[w][P - 1];
+    const double kq = 1.6021766208e-19, km = 9.10938356e-31;
+    const double nu = __dmul_rn(cur, __dmul_rn(a.N, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dmul_rn(energy, 2.0), kq), km))));
+    a.nu_tot[i] = nu;
+    a.nu_pair[i].x = (float)nu;
+    if (i > 0) a.nu_pair[i - 1].y = (float)nu;
+    if (i == a.M - 1) a.nu_pair[i].y = (float)nu;
+  }
+}
+
+// running maximum of nu_tot (one block of 1024 threads, tiles of 1024 rows;
+// max is exact in any order)
+constexpr int kPrefixThreads = 1024;
+
+__global__ void __launch_bounds__(kPrefixThreads) k_prefix_max(const double* nu_tot, double* nu_max, int M) {
+  __shared__ double s_w[kPrefixThreads / 32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  double carry = 0.0;
+  for (int base = 0; base < M; base += kPrefixThreads) {
+    const int i = base + t;
+    double v = i < M ? nu_tot[i] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v = fmax(v, u);
+    }
+    if (lane == 31) s_w[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      double x = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = fmax(x, u);
+      }
+      s_w[lane] = x;
+    }
+    __syncthreads();
+    double r = fmax(carry, v);
+    if (w > 0) r = fmax(r, s_w[w - 1]);
+    if (i < M) nu_max[i] = r;
+    carry = fmax(carry, s_w[kPrefixThreads / 32 - 1]);
+    __syncthreads();
   }
 }
 
@@ -833,9 +868,9 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
   // With the EADF in shared memory the EEDF count of a cell is its EADF row
   // sum, so only electrons outside the cos cells (cos rounding to 1, zero
   // speed) are counted into hE: one shared-memory atomic per electron.
-  for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+  auto bin = [&](float4 B) {
     int c, cy, rx, ry;
-    hist_cells(a, a.state[2 * i + 1], c, cy, rx, ry);
+    hist_cells(a, B, c, cy, rx, ry);
     if (c >= 0 && c < nE) {
       if (a.cylindrical && cy < a.n_cos && cy >= 0) {
         const int idx = c * a.n_cos + cy;
@@ -849,7 +884,19 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
         atomicAdd(&hE[c], 1u);
       }
     }
+  };
+  // four electrons' loads in flight per thread before their counts
+  const int st = blockDim.x;
+  int i = first + threadIdx.x;
+  for (; i + 3 * st < last; i += 4 * st) {
+    const float4 B0 = a.state[2 * i + 1], B1 = a.state[2 * (i + st) + 1];
+    const float4 B2 = a.state[2 * (i + 2 * st) + 1], B3 = a.state[2 * (i + 3 * st) + 1];
+    bin(B0);
+    bin(B1);
+    bin(B2);
+    bin(B3);
   }
+  for (; i < last; i += st) bin(a.state[2 * i + 1]);
   __syncthreads();
   for (int c = threadIdx.x; c < nE; c += blockDim.x) {
     unsigned int h = hE[c];
@@ -1164,7 +1211,7 @@ __global__ void __launch_bounds__(kHistBThreads) k_hist_b_batch(BatchArgs b) {
 constexpr int kSampleBatchThreads = 512;
 constexpr int kSampleBatchSmem = 80 * 1024;  // EVDF counts, two blocks per SM
 
-__global__ void __launch_bounds__(kSampleBatchThreads) k_sample_batch(BatchArgs b) {
+__global__ void __launch_bounds__(kSampleBatchThreads, 2) k_sample_batch(BatchArgs b) {
   __shared__ double s_m[kSampleBatchThreads / 32][kMoments];
   extern __shared__ unsigned int sm_evdf[];
   const int n_slots = b.hdr->n_slots, total = b.hdr->smp_chunks;
@@ -1298,8 +1345,8 @@ void launch_init(const InitArgs& a, cudaStream_t s) {
 }
 
 void launch_build_tables(const TableBuildArgs& a, cudaStream_t s) {
-  k_build_tables<<<blocks_for(a.M, 128), 128, 0, s>>>(a);
-  k_prefix_max<<<1, 1024, 0, s>>>(a.nu_tot, a.nu_max, a.M);
+  k_build_tables<<<blocks_for(a.M, kTableWarps), 32 * kTableWarps, 0, s>>>(a);
+  k_prefix_max<<<1, kPrefixThreads, 0, s>>>(a.nu_tot, a.nu_max, a.M);
   if (a.nu_coarse) k_coarse_max<<<1, kMaxCoarse, 0, s>>>(a.nu_pair, a.M, a.coarse_shift, a.nu_coarse, a.n_coarse);
 }
 
