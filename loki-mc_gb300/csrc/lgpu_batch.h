@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -36,8 +37,8 @@ class Batch {
   char* d_stage_ = nullptr;
   DevScalars* h_gather_ = nullptr;
   DevScalars* d_gather_ = nullptr;
-  cudaGraphExec_t graph_ = nullptr;
-  long long graph_kernels_ = 0;
+  // one instantiated graph per set of launch groups in use (BatchParts)
+  std::map<unsigned, std::pair<cudaGraphExec_t, int>> graphs_;
   // totals since creation
   long long intervals_ = 0, launches_ = 0;
   double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
@@ -115,8 +116,8 @@ class Batch {
       if (m.e && !m.done) m.e->leave_batch();
     members_.clear();
     active_.clear();
-    if (graph_) cudaGraphExecDestroy(graph_);
-    graph_ = nullptr;
+    for (auto& g : graphs_) cudaGraphExecDestroy(g.second.first);
+    graphs_.clear();
     if (d_stage_) cudaFree(d_stage_);
     if (h_stage_) cudaFreeHost(h_stage_);
     if (d_gather_) cudaFree(d_gather_);
@@ -144,24 +145,27 @@ class Batch {
 
   // the kernels of one interval, captured once (their sizes come from the
   // staged header, so one graph serves every interval and every membership)
-  int graph(cudaGraphExec_t* out) {
-    if (!graph_) {
+  int graph(unsigned parts, cudaGraphExec_t* out, int* kernels) {
+    auto it = graphs_.find(parts);
+    if (it == graphs_.end()) {
       cudaGraph_t g;
       int rc;
       if ((rc = cuda(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture"))) return rc;
       const BatchArgs b = args();
-      launch_batch_pre(b, sm_count_, max_slots_, stream_);
+      int n = launch_batch_pre(b, sm_count_, max_slots_, parts, stream_);
       cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
-      launch_batch_advance(b, sm_count_, stream_);
+      n += launch_batch_advance(b, sm_count_, parts, stream_);
       cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
-      launch_batch_post(b, sm_count_, max_slots_, stream_);
+      n += launch_batch_post(b, sm_count_, max_slots_, parts, stream_);
       if ((rc = cuda(cudaStreamEndCapture(stream_, &g), "capture"))) return rc;
-      rc = cuda(cudaGraphInstantiate(&graph_, g, 0), "instantiate");
+      cudaGraphExec_t ge = nullptr;
+      rc = cuda(cudaGraphInstantiate(&ge, g, 0), "instantiate");
       cudaGraphDestroy(g);
       if (rc) return rc;
-      graph_kernels_ = kBatchLaunches;
+      it = graphs_.emplace(parts, std::make_pair(ge, n)).first;
     }
-    *out = graph_;
+    *out = it->second.first;
+    *kernels = it->second.second;
     return LGPU_OK;
   }
 
@@ -255,6 +259,7 @@ class Batch {
     int* vp = hp + (kBatchMaxSlots + 1);
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
     int na = 0, ns = 0, nh = 0, nv = 0;
+    unsigned parts = 0;
     double electrons = 0;
     const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
     for (int s = 0; s < n; ++s) {
@@ -266,6 +271,8 @@ class Batch {
       }
       const int N = e->n_electrons();
       electrons += N;
+      parts |= 1u << e->field_mode();
+      if (sl[s].flags & kSlotIonAtt) parts |= kPartIonAtt;
       ap[s] = na;
       sp[s] = ns;
       hp[s] = nh;
@@ -287,14 +294,17 @@ class Batch {
     hdr->smp_chunks = ns;
     hdr->hist_chunks = nh;
     hdr->hist2_chunks = nv;
+    if (ns) parts |= kPartSample;
+    if (nh) parts |= kPartHistA;
+    if (nv) parts |= kPartHistB;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];
       hdr->mode_slot[m] = s;
     }
     cudaGraphExec_t ge;
-    int rc;
-    if ((rc = graph(&ge))) return rc;
+    int rc, kernels = 0;
+    if ((rc = graph(parts, &ge, &kernels))) return rc;
     const size_t up = batch_slots_offset() + (size_t)n * sizeof(BatchSlot);
     const size_t down = (size_t)n * sizeof(DevScalars);
     if ((rc = cuda(cudaMemcpyAsync(d_stage_, h_stage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
@@ -326,7 +336,7 @@ class Batch {
     }
     electron_steps_ += electrons;
     ++intervals_;
-    launches_ += graph_kernels_;
+    launches_ += kernels;
     h2d_bytes_ += (double)up;
     d2h_bytes_ += (double)down;
     std::vector<int> still;

@@ -581,6 +581,9 @@ __global__ void __launch_bounds__(32) k_advance_drain_batch(BatchArgs b) {
   __shared__ AdvanceArgs s_a;
   const int slot = blockIdx.x;
   if (slot >= b.hdr->n_slots || !(b.slots[slot].flags & kSlotIonAtt)) return;
+  // the warps took their own queues during the advance: only spilled
+  // secondaries are left (the count is final: the advance launches came first)
+  if (*(volatile const int*)b.slots[slot].adv.spill_count == 0) return;
   load_slot_args(&b.slots[slot].adv, &s_a);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1386,31 +1389,49 @@ size_t batch_slots_offset() {
   return (batch_prefix_offset() + 4 * (kBatchMaxSlots + 1) * sizeof(int) + 255) / 256 * 256;
 }
 
-void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
+int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s) {
   const int slots = max(1, min(max_slots, kBatchMaxSlots));
+  int n = 1;
   k_batch_prep<<<(slots + 7) / 8, 256, 0, s>>>(b);
-  k_hist_a_batch<<<sm_count, kHistAThreads, kHistASmem, s>>>(b);
-  k_hist_b_batch<<<sm_count * 2, kHistBThreads, kHistBSmem, s>>>(b);
+  if (parts & kPartHistA) {
+    k_hist_a_batch<<<sm_count, kHistAThreads, kHistASmem, s>>>(b);
+    ++n;
+  }
+  if (parts & kPartHistB) {
+    k_hist_b_batch<<<sm_count * 2, kHistBThreads, kHistBSmem, s>>>(b);
+    ++n;
+  }
+  return n;
 }
 
-void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s) {
+int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s) {
   const int grid = sm_count * kAdvanceBlocksPerSM;
-  k_advance_batch<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(b);
-  k_advance_batch<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(b);
-  k_advance_batch<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(b);
-  k_advance_batch<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(b);
-  k_advance_batch<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(b);
+  int n = 0;
+  if (parts & (1u << kFieldDC)) k_advance_batch<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldAC)) k_advance_batch<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldB)) k_advance_batch<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldECR)) k_advance_batch<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldACB)) k_advance_batch<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  return n;
 }
 
-void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s) {
+int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s) {
   const int slots = max(1, min(max_slots, kBatchMaxSlots));
-  k_advance_drain_batch<<<slots, 32, 0, s>>>(b);
-  PopBatch pb;
-  pb.hdr = b.hdr;
-  pb.slots = b.slots;
-  launch_pop_phases(pb, dim3(kPopBlocksPerSlot, slots), s);
-  k_sample_batch<<<sm_count * 2, kSampleBatchThreads, kSampleBatchSmem, s>>>(b);
+  int n = 1;
+  if (parts & kPartIonAtt) {
+    k_advance_drain_batch<<<slots, 32, 0, s>>>(b);
+    PopBatch pb;
+    pb.hdr = b.hdr;
+    pb.slots = b.slots;
+    launch_pop_phases(pb, dim3(kPopBlocksPerSlot, slots), s);
+    n += 1 + kPopLaunches;
+  }
+  if (parts & kPartSample) {
+    k_sample_batch<<<sm_count * 2, kSampleBatchThreads, kSampleBatchSmem, s>>>(b);
+    ++n;
+  }
   k_batch_gather<<<min(slots, 64), 64, 0, s>>>(b);
+  return n;
 }
 
 void launch_replay_flight(const ReplayFlightArgs& a, cudaStream_t s) {

@@ -236,10 +236,18 @@ size_t batch_slots_offset();    // bytes from the staging start to slots[0]
 //   pre:     slot control blocks and per-interval scalars, deferred histograms
 //   advance: one persistent launch per field mode
 //   post:    drain of spilled secondaries, population control, moments, gather
-void launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
-void launch_batch_advance(const BatchArgs& b, int sm_count, cudaStream_t s);
-void launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, cudaStream_t s);
-constexpr int kBatchLaunches = 16;  // kernels per batched interval
+// `parts` leaves out the launches no slot of the interval needs: bit m (m <
+// kFieldModes) for field mode m, then the flags below. Each returns the
+// kernels it launched.
+enum BatchParts : unsigned {
+  kPartHistA = 1u << 8,   // a slot records its energy distributions
+  kPartHistB = 1u << 9,   // a slot records its velocity distribution in a separate pass
+  kPartSample = 1u << 10, // a slot samples its moments
+  kPartIonAtt = 1u << 11, // a slot has ionization or attachment (drain, population control)
+};
+int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
+int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
+int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 
 // Replay kernels for the parity tests: the production device functions
 // driven by given inputs and recorded uniforms.
