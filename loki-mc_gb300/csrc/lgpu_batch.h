@@ -39,6 +39,7 @@ class Batch {
   DevScalars* d_gather_ = nullptr;
   // one instantiated graph per set of launch groups in use (BatchParts)
   std::map<unsigned, std::pair<cudaGraphExec_t, int>> graphs_;
+  std::vector<std::pair<int, int>> part_s_, part_h_, part_v_;  // (partial chunk size, slot) of each pass
   // totals since creation
   long long intervals_ = 0, launches_ = 0;
   double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
@@ -138,6 +139,9 @@ class Batch {
     b.smp_prefix = b.adv_prefix + (kBatchMaxSlots + 1);
     b.hist_prefix = b.smp_prefix + (kBatchMaxSlots + 1);
     b.hist2_prefix = b.hist_prefix + (kBatchMaxSlots + 1);
+    b.smp_part = b.hist2_prefix + (kBatchMaxSlots + 1);
+    b.hist_part = b.smp_part + kBatchMaxSlots;
+    b.hist2_part = b.hist_part + kBatchMaxSlots;
     b.slots = reinterpret_cast<const BatchSlot*>(d_stage_ + batch_slots_offset());
     b.gather = d_gather_;
     return b;
@@ -257,6 +261,12 @@ class Batch {
     int* sp = ap + (kBatchMaxSlots + 1);
     int* hp = sp + (kBatchMaxSlots + 1);
     int* vp = hp + (kBatchMaxSlots + 1);
+    int* spart = vp + (kBatchMaxSlots + 1);
+    int* hpart = spart + kBatchMaxSlots;
+    int* vpart = hpart + kBatchMaxSlots;
+    part_s_.clear();
+    part_h_.clear();
+    part_v_.clear();
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
     int na = 0, ns = 0, nh = 0, nv = 0;
     unsigned parts = 0;
@@ -278,25 +288,44 @@ class Batch {
       hp[s] = nh;
       vp[s] = nv;
       na += (N + kBatchAdvanceChunk - 1) / kBatchAdvanceChunk;
-      if (sl[s].flags & kSlotSample) ns += (N + kBatchSampleChunk - 1) / kBatchSampleChunk;
+      if (sl[s].flags & kSlotSample) {
+        ns += N / kBatchSampleChunk;
+        if (N % kBatchSampleChunk) part_s_.emplace_back(N % kBatchSampleChunk, s);
+      }
       if (sl[s].flags & kSlotHist) {
-        nh += (N + kBatchHistChunk - 1) / kBatchHistChunk;
-        if (sl[s].hist.cylindrical && !sl[s].hist.evdf_done) nv += (N + kBatchHistChunk - 1) / kBatchHistChunk;
+        nh += N / kBatchHistChunk;
+        if (N % kBatchHistChunk) part_h_.emplace_back(N % kBatchHistChunk, s);
+        if (sl[s].hist.cylindrical && !sl[s].hist.evdf_done) {
+          nv += N / kBatchHistChunk;
+          if (N % kBatchHistChunk) part_v_.emplace_back(N % kBatchHistChunk, s);
+        }
       }
     }
     ap[n] = na;
     sp[n] = ns;
     hp[n] = nh;
     vp[n] = nv;
+    // partial chunks after the full ones, largest first
+    auto order = [](std::vector<std::pair<int, int>>& v, int* dst) {
+      std::stable_sort(v.begin(), v.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+        return x.first > y.first;
+      });
+      for (size_t k = 0; k < v.size(); ++k) dst[k] = v[k].second;
+      return (int)v.size();
+    };
+    const int ps = order(part_s_, spart), ph = order(part_h_, hpart), pv = order(part_v_, vpart);
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_slots = n;
     hdr->adv_chunks = na;
-    hdr->smp_chunks = ns;
-    hdr->hist_chunks = nh;
-    hdr->hist2_chunks = nv;
-    if (ns) parts |= kPartSample;
-    if (nh) parts |= kPartHistA;
-    if (nv) parts |= kPartHistB;
+    hdr->smp_full = ns;
+    hdr->hist_full = nh;
+    hdr->hist2_full = nv;
+    hdr->smp_chunks = ns + ps;
+    hdr->hist_chunks = nh + ph;
+    hdr->hist2_chunks = nv + pv;
+    if (hdr->smp_chunks) parts |= kPartSample;
+    if (hdr->hist_chunks) parts |= kPartHistA;
+    if (hdr->hist2_chunks) parts |= kPartHistB;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];

@@ -837,6 +837,8 @@ constexpr int kHistBThreads = 512;
 constexpr int kHistASmem = 224 * 1024;  // one block per SM
 constexpr int kHistBSmem = 96 * 1024;   // two blocks per SM
 
+__device__ __forceinline__ float radial_speed(float v2xy) { return v2xy > 0.0f ? v2xy * rsqrtf(v2xy) : 0.0f; }
+
 __device__ __forceinline__ void hist_cells(const HistArgs& a, float4 B, int& c, int& cy, int& rx, int& ry) {
   // MathFunctions.C:61-81 (energy) and 106-127 (energy x cos, radial x axial velocity)
   const float v2xy = __fmaf_rn(B.y, B.y, __fmul_rn(B.x, B.x));
@@ -845,10 +847,12 @@ __device__ __forceinline__ void hist_cells(const HistArgs& a, float4 B, int& c, 
   c = (int)(e * a.inv_e_step);
   cy = rx = ry = -1;
   if (a.cylindrical) {
-    const float speed = sqrtf(v2);
-    const float cosang = B.z / speed;
+    // cos and radial speed from the hardware reciprocal square root: a cell
+    // edge moves by a few 1e-7 relative, far below the statistical resolution
+    // of any cell (a zero speed has no angle and stays outside the cos cells)
+    const float cosang = v2 > 0.0f ? B.z * rsqrtf(v2) : 2.0f;
     cy = (int)((cosang + 1.0f) * (0.5f * (float)a.n_cos));
-    rx = (int)(sqrtf(v2xy) * a.inv_rad_step);
+    rx = (int)(radial_speed(v2xy) * a.inv_rad_step);
     ry = (int)((B.z + a.max_speed) * a.inv_ax_step);
   }
 }
@@ -1185,25 +1189,51 @@ __global__ void k_batch_prep(BatchArgs b) {
 }
 
 // distribution tallies of the slots that sample them this interval
+// chunk c of a pass laid out as in BatchHeader: its slot and first electron
+struct ChunkRef {
+  int slot, first;
+};
+__device__ __forceinline__ ChunkRef pass_chunk(const int* full_prefix, const int* part_slot, int n_slots, int n_full,
+                                               int chunk, int c) {
+  ChunkRef r;
+  if (c < n_full) {
+    r.slot = slot_of_chunk(full_prefix, n_slots, c);
+    r.first = (c - full_prefix[r.slot]) * chunk;
+  } else {
+    r.slot = part_slot[c - n_full];
+    r.first = (full_prefix[r.slot + 1] - full_prefix[r.slot]) * chunk;
+  }
+  return r;
+}
+// the chunk a block takes in round r: rounds of gridDim.x chunks, every other
+// round in reverse block order (over a list sorted by size, the blocks' totals
+// differ by about one partial chunk)
+__device__ __forceinline__ int snake_chunk(int r) {
+  const int G = gridDim.x, bx = blockIdx.x;
+  return r * G + ((r & 1) ? G - 1 - bx : bx);
+}
+
 __global__ void __launch_bounds__(kHistAThreads) k_hist_a_batch(BatchArgs b) {
   extern __shared__ unsigned int sm_hist[];
-  const int n_slots = b.hdr->n_slots, total = b.hdr->hist_chunks;
-  for (int c = blockIdx.x; c < total; c += gridDim.x) {
-    const int slot = slot_of_chunk(b.hist_prefix, n_slots, c);
-    const HistArgs& a = b.slots[slot].hist;
-    const int first = (c - b.hist_prefix[slot]) * kHistChunk;
-    hist_chunk_a(a, first, min(first + kHistChunk, a.n), sm_hist, kHistASmem / 4);
+  const int n_slots = b.hdr->n_slots, total = b.hdr->hist_chunks, n_full = b.hdr->hist_full;
+  for (int r = 0; r * (int)gridDim.x < total; ++r) {
+    const int c = snake_chunk(r);
+    if (c >= total) continue;
+    const ChunkRef k = pass_chunk(b.hist_prefix, b.hist_part, n_slots, n_full, kHistChunk, c);
+    const HistArgs& a = b.slots[k.slot].hist;
+    hist_chunk_a(a, k.first, min(k.first + kHistChunk, a.n), sm_hist, kHistASmem / 4);
   }
 }
 
 __global__ void __launch_bounds__(kHistBThreads) k_hist_b_batch(BatchArgs b) {
   extern __shared__ unsigned int sm_hist[];
-  const int n_slots = b.hdr->n_slots, total = b.hdr->hist2_chunks;
-  for (int c = blockIdx.x; c < total; c += gridDim.x) {
-    const int slot = slot_of_chunk(b.hist2_prefix, n_slots, c);
-    const HistArgs& a = b.slots[slot].hist;
-    const int first = (c - b.hist2_prefix[slot]) * kHistChunk;
-    hist_chunk_b(a, first, min(first + kHistChunk, a.n), sm_hist, kHistBSmem / 4);
+  const int n_slots = b.hdr->n_slots, total = b.hdr->hist2_chunks, n_full = b.hdr->hist2_full;
+  for (int r = 0; r * (int)gridDim.x < total; ++r) {
+    const int c = snake_chunk(r);
+    if (c >= total) continue;
+    const ChunkRef k = pass_chunk(b.hist2_prefix, b.hist2_part, n_slots, n_full, kHistChunk, c);
+    const HistArgs& a = b.slots[k.slot].hist;
+    hist_chunk_b(a, k.first, min(k.first + kHistChunk, a.n), sm_hist, kHistBSmem / 4);
   }
 }
 
@@ -1217,12 +1247,14 @@ constexpr int kSampleBatchSmem = 80 * 1024;  // EVDF counts, two blocks per SM
 __global__ void __launch_bounds__(kSampleBatchThreads, 2) k_sample_batch(BatchArgs b) {
   __shared__ double s_m[kSampleBatchThreads / 32][kMoments];
   extern __shared__ unsigned int sm_evdf[];
-  const int n_slots = b.hdr->n_slots, total = b.hdr->smp_chunks;
-  for (int c = blockIdx.x; c < total; c += gridDim.x) {
-    const int slot = slot_of_chunk(b.smp_prefix, n_slots, c);
-    const BatchSlot& sl = b.slots[slot];
+  const int n_slots = b.hdr->n_slots, total = b.hdr->smp_chunks, n_full = b.hdr->smp_full;
+  for (int r = 0; r * (int)gridDim.x < total; ++r) {
+    const int c = snake_chunk(r);
+    if (c >= total) continue;
+    const ChunkRef k = pass_chunk(b.smp_prefix, b.smp_part, n_slots, n_full, kBatchSampleChunk, c);
+    const BatchSlot& sl = b.slots[k.slot];
     const SampleArgs& a = sl.smp;
-    const int first = (c - b.smp_prefix[slot]) * kBatchSampleChunk;
+    const int first = k.first;
     const int last = min(first + kBatchSampleChunk, a.n);
     const bool evdf = (sl.flags & kSlotEvdf) != 0;
     const HistArgs& h = sl.vhist;
@@ -1235,7 +1267,7 @@ __global__ void __launch_bounds__(kSampleBatchThreads, 2) k_sample_batch(BatchAr
     if (evdf) {
       auto bin = [&](float4 B) {
         const float v2xy = __fmaf_rn(B.y, B.y, __fmul_rn(B.x, B.x));
-        const int rx = (int)(sqrtf(v2xy) * h.inv_rad_step);
+        const int rx = (int)(radial_speed(v2xy) * h.inv_rad_step);
         const int ry = (int)((B.z + h.max_speed) * h.inv_ax_step);
         if (rx < h.n_rad && rx >= 0 && ry < h.n_ax && ry >= 0) {
           const int idx = rx * h.n_ax + ry;
@@ -1386,7 +1418,7 @@ cudaError_t prepare_kernels() {
 
 size_t batch_prefix_offset() { return (sizeof(BatchHeader) + 15) / 16 * 16; }
 size_t batch_slots_offset() {
-  return (batch_prefix_offset() + 4 * (kBatchMaxSlots + 1) * sizeof(int) + 255) / 256 * 256;
+  return (batch_prefix_offset() + (4 * (kBatchMaxSlots + 1) + 3 * kBatchMaxSlots) * sizeof(int) + 255) / 256 * 256;
 }
 
 int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s) {

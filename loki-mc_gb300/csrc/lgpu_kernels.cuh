@@ -211,11 +211,15 @@ struct BatchHeader {
   int mode_chunk[kFieldModes + 1];          // first advance chunk of each mode's slots
   int mode_slot[kFieldModes + 1];           // first slot of each mode
   int hist2_chunks;                         // velocity-distribution chunks (cylindrical slots)
+  // the moment and distribution passes list each slot's full chunks first
+  // (prefix over slots) and then one partial chunk per slot, largest first,
+  // so that the blocks' static shares of the list come out even
+  int smp_full, hist_full, hist2_full;
 };
 
 constexpr int kBatchMaxSlots = 1024;
 constexpr int kBatchAdvanceChunk = 4096;   // granularity of the advance's initial spread of blocks over slots
-constexpr int kBatchSampleChunk = 32768;   // electrons per block of the moment sums (and EVDF: < 2^16)
+constexpr int kBatchSampleChunk = 65535;   // electrons per block of the moment sums (and EVDF: < 2^16)
 constexpr int kBatchHistChunk = 65535;     // electrons per block of the histograms (16-bit counts)
 
 // Staging layout (host pinned mirror and device copy are identical):
@@ -225,9 +229,12 @@ struct BatchArgs {
   BatchHeader* hdr;
   const BatchSlot* slots;
   const int* adv_prefix;
-  const int* smp_prefix;
+  const int* smp_prefix;    // full chunks before each slot
   const int* hist_prefix;   // energy and energy-angle distributions
   const int* hist2_prefix;  // velocity distribution (cylindrical slots)
+  const int* smp_part;      // slots with a partial chunk, largest partial first
+  const int* hist_part;
+  const int* hist2_part;
   DevScalars* gather;       // [kBatchMaxSlots]: each slot's scalars after the interval
 };
 size_t batch_prefix_offset();   // bytes from the staging start to adv_prefix
