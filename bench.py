@@ -67,9 +67,9 @@ N_ELECTRONS = 1_000_000
 DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch), from
-# one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 852.6 MB
-# read + 586.6 MB written for 1.98e7 electrons
-SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (852.604928e6 + 586.584320e6) / 19795598
+# one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 804.1 MB
+# read + 539.5 MB written for 1.98e7 electrons
+SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (804.066304e6 + 539.468800e6) / 19795598
 
 # sweep workload
 SWEEP_POINTS = 64
