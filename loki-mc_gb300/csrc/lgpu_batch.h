@@ -35,9 +35,13 @@ class Batch {
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   char* h_stage_ = nullptr;
   char* d_stage_ = nullptr;
+  char* h_hstage_ = nullptr;  // the distribution passes' staging (same layout)
+  char* d_hstage_ = nullptr;
   DevScalars* h_gather_ = nullptr;
   DevScalars* d_gather_ = nullptr;
-  // one instantiated graph per set of launch groups in use (BatchParts)
+  // one instantiated graph per set of launch groups in use (BatchParts; the
+  // distribution passes' graphs carry kGraphHist)
+  static constexpr unsigned kGraphHist = 1u << 16;
   std::map<unsigned, std::pair<cudaGraphExec_t, int>> graphs_;
   std::vector<std::pair<int, int>> part_s_, part_h_, part_v_;  // (partial chunk size, slot) of each pass
   // totals since creation
@@ -105,6 +109,10 @@ class Batch {
     if ((rc = cuda(cudaMalloc((void**)&d_stage_, sb), "cudaMalloc"))) return rc;
     std::memset(h_stage_, 0, sb);
     if ((rc = cuda(cudaMemsetAsync(d_stage_, 0, sb, stream_), "memset"))) return rc;
+    if ((rc = cuda(cudaMallocHost((void**)&h_hstage_, sb), "cudaMallocHost"))) return rc;
+    if ((rc = cuda(cudaMalloc((void**)&d_hstage_, sb), "cudaMalloc"))) return rc;
+    std::memset(h_hstage_, 0, sb);
+    if ((rc = cuda(cudaMemsetAsync(d_hstage_, 0, sb, stream_), "memset"))) return rc;
     if ((rc = cuda(cudaMallocHost((void**)&h_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMallocHost")))
       return rc;
     if ((rc = cuda(cudaMalloc((void**)&d_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMalloc"))) return rc;
@@ -121,6 +129,9 @@ class Batch {
     graphs_.clear();
     if (d_stage_) cudaFree(d_stage_);
     if (h_stage_) cudaFreeHost(h_stage_);
+    if (d_hstage_) cudaFree(d_hstage_);
+    if (h_hstage_) cudaFreeHost(h_hstage_);
+    d_hstage_ = h_hstage_ = nullptr;
     if (d_gather_) cudaFree(d_gather_);
     if (h_gather_) cudaFreeHost(h_gather_);
     d_stage_ = h_stage_ = nullptr;
@@ -132,17 +143,17 @@ class Batch {
     stream_ = nullptr;
   }
 
-  BatchArgs args() const {
+  BatchArgs args(char* stage) const {
     BatchArgs b{};
-    b.hdr = reinterpret_cast<BatchHeader*>(d_stage_);
-    b.adv_prefix = reinterpret_cast<const int*>(d_stage_ + batch_prefix_offset());
+    b.hdr = reinterpret_cast<BatchHeader*>(stage);
+    b.adv_prefix = reinterpret_cast<const int*>(stage + batch_prefix_offset());
     b.smp_prefix = b.adv_prefix + (kBatchMaxSlots + 1);
     b.hist_prefix = b.smp_prefix + (kBatchMaxSlots + 1);
     b.hist2_prefix = b.hist_prefix + (kBatchMaxSlots + 1);
     b.smp_part = b.hist2_prefix + (kBatchMaxSlots + 1);
     b.hist_part = b.smp_part + kBatchMaxSlots;
     b.hist2_part = b.hist_part + kBatchMaxSlots;
-    b.slots = reinterpret_cast<const BatchSlot*>(d_stage_ + batch_slots_offset());
+    b.slots = reinterpret_cast<const BatchSlot*>(stage + batch_slots_offset());
     b.gather = d_gather_;
     return b;
   }
@@ -155,12 +166,17 @@ class Batch {
       cudaGraph_t g;
       int rc;
       if ((rc = cuda(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture"))) return rc;
-      const BatchArgs b = args();
-      int n = launch_batch_pre(b, sm_count_, max_slots_, parts, stream_);
-      cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
-      n += launch_batch_advance(b, sm_count_, parts, stream_);
-      cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
-      n += launch_batch_post(b, sm_count_, max_slots_, parts, stream_);
+      int n = 0;
+      if (parts & kGraphHist) {
+        n = launch_batch_hist(args(d_hstage_), sm_count_, parts, stream_);
+      } else {
+        const BatchArgs b = args(d_stage_);
+        n = launch_batch_pre(b, sm_count_, max_slots_, parts, stream_);
+        cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
+        n += launch_batch_advance(b, sm_count_, parts, stream_);
+        cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
+        n += launch_batch_post(b, sm_count_, max_slots_, parts, stream_);
+      }
       if ((rc = cuda(cudaStreamEndCapture(stream_, &g), "capture"))) return rc;
       cudaGraphExec_t ge = nullptr;
       rc = cuda(cudaGraphInstantiate(&ge, g, 0), "instantiate");
@@ -227,6 +243,9 @@ class Batch {
   // this interval) sits the interval out and goes on at the next step.
   int step(std::vector<int>* finished = nullptr) {
     const auto h0 = std::chrono::steady_clock::now();
+    // the previous samples' distribution passes first: the host work below
+    // (stop criteria, trial frequencies, staging) runs while they do
+    if (int rc = launch_pending_hists()) return rc;
     std::vector<int> go, wait;
     go.reserve(active_.size());
     for (int idx : active_) {
@@ -259,16 +278,10 @@ class Batch {
     auto* hdr = reinterpret_cast<BatchHeader*>(h_stage_);
     int* ap = reinterpret_cast<int*>(h_stage_ + batch_prefix_offset());
     int* sp = ap + (kBatchMaxSlots + 1);
-    int* hp = sp + (kBatchMaxSlots + 1);
-    int* vp = hp + (kBatchMaxSlots + 1);
-    int* spart = vp + (kBatchMaxSlots + 1);
-    int* hpart = spart + kBatchMaxSlots;
-    int* vpart = hpart + kBatchMaxSlots;
+    int* spart = sp + 3 * (kBatchMaxSlots + 1);  // after the two distribution prefixes (other staging)
     part_s_.clear();
-    part_h_.clear();
-    part_v_.clear();
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
-    int na = 0, ns = 0, nh = 0, nv = 0;
+    int na = 0, ns = 0;
     unsigned parts = 0;
     double electrons = 0;
     const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
@@ -285,47 +298,21 @@ class Batch {
       if (sl[s].flags & kSlotIonAtt) parts |= kPartIonAtt;
       ap[s] = na;
       sp[s] = ns;
-      hp[s] = nh;
-      vp[s] = nv;
       na += (N + kBatchAdvanceChunk - 1) / kBatchAdvanceChunk;
       if (sl[s].flags & kSlotSample) {
         ns += N / kBatchSampleChunk;
         if (N % kBatchSampleChunk) part_s_.emplace_back(N % kBatchSampleChunk, s);
       }
-      if (sl[s].flags & kSlotHist) {
-        nh += N / kBatchHistChunk;
-        if (N % kBatchHistChunk) part_h_.emplace_back(N % kBatchHistChunk, s);
-        if (sl[s].hist.cylindrical && !sl[s].hist.evdf_done) {
-          nv += N / kBatchHistChunk;
-          if (N % kBatchHistChunk) part_v_.emplace_back(N % kBatchHistChunk, s);
-        }
-      }
     }
     ap[n] = na;
     sp[n] = ns;
-    hp[n] = nh;
-    vp[n] = nv;
-    // partial chunks after the full ones, largest first
-    auto order = [](std::vector<std::pair<int, int>>& v, int* dst) {
-      std::stable_sort(v.begin(), v.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
-        return x.first > y.first;
-      });
-      for (size_t k = 0; k < v.size(); ++k) dst[k] = v[k].second;
-      return (int)v.size();
-    };
-    const int ps = order(part_s_, spart), ph = order(part_h_, hpart), pv = order(part_v_, vpart);
+    const int ps = order_parts(part_s_, spart);
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_slots = n;
     hdr->adv_chunks = na;
     hdr->smp_full = ns;
-    hdr->hist_full = nh;
-    hdr->hist2_full = nv;
     hdr->smp_chunks = ns + ps;
-    hdr->hist_chunks = nh + ph;
-    hdr->hist2_chunks = nv + pv;
     if (hdr->smp_chunks) parts |= kPartSample;
-    if (hdr->hist_chunks) parts |= kPartHistA;
-    if (hdr->hist2_chunks) parts |= kPartHistB;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];
@@ -394,6 +381,65 @@ class Batch {
     active_ = still;
     const auto h3 = std::chrono::steady_clock::now();
     host_ms_ += 1e3 * (std::chrono::duration<double>(h1 - h0).count() + std::chrono::duration<double>(h3 - h2).count());
+    return LGPU_OK;
+  }
+
+  // partial chunks after the full ones, largest first: their slots into dst
+  static int order_parts(std::vector<std::pair<int, int>>& v, int* dst) {
+    std::stable_sort(v.begin(), v.end(),
+                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first > y.first; });
+    for (size_t k = 0; k < v.size(); ++k) dst[k] = v[k].second;
+    return (int)v.size();
+  }
+
+  // The deferred distribution tallies of the running members' last samples
+  // (EEDF, EADF and, before the velocity grid is fixed, EVDF), staged in the
+  // second staging area and launched as their own graph on the batch stream,
+  // ahead of the interval that would otherwise advance the ensemble first.
+  int launch_pending_hists() {
+    auto* hdr = reinterpret_cast<BatchHeader*>(h_hstage_);
+    int* hp = reinterpret_cast<int*>(h_hstage_ + batch_prefix_offset()) + 2 * (kBatchMaxSlots + 1);
+    int* vp = hp + (kBatchMaxSlots + 1);
+    int* hpart = vp + (kBatchMaxSlots + 1) + kBatchMaxSlots;
+    int* vpart = hpart + kBatchMaxSlots;
+    auto* sl = reinterpret_cast<BatchSlot*>(h_hstage_ + batch_slots_offset());
+    part_h_.clear();
+    part_v_.clear();
+    int n = 0, nh = 0, nv = 0;
+    for (int idx : active_) {
+      HistArgs h;
+      if (!members_[idx].e->take_pending_hist(&h)) continue;
+      sl[n].hist = h;
+      const int N = h.n;
+      hp[n] = nh;
+      vp[n] = nv;
+      nh += N / kBatchHistChunk;
+      if (N % kBatchHistChunk) part_h_.emplace_back(N % kBatchHistChunk, n);
+      if (h.cylindrical && !h.evdf_done) {
+        nv += N / kBatchHistChunk;
+        if (N % kBatchHistChunk) part_v_.emplace_back(N % kBatchHistChunk, n);
+      }
+      ++n;
+    }
+    if (n == 0) return LGPU_OK;
+    hp[n] = nh;
+    vp[n] = nv;
+    const int ph = order_parts(part_h_, hpart), pv = order_parts(part_v_, vpart);
+    std::memset(hdr, 0, sizeof(BatchHeader));
+    hdr->n_slots = n;
+    hdr->hist_full = nh;
+    hdr->hist2_full = nv;
+    hdr->hist_chunks = nh + ph;
+    hdr->hist2_chunks = nv + pv;
+    const unsigned parts = kGraphHist | (hdr->hist_chunks ? kPartHistA : 0u) | (hdr->hist2_chunks ? kPartHistB : 0u);
+    cudaGraphExec_t ge;
+    int rc, kernels = 0;
+    if ((rc = graph(parts, &ge, &kernels))) return rc;
+    const size_t up = batch_slots_offset() + (size_t)n * sizeof(BatchSlot);
+    if ((rc = cuda(cudaMemcpyAsync(d_hstage_, h_hstage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
+    if ((rc = cuda(cudaGraphLaunch(ge, stream_), "graph launch"))) return rc;
+    launches_ += kernels;
+    h2d_bytes_ += (double)up;
     return LGPU_OK;
   }
 

@@ -1227,11 +1227,14 @@ class Engine {
       v.evdf = d_evdf_;
       v.cylindrical = 1;
     }
-    if (hist_pending_) {
-      sl->hist = pending_hist_;
-      sl->flags |= kSlotHist;
-      hist_pending_ = false;
-    }
+  }
+  // the deferred tallies of the last sample, handed to the batch's
+  // distribution passes (false when there are none)
+  bool take_pending_hist(HistArgs* h) {
+    if (!hist_pending_) return false;
+    *h = pending_hist_;
+    hist_pending_ = false;
+    return true;
   }
   int field_mode() const { return field_.mode; }
 

@@ -1423,8 +1423,12 @@ size_t batch_slots_offset() {
 
 int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s) {
   const int slots = max(1, min(max_slots, kBatchMaxSlots));
-  int n = 1;
   k_batch_prep<<<(slots + 7) / 8, 256, 0, s>>>(b);
+  return 1;
+}
+
+int launch_batch_hist(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s) {
+  int n = 0;
   if (parts & kPartHistA) {
     k_hist_a_batch<<<sm_count, kHistAThreads, kHistASmem, s>>>(b);
     ++n;

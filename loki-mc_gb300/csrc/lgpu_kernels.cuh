@@ -183,16 +183,15 @@ constexpr int kPopLaunches = 5;
 // Each slot carries the same argument blocks a single-condition launch takes;
 // the kernels split every slot's ensemble into fixed-size chunks and find the
 // slot of a chunk by bisection over exclusive prefix sums of the chunk counts.
-// kSlotHist: the previous sample's distributions are tallied at the head of
-// this interval; kSlotEvdf: this interval's sample also counts the EVDF (its
-// grid is fixed from the steady state on, so it needs no re-binning check)
-enum SlotFlags : int { kSlotIonAtt = 1, kSlotSample = 2, kSlotHist = 4, kSlotEvdf = 8 };
+// kSlotEvdf: this interval's sample also counts the EVDF (its grid is fixed
+// from the steady state on, so it needs no re-binning check)
+enum SlotFlags : int { kSlotIonAtt = 1, kSlotSample = 2, kSlotEvdf = 8 };
 
 struct BatchSlot {
   AdvanceArgs adv;        // adv.ctl points at ctl_dst
   PopArgs pop;
   SampleArgs smp;
-  HistArgs hist;          // deferred tallies of the previous sample (kSlotHist)
+  HistArgs hist;          // distribution staging only: the deferred tallies of a previous sample
   HistArgs vhist;         // EVDF counted with this interval's sample (kSlotEvdf)
   IntervalCtl ctl;        // this interval's values, copied to *ctl_dst by the prep kernel
   IntervalCtl* ctl_dst;
@@ -240,9 +239,13 @@ struct BatchArgs {
 size_t batch_prefix_offset();   // bytes from the staging start to adv_prefix
 size_t batch_slots_offset();    // bytes from the staging start to slots[0]
 // One batched interval is three launch groups on one stream:
-//   pre:     slot control blocks and per-interval scalars, deferred histograms
+//   pre:     slot control blocks and per-interval scalars
 //   advance: one persistent launch per field mode
 //   post:    drain of spilled secondaries, population control, moments, gather
+// ahead of them, from a second staging area of the same layout, the
+// distribution passes of the previous interval's samples (`hist` of each
+// slot), launched before the host prepares the interval so that its work
+// runs beside them.
 // `parts` leaves out the launches no slot of the interval needs: bit m (m <
 // kFieldModes) for field mode m, then the flags below. Each returns the
 // kernels it launched.
@@ -253,6 +256,7 @@ enum BatchParts : unsigned {
   kPartIonAtt = 1u << 11, // a slot has ionization or attachment (drain, population control)
 };
 int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
+int launch_batch_hist(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
 int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
 int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 
