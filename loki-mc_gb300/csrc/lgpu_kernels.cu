@@ -559,17 +559,24 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
     __syncthreads();  // every warp is done with the slot
     block_flush(s_a, sh, tl, lane, wid);
     __syncthreads();  // the flush has read the shared tallies and arguments
-    if (threadIdx.x == 0) {
+    // the next slot of the branch with electrons left, in rotation order from
+    // this one: warp 0 checks 32 slots' counters per round
+    if (wid == 0) {
+      const int cnt = s1 - s0;
       int nxt = -1;
-      for (int k = 1; k <= s1 - s0; ++k) {
-        const int s = s0 + (slot - s0 + k) % (s1 - s0);
-        const AdvanceArgs& o = b.slots[s].adv;
-        if (*(volatile int*)o.work_counter < o.n) {
-          nxt = s;
-          break;
+      for (int base = 1; base <= cnt && nxt < 0; base += 32) {
+        const int k = base + lane;
+        int s = -1;
+        bool left = false;
+        if (k <= cnt) {
+          s = s0 + (slot - s0 + k) % cnt;
+          const AdvanceArgs& o = b.slots[s].adv;
+          left = *(volatile int*)o.work_counter < o.n;
         }
+        const unsigned m = __ballot_sync(0xffffffffu, left);
+        if (m) nxt = __shfl_sync(0xffffffffu, s, __ffs(m) - 1);
       }
-      s_slot = nxt;
+      if (lane == 0) s_slot = nxt;
     }
     __syncthreads();
   }
