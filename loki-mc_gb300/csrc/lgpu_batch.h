@@ -37,8 +37,8 @@ class Batch {
   char* d_stage_ = nullptr;
   char* h_hstage_ = nullptr;  // the distribution passes' staging (same layout)
   char* d_hstage_ = nullptr;
-  DevScalars* h_gather_ = nullptr;
-  DevScalars* d_gather_ = nullptr;
+  DevScalars* h_gather_ = nullptr;  // mapped pinned memory: the gather kernel writes it directly
+  DevScalars* d_gather_ = nullptr;  // its device address
   // one instantiated graph per set of launch groups in use (BatchParts; the
   // distribution passes' graphs carry kGraphHist)
   static constexpr unsigned kGraphHist = 1u << 16;
@@ -113,9 +113,10 @@ class Batch {
     if ((rc = cuda(cudaMalloc((void**)&d_hstage_, sb), "cudaMalloc"))) return rc;
     std::memset(h_hstage_, 0, sb);
     if ((rc = cuda(cudaMemsetAsync(d_hstage_, 0, sb, stream_), "memset"))) return rc;
-    if ((rc = cuda(cudaMallocHost((void**)&h_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMallocHost")))
+    if ((rc = cuda(cudaHostAlloc((void**)&h_gather_, (size_t)max_slots * sizeof(DevScalars), cudaHostAllocMapped),
+                   "cudaHostAlloc")))
       return rc;
-    if ((rc = cuda(cudaMalloc((void**)&d_gather_, (size_t)max_slots * sizeof(DevScalars)), "cudaMalloc"))) return rc;
+    if ((rc = cuda(cudaHostGetDevicePointer((void**)&d_gather_, h_gather_, 0), "cudaHostGetDevicePointer"))) return rc;
     return cuda(cudaStreamSynchronize(stream_), "init");
   }
 
@@ -132,7 +133,6 @@ class Batch {
     if (d_hstage_) cudaFree(d_hstage_);
     if (h_hstage_) cudaFreeHost(h_hstage_);
     d_hstage_ = h_hstage_ = nullptr;
-    if (d_gather_) cudaFree(d_gather_);
     if (h_gather_) cudaFreeHost(h_gather_);
     d_stage_ = h_stage_ = nullptr;
     d_gather_ = h_gather_ = nullptr;
@@ -325,7 +325,6 @@ class Batch {
     const size_t down = (size_t)n * sizeof(DevScalars);
     if ((rc = cuda(cudaMemcpyAsync(d_stage_, h_stage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
     if ((rc = cuda(cudaGraphLaunch(ge, stream_), "graph launch"))) return rc;
-    if ((rc = cuda(cudaMemcpyAsync(h_gather_, d_gather_, down, cudaMemcpyDeviceToHost, stream_), "gather"))) return rc;
     const auto h1 = std::chrono::steady_clock::now();
     if ((rc = cuda(cudaStreamSynchronize(stream_), "batched interval"))) return rc;
     const auto h2 = std::chrono::steady_clock::now();
