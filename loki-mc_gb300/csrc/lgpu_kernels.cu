@@ -1018,149 +1018,233 @@ __device__ __forceinline__ float energy4(float4 B, float hme) { return energy_of
 //  (4) the listed secondaries move into the removed slots; removal marks are
 //      cleared, so the bitmap is zero again.
 constexpr int kPopThreads = 256;
-constexpr int kPopBlocks = 64;           // blocks per slot, single condition
-constexpr int kPopBlocksPerSlot = 48;    // blocks per slot, batches
+constexpr int kPopBlocks = 64;           // blocks, single condition
+constexpr int kPopBlocksPerSM = 2;       // blocks per SM, batches
 
 // one condition, arguments by value
 struct PopOne {
   PopArgs a;
+  __device__ int count() const { return 1; }
   __device__ const PopArgs* get(int s) const { return s == 0 ? &a : nullptr; }
 };
 // the slots of a batch that ionize or attach
 struct PopBatch {
   const BatchHeader* hdr;
   const BatchSlot* slots;
+  __device__ int count() const { return hdr->n_slots; }
   __device__ const PopArgs* get(int s) const {
     return (s < hdr->n_slots && (slots[s].flags & kSlotIonAtt)) ? &slots[s].pop : nullptr;
   }
 };
 
-__device__ __forceinline__ int pop_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ int pop_stride() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ int pop_sec_total(const PopArgs& a) { return min(*a.sec_count, a.sec_cap); }
 __device__ __forceinline__ bool claimed(const unsigned int* claim, int i) { return (claim[i >> 5] >> (i & 31)) & 1u; }
 
+// Each phase is a list of items per slot (its length from the slot's counts
+// as the previous phases left them). The grid works through all slots' items
+// in 32-item warp chunks, so a warp's lanes always belong to one slot (the
+// warp-aggregated appends and growth sums stay within it).
+struct PopPlan {
+  int pre[kBatchMaxSlots + 1];  // exclusive prefix of the slots' chunk counts
+  int items[kBatchMaxSlots];
+  int warp[kPopThreads / 32];
+};
+
+// exclusive block-wide prefix sum of v (every thread calls it); *total = the sum
+__device__ __forceinline__ int block_exclusive_sum(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) s_warp[lane] = w;
+  }
+  __syncthreads();
+  const int off = wid ? s_warp[wid - 1] : 0;
+  *total = s_warp[nw - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+// the phase's item counts and chunk prefix in shared memory; returns the chunks
+template <class Src, class Items>
+__device__ __forceinline__ int pop_plan(const Src& src, int n, Items items, PopPlan& pl) {
+  int carry = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int s = base + threadIdx.x;
+    int k = 0;
+    if (s < n) {
+      const PopArgs* ap = src.get(s);
+      k = ap ? max(items(*ap), 0) : 0;
+      pl.items[s] = k;
+    }
+    int tot = 0;
+    const int ex = block_exclusive_sum((k + 31) >> 5, pl.warp, &tot);
+    if (s < n) pl.pre[s] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) pl.pre[n] = carry;
+  __syncthreads();
+  return carry;
+}
+
+// body(a, i) for every item i of every slot
+template <class Src, class Items, class Body>
+__device__ __forceinline__ void pop_phase(const Src& src, Items items, Body body) {
+  __shared__ PopPlan pl;
+  const int n = src.count();
+  const int total = pop_plan(src, n, items, pl);
+  const int lane = threadIdx.x & 31;
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), GW = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int c = gw; c < total; c += GW) {
+    int lo = 0, hi = n;  // largest s with pre[s] <= c
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (pl.pre[mid] <= c) lo = mid;
+      else hi = mid;
+    }
+    const int i = ((c - pl.pre[lo]) << 5) + lane;
+    if (i < pl.items[lo]) body(*src.get(lo), i);
+  }
+}
+
 template <class Src>
 __global__ void __launch_bounds__(kPopThreads) k_pop_list(Src src) {
-  const PopArgs* ap = src.get(blockIdx.y);
-  if (!ap) return;
-  const PopArgs& a = *ap;
-  const int n = pop_sec_total(a);
-  for (int j = pop_tid(); j < n; j += pop_stride())
-    if (a.sec[2 * j + 1].w == 0.0f) a.alive[append_slot(&a.counts[0])] = j;
+  pop_phase(
+      src, [](const PopArgs& a) { return pop_sec_total(a); },
+      [](const PopArgs& a, int j) {
+        if (a.sec[2 * j + 1].w == 0.0f) a.alive[append_slot(&a.counts[0])] = j;
+      });
 }
 
+// items: every attached slot; the first min(n_att, n_sec) take secondaries,
+// the rest are marked for clones
 template <class Src>
 __global__ void __launch_bounds__(kPopThreads) k_pop_fill(Src src) {
-  const PopArgs* ap = src.get(blockIdx.y);
-  if (!ap) return;
-  const PopArgs& a = *ap;
-  const int n_att = *a.att_count, n_sec = a.counts[0];
-  const int k = min(n_att, n_sec);
-  for (int j = pop_tid(); j < k; j += pop_stride()) {
-    const int slot = a.att_list[j];
-    const int sidx = a.alive[n_sec - 1 - j];
-    a.state[2 * slot] = a.sec[2 * sidx];
-    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
-  }
-  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
-    const int dest = a.att_list[n_sec + jj];
-    atomicOr(&a.claim[dest >> 5], 1u << (dest & 31));
-  }
+  pop_phase(
+      src, [](const PopArgs& a) { return *a.att_count; },
+      [](const PopArgs& a, int j) {
+        const int n_att = *a.att_count, n_sec = a.counts[0];
+        const int k = min(n_att, n_sec);
+        if (j < k) {
+          const int slot = a.att_list[j];
+          const int sidx = a.alive[n_sec - 1 - j];
+          a.state[2 * slot] = a.sec[2 * sidx];
+          a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
+        } else {
+          const int dest = a.att_list[j];
+          atomicOr(&a.claim[dest >> 5], 1u << (dest & 31));
+        }
+      });
 }
 
+// items: the clones (n_att > n_sec) or the removal draws (n_sec > n_att)
 template <class Src>
 __global__ void __launch_bounds__(kPopThreads) k_pop_draw(Src src) {
-  const PopArgs* ap = src.get(blockIdx.y);
-  if (!ap) return;
-  const PopArgs& a = *ap;
-  const int n_att = *a.att_count, n_sec = a.counts[0];
-  const uint64_t interval = a.ctl->interval;
-  const float hme = a.half_me_over_e;
-  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
-    const int j = n_sec + jj;
-    const int dest = a.att_list[j];
-    int src_slot = -1;
-    for (uint32_t d = 0; d < 4096u; ++d) {
-      const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
-      if (!claimed(a.claim, r) && a.state[2 * r + 1].w == 0.0f) {
-        src_slot = r;
-        break;
-      }
-    }
-    if (src_slot < 0) {
-      atomicExch(a.error_flag, 4);
-      continue;
-    }
-    const float4 A = a.state[2 * src_slot], B = a.state[2 * src_slot + 1];
-    a.state[2 * dest] = A;
-    a.state[2 * dest + 1] = B;
-    add_growth(a.growth, (double)energy4(B, hme));
-  }
-  const int m = n_sec - n_att;
-  const int pool = a.n_electrons + m;
-  for (int j = pop_tid(); j < m; j += pop_stride()) {
-    int got = -1;
-    for (uint32_t d = 0; d < 4096u; ++d) {
-      const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 2u, d), pool);
-      const unsigned int bit = 1u << (r & 31);
-      const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
-      if (!(old & bit)) {
-        got = r;
-        break;
-      }
-    }
-    a.removed[j] = got;
-    if (got < 0) atomicExch(a.error_flag, 5);
-  }
+  pop_phase(
+      src, [](const PopArgs& a) { return abs(*a.att_count - a.counts[0]); },
+      [](const PopArgs& a, int item) {
+        const int n_att = *a.att_count, n_sec = a.counts[0];
+        const uint64_t interval = a.ctl->interval;
+        if (n_att > n_sec) {
+          const int j = n_sec + item;
+          const int dest = a.att_list[j];
+          int src_slot = -1;
+          for (uint32_t d = 0; d < 4096u; ++d) {
+            const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 1u, d), a.n_electrons);
+            if (!claimed(a.claim, r) && a.state[2 * r + 1].w == 0.0f) {
+              src_slot = r;
+              break;
+            }
+          }
+          if (src_slot < 0) {
+            atomicExch(a.error_flag, 4);
+            return;
+          }
+          const float4 A = a.state[2 * src_slot], B = a.state[2 * src_slot + 1];
+          a.state[2 * dest] = A;
+          a.state[2 * dest + 1] = B;
+          add_growth(a.growth, (double)energy4(B, a.half_me_over_e));
+        } else {
+          const int j = item;
+          const int pool = a.n_electrons + (n_sec - n_att);
+          int got = -1;
+          for (uint32_t d = 0; d < 4096u; ++d) {
+            const int r = uniform_index(pop_word((uint32_t)j, interval, a.seed, 2u, d), pool);
+            const unsigned int bit = 1u << (r & 31);
+            const unsigned int old = atomicOr(&a.claim[r >> 5], bit);
+            if (!(old & bit)) {
+              got = r;
+              break;
+            }
+          }
+          a.removed[j] = got;
+          if (got < 0) atomicExch(a.error_flag, 5);
+        }
+      });
 }
 
+// items: the clone marks to clear (n_att > n_sec) or the removal outcomes to
+// list (n_sec > n_att)
 template <class Src>
 __global__ void __launch_bounds__(kPopThreads) k_pop_sort(Src src) {
-  const PopArgs* ap = src.get(blockIdx.y);
-  if (!ap) return;
-  const PopArgs& a = *ap;
-  const int n_att = *a.att_count, n_sec = a.counts[0];
-  const float hme = a.half_me_over_e;
-  for (int jj = pop_tid(); jj < n_att - n_sec; jj += pop_stride()) {
-    const int dest = a.att_list[n_sec + jj];
-    atomicAnd(&a.claim[dest >> 5], ~(1u << (dest & 31)));
-  }
-  const int m = n_sec - n_att;
-  for (int j = pop_tid(); j < m; j += pop_stride()) {
-    const int r = a.removed[j];
-    if (r >= 0 && r < a.n_electrons) {
-      a.pair_slot[append_slot(&a.counts[1])] = r;
-      add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], hme));
-    } else if (r >= a.n_electrons) {
-      add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], hme));
-    }
-    if (!claimed(a.claim, a.n_electrons + j)) a.pair_sec[append_slot(&a.counts[2])] = a.alive[j];
-  }
+  pop_phase(
+      src, [](const PopArgs& a) { return abs(*a.att_count - a.counts[0]); },
+      [](const PopArgs& a, int item) {
+        const int n_att = *a.att_count, n_sec = a.counts[0];
+        if (n_att > n_sec) {
+          const int dest = a.att_list[n_sec + item];
+          atomicAnd(&a.claim[dest >> 5], ~(1u << (dest & 31)));
+          return;
+        }
+        const int j = item;
+        const int r = a.removed[j];
+        if (r >= 0 && r < a.n_electrons) {
+          a.pair_slot[append_slot(&a.counts[1])] = r;
+          add_growth(a.growth, -(double)energy4(a.state[2 * r + 1], a.half_me_over_e));
+        } else if (r >= a.n_electrons) {
+          add_growth(a.growth, -(double)energy4(a.sec[2 * a.alive[r - a.n_electrons] + 1], a.half_me_over_e));
+        }
+        if (!claimed(a.claim, a.n_electrons + j)) a.pair_sec[append_slot(&a.counts[2])] = a.alive[j];
+      });
 }
 
+// items: the (removed slot, surviving secondary) pairs, then the removal
+// marks to clear
 template <class Src>
 __global__ void __launch_bounds__(kPopThreads) k_pop_place(Src src) {
-  const PopArgs* ap = src.get(blockIdx.y);
-  if (!ap) return;
-  const PopArgs& a = *ap;
-  const int n_att = *a.att_count, n_sec = a.counts[0];
-  const int np = min(a.counts[1], a.counts[2]);
-  for (int q = pop_tid(); q < np; q += pop_stride()) {
-    const int slot = a.pair_slot[q];
-    const int sidx = a.pair_sec[q];
-    a.state[2 * slot] = a.sec[2 * sidx];
-    a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
-  }
-  const int m = n_sec - n_att;
-  for (int j = pop_tid(); j < m; j += pop_stride()) {
-    const int r = a.removed[j];
-    if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
-  }
+  pop_phase(
+      src,
+      [](const PopArgs& a) {
+        return min(a.counts[1], a.counts[2]) + max(a.counts[0] - *a.att_count, 0);
+      },
+      [](const PopArgs& a, int item) {
+        const int np = min(a.counts[1], a.counts[2]);
+        if (item < np) {
+          const int slot = a.pair_slot[item];
+          const int sidx = a.pair_sec[item];
+          a.state[2 * slot] = a.sec[2 * sidx];
+          a.state[2 * slot + 1] = a.sec[2 * sidx + 1];
+        } else {
+          const int r = a.removed[item - np];
+          if (r >= 0) atomicAnd(&a.claim[r >> 5], ~(1u << (r & 31)));
+        }
+      });
 }
 
 template <class Src>
-void launch_pop_phases(const Src& src, dim3 grid, cudaStream_t s) {
+void launch_pop_phases(const Src& src, int grid, cudaStream_t s) {
   k_pop_list<<<grid, kPopThreads, 0, s>>>(src);
   k_pop_fill<<<grid, kPopThreads, 0, s>>>(src);
   k_pop_draw<<<grid, kPopThreads, 0, s>>>(src);
@@ -1408,7 +1492,7 @@ void launch_hist(const HistArgs& a, cudaStream_t s) {
 void launch_pop_control(const PopArgs& a, cudaStream_t s) {
   PopOne one;
   one.a = a;
-  launch_pop_phases(one, dim3(kPopBlocks, 1), s);
+  launch_pop_phases(one, kPopBlocks, s);
 }
 
 cudaError_t prepare_kernels() {
@@ -1466,7 +1550,7 @@ int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned 
     PopBatch pb;
     pb.hdr = b.hdr;
     pb.slots = b.slots;
-    launch_pop_phases(pb, dim3(kPopBlocksPerSlot, slots), s);
+    launch_pop_phases(pb, sm_count * kPopBlocksPerSM, s);
     n += 1 + kPopLaunches;
   }
   if (parts & kPartSample) {
