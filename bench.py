@@ -436,15 +436,26 @@ def _sweep_served(capi, ps, conds, local, rank, args):
                 peak_footprint=rep.peak_footprint_bytes)
 
 
+def _largest_deviation(conds, batched, plain, zs):
+    """The condition whose batched and plain mean energies differ by the most
+    standard errors: E/N, electrons, both mean energies and errors."""
+    i = max(range(len(zs)), key=lambda k: zs[k])
+    rb, rp = batched["results"][i], plain["results"][i]
+    return {"E/N_Td": float(conds[i][0]), "electrons": int(conds[i][1]),
+            "batched_eV": [float(rb.mean_energy), float(rb.mean_energy_err)],
+            "plain_eV": [float(rp.mean_energy), float(rp.mean_energy_err)]}
+
+
 def _accuracy(conds, batched, plain):
     """Convergence and agreement of the batched solves with the plain ones."""
     import numpy as np
 
-    rel_err, zs, rate_dev = [], [], []
+    rel_err, zs, rel_dev, rate_dev = [], [], [], []
     for i in range(len(conds)):
         rb, rp = batched["results"][i], plain["results"][i]
         rel_err.append(rb.mean_energy_err / rb.mean_energy)
         zs.append(abs(rb.mean_energy - rp.mean_energy) / max(np.hypot(rb.mean_energy_err, rp.mean_energy_err), 1e-300))
+        rel_dev.append(abs(rb.mean_energy / rp.mean_energy - 1.0))
         cb, qb = batched["rates"][i]
         cp, qp = plain["rates"][i]
         for p in range(len(qb)):
@@ -454,6 +465,8 @@ def _accuracy(conds, batched, plain):
     return {"max_mean_energy_rel_err": float(max(rel_err)),
             "mean_energy_batched_vs_plain_max_sigmas": float(max(zs)),
             "mean_energy_batched_vs_plain_median_sigmas": float(np.median(zs)),
+            "mean_energy_batched_vs_plain_max_rel": float(max(rel_dev)),
+            "largest_sigmas_at": _largest_deviation(conds, batched, plain, zs),
             "rates_batched_vs_plain_median_poisson_sigmas": float(np.median(rate_dev)) if rate_dev else None,
             "rates_compared": len(rate_dev),
             "criterion": f"each condition stops when its mean-energy standard error < {SWEEP_ERR:.1%} "
