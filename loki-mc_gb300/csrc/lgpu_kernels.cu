@@ -496,6 +496,9 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
 template <int MODE>
 __global__ void __launch_bounds__(32) k_advance_drain(AdvanceArgs a) {
   __shared__ AdvShared sh;
+  // the warps took their own queues during the advance: only spilled
+  // secondaries are left (the count is final: the advance launch came first)
+  if (*(volatile const int*)a.spill_count == 0) return;
   advance_body<MODE>(a, sh);
 }
 
