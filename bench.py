@@ -63,8 +63,8 @@ E_N = 200.0
 N_ELECTRONS = 1_000_000
 # DRAM bytes per electron and interval of k_advance, from one ncu capture of the
 # same kernel on 4e6 electrons (profiles/k_advance_n2_dc200.md): 130.5 MB read +
-# 73.6 MB written; traffic grows in proportion to the electrons advanced
-DRAM_BYTES_PER_ELECTRON_STEP = (130.535168e6 + 73.571328e6) / 4.0e6
+# 73.8 MB written; traffic grows in proportion to the electrons advanced
+DRAM_BYTES_PER_ELECTRON_STEP = (130.522112e6 + 73.842176e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch), from
 # one ncu capture of the sweep (profiles/k_advance_batch_sweep64.md): 804.1 MB
