@@ -1,8 +1,8 @@
 /*
  * loki_oracle.c - CPU restatement of LoKI-MC's electron Monte Carlo engine.
  *
- * TEST INFRASTRUCTURE, NOT PRODUCT: the checker for the GPU path and the CPU
- * baseline of the benchmark. Compiled with -ffp-contract=off so that, like
+ * TEST INFRASTRUCTURE, NOT PRODUCT: the results the GPU path is compared with
+ * and the CPU baseline of the benchmark. Compiled with -ffp-contract=off so that, like
  * the reference built on x86-64, no a*b+c is fused.
  *
  * Each routine cites the reference routine it restates (file:line under the

@@ -2,8 +2,8 @@
  * loki_oracle.h - CPU restatement of LoKI-MC's electron Monte Carlo engine.
  *
  * TEST INFRASTRUCTURE, NOT PRODUCT. Only the tests, the smoke check and the
- * CPU-baseline leg of the benchmark may load this library, and only as the
- * checker or the timed CPU baseline. The GPU product never links it.
+ * CPU-baseline leg of the benchmark may load this library, and only for the
+ * results the GPU path is compared with or as the timed CPU baseline. The GPU product never links it.
  *
  * Every function restates one routine of the reference engine
  * (Code/LoKI-MC/Sources/BoltzmannMC.C, Code/LoKI-MC/Sources/MathFunctions.C,

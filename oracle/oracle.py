@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/loki_oracle.c).
 
 TEST INFRASTRUCTURE, NOT PRODUCT: imported only by the tests, the smoke check
-and the CPU-baseline leg of the benchmark, as the checker.
+and the CPU-baseline leg of the benchmark, as the reference results the GPU
+path is compared with (never as the thing measured or shipped).
 """
 from __future__ import annotations
 
