@@ -3,14 +3,17 @@
 // A Batch drives any number of Engines (one swarm condition each) through
 // their own solve steps - the control flow of BoltzmannMC::evaluateEEDF
 // (BoltzmannMC.C:299-426) stays per condition, on the host - while the device
-// work of one synchronisation interval of every running condition is one CUDA
-// graph launch: slot control blocks and scalars (prep), deferred distribution
-// tallies, one persistent advance launch per field branch over all slots'
-// electrons, the drain of spilled secondaries, population control (one block
-// per slot), the moment sums and a gather of every slot's scalars, followed by
-// a single read-back. Per interval the host stages one BatchSlot per running
-// condition (the argument blocks the single-condition launches take, plus the
-// interval's control block) into pinned memory and copies it over once.
+// work of one synchronisation interval of every running condition is two CUDA
+// graph launches: first the previous samples' distribution tallies (launched
+// before the host works through the conditions, so that its work runs beside
+// them), then slot control blocks and scalars (prep), one persistent advance
+// launch per field branch over all slots' electrons, the drain of spilled
+// secondaries, population control over all slots' items, the moment sums and
+// a gather of every slot's scalars into mapped host memory. Per interval the
+// host stages one BatchSlot per running condition (the argument blocks the
+// single-condition launches take, plus the interval's control block) into
+// pinned memory and copies it over once. A condition whose energy grid is
+// re-built sits an interval out while the re-build runs on its own stream.
 //
 // Slots: at most max_slots conditions run at a time; conditions beyond that
 // wait in order of addition and start as running ones finish, so a long run
@@ -158,8 +161,9 @@ class Batch {
     return b;
   }
 
-  // the kernels of one interval, captured once (their sizes come from the
-  // staged header, so one graph serves every interval and every membership)
+  // the kernels of one interval (or of the distribution passes, kGraphHist),
+  // captured once per set of launch groups: their sizes come from the staged
+  // header, so one graph serves every interval and every membership
   int graph(unsigned parts, cudaGraphExec_t* out, int* kernels) {
     auto it = graphs_.find(parts);
     if (it == graphs_.end()) {

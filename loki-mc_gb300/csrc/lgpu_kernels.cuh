@@ -223,7 +223,9 @@ constexpr int kBatchHistChunk = 65535;     // electrons per block of the histogr
 
 // Staging layout (host pinned mirror and device copy are identical):
 //   BatchHeader | adv_prefix | smp_prefix | hist_prefix | hist2_prefix (kBatchMaxSlots+1 ints
-//   each, padded) | BatchSlot[...]
+//   each) | smp_part | hist_part | hist2_part (kBatchMaxSlots ints each, padded) | BatchSlot[...]
+// The interval's staging fills the advance and moment parts, the distribution
+// passes' staging (same layout) the hist parts and each slot's `hist`.
 struct BatchArgs {
   BatchHeader* hdr;
   const BatchSlot* slots;
