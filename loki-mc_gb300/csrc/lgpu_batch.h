@@ -46,7 +46,11 @@ class Batch {
   // distribution passes' graphs carry kGraphHist)
   static constexpr unsigned kGraphHist = 1u << 16;
   std::map<unsigned, std::pair<cudaGraphExec_t, int>> graphs_;
-  std::vector<std::pair<int, int>> part_s_, part_h_, part_v_;  // (partial chunk size, slot) of each pass
+  // scratch of the pass layouts (lgpu_chunks.h): electrons and inclusion per
+  // slot, remainders
+  std::vector<int> n_;
+  std::vector<unsigned char> take_, all_;
+  std::vector<std::pair<int, int>> rem_;
   // totals since creation
   long long intervals_ = 0, launches_ = 0;
   double adv_ms_ = 0, electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
@@ -283,9 +287,10 @@ class Batch {
     int* ap = reinterpret_cast<int*>(h_stage_ + batch_prefix_offset());
     int* sp = ap + (kBatchMaxSlots + 1);
     int* spart = sp + 3 * (kBatchMaxSlots + 1);  // after the two distribution prefixes (other staging)
-    part_s_.clear();
+    n_.resize(n);
+    take_.resize(n);
     auto* sl = reinterpret_cast<BatchSlot*>(h_stage_ + batch_slots_offset());
-    int na = 0, ns = 0;
+    int na = 0;
     unsigned parts = 0;
     double electrons = 0;
     const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
@@ -301,21 +306,17 @@ class Batch {
       parts |= 1u << e->field_mode();
       if (sl[s].flags & kSlotIonAtt) parts |= kPartIonAtt;
       ap[s] = na;
-      sp[s] = ns;
       na += (N + kBatchAdvanceChunk - 1) / kBatchAdvanceChunk;
-      if (sl[s].flags & kSlotSample) {
-        ns += N / kBatchSampleChunk;
-        if (N % kBatchSampleChunk) part_s_.emplace_back(N % kBatchSampleChunk, s);
-      }
+      n_[s] = N;
+      take_[s] = (sl[s].flags & kSlotSample) ? 1 : 0;
     }
     ap[n] = na;
-    sp[n] = ns;
-    const int ps = order_parts(part_s_, spart);
+    const auto smp = layout_pass(n, n_.data(), take_.data(), kBatchSampleChunk, sp, spart, rem_);
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_slots = n;
     hdr->adv_chunks = na;
-    hdr->smp_full = ns;
-    hdr->smp_chunks = ns + ps;
+    hdr->smp_full = smp.first;
+    hdr->smp_chunks = smp.first + smp.second;
     if (hdr->smp_chunks) parts |= kPartSample;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
       while (s < n && members_[go[s]].e->field_mode() < m) ++s;
@@ -387,14 +388,6 @@ class Batch {
     return LGPU_OK;
   }
 
-  // partial chunks after the full ones, largest first: their slots into dst
-  static int order_parts(std::vector<std::pair<int, int>>& v, int* dst) {
-    std::stable_sort(v.begin(), v.end(),
-                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first > y.first; });
-    for (size_t k = 0; k < v.size(); ++k) dst[k] = v[k].second;
-    return (int)v.size();
-  }
-
   // The deferred distribution tallies of the running members' last samples
   // (EEDF, EADF and, before the velocity grid is fixed, EVDF), staged in the
   // second staging area and launched as their own graph on the batch stream,
@@ -406,34 +399,26 @@ class Batch {
     int* hpart = vp + (kBatchMaxSlots + 1) + kBatchMaxSlots;
     int* vpart = hpart + kBatchMaxSlots;
     auto* sl = reinterpret_cast<BatchSlot*>(h_hstage_ + batch_slots_offset());
-    part_h_.clear();
-    part_v_.clear();
-    int n = 0, nh = 0, nv = 0;
+    int n = 0;
+    n_.clear();
+    take_.clear();
     for (int idx : active_) {
       HistArgs h;
       if (!members_[idx].e->take_pending_hist(&h)) continue;
-      sl[n].hist = h;
-      const int N = h.n;
-      hp[n] = nh;
-      vp[n] = nv;
-      nh += N / kBatchHistChunk;
-      if (N % kBatchHistChunk) part_h_.emplace_back(N % kBatchHistChunk, n);
-      if (h.cylindrical && !h.evdf_done) {
-        nv += N / kBatchHistChunk;
-        if (N % kBatchHistChunk) part_v_.emplace_back(N % kBatchHistChunk, n);
-      }
-      ++n;
+      sl[n++].hist = h;
+      n_.push_back(h.n);
+      take_.push_back(h.cylindrical && !h.evdf_done ? 1 : 0);  // pass B: the EVDF not counted yet
     }
     if (n == 0) return LGPU_OK;
-    hp[n] = nh;
-    vp[n] = nv;
-    const int ph = order_parts(part_h_, hpart), pv = order_parts(part_v_, vpart);
+    all_.assign(n, 1);
+    const auto pa = layout_pass(n, n_.data(), all_.data(), kBatchHistChunk, hp, hpart, rem_);
+    const auto pb = layout_pass(n, n_.data(), take_.data(), kBatchHistChunk, vp, vpart, rem_);
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_slots = n;
-    hdr->hist_full = nh;
-    hdr->hist2_full = nv;
-    hdr->hist_chunks = nh + ph;
-    hdr->hist2_chunks = nv + pv;
+    hdr->hist_full = pa.first;
+    hdr->hist2_full = pb.first;
+    hdr->hist_chunks = pa.first + pa.second;
+    hdr->hist2_chunks = pb.first + pb.second;
     const unsigned parts = kGraphHist | (hdr->hist_chunks ? kPartHistA : 0u) | (hdr->hist2_chunks ? kPartHistB : 0u);
     cudaGraphExec_t ge;
     int rc, kernels = 0;

@@ -503,17 +503,6 @@ __global__ void __launch_bounds__(32) k_advance_drain(AdvanceArgs a) {
 }
 
 // ------------------------------------------------------------ batched advance
-// largest s < n_slots with prefix[s] <= c, for 0 <= c < prefix[n_slots]
-__device__ __forceinline__ int slot_of_chunk(const int* prefix, int n_slots, int c) {
-  int lo = 0, hi = n_slots;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (prefix[mid] <= c) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
 // word copy of a slot's advance arguments into shared memory (all threads)
 __device__ __forceinline__ void load_slot_args(const AdvanceArgs* src, AdvanceArgs* dst) {
   const int* s = reinterpret_cast<const int*>(src);
@@ -1283,29 +1272,8 @@ __global__ void k_batch_prep(BatchArgs b) {
 }
 
 // distribution tallies of the slots that sample them this interval
-// chunk c of a pass laid out as in BatchHeader: its slot and first electron
-struct ChunkRef {
-  int slot, first;
-};
-__device__ __forceinline__ ChunkRef pass_chunk(const int* full_prefix, const int* part_slot, int n_slots, int n_full,
-                                               int chunk, int c) {
-  ChunkRef r;
-  if (c < n_full) {
-    r.slot = slot_of_chunk(full_prefix, n_slots, c);
-    r.first = (c - full_prefix[r.slot]) * chunk;
-  } else {
-    r.slot = part_slot[c - n_full];
-    r.first = (full_prefix[r.slot + 1] - full_prefix[r.slot]) * chunk;
-  }
-  return r;
-}
-// the chunk a block takes in round r: rounds of gridDim.x chunks, every other
-// round in reverse block order (over a list sorted by size, the blocks' totals
-// differ by about one partial chunk)
-__device__ __forceinline__ int snake_chunk(int r) {
-  const int G = gridDim.x, bx = blockIdx.x;
-  return r * G + ((r & 1) ? G - 1 - bx : bx);
-}
+// the chunk this block takes in round r (snake order, lgpu_chunks.h)
+__device__ __forceinline__ int snake_chunk(int r) { return snake_index(r, gridDim.x, blockIdx.x); }
 
 __global__ void __launch_bounds__(kHistAThreads) k_hist_a_batch(BatchArgs b) {
   extern __shared__ unsigned int sm_hist[];

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "lgpu_chunks.h"
 #include "lgpu_types.h"
 
 namespace lgpu {
