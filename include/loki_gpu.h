@@ -303,10 +303,14 @@ int lgpu_batch_add(lgpu_batch* batch, lgpu_ctx* ctx);
 int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, lgpu_batch_report* report);
 /* Interval-level control (benchmarks, callers with their own loop):
  * lgpu_batch_start starts the queued contexts that fit the slots (their
- * lgpu_init_ensemble), lgpu_batch_step advances every running context by n
- * intervals (a context whose stop criteria hold finishes and leaves its slot
- * to a waiting one; *running counts those still running), and a later
- * lgpu_batch_run completes what is left. report counts only this call. */
+ * lgpu_init_ensemble), lgpu_batch_step runs n batched intervals (a context
+ * whose stop criteria hold finishes and leaves its slot to a waiting one;
+ * *running counts those still running), and a later lgpu_batch_run completes
+ * what is left. report counts only this call. A context whose energy grid
+ * must be re-built (the trial-frequency check, BoltzmannMC.C:617-688) sits
+ * one batched interval out while the re-build runs beside it, so n batched
+ * intervals advance it by n or fewer of its own; its own sequence of
+ * intervals, and so its results, do not change. */
 int lgpu_batch_start(lgpu_batch* batch);
 int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* report);
 /* The cudaStream_t all of the batch's work runs on. */
