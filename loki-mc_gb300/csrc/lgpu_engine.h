@@ -444,7 +444,6 @@ class Engine {
     LGPU_CU(cudaEventSynchronize(tables_ev_));
     return cuda(cudaGetLastError(), "build_tables");
   }
-  bool tables_ready() const { return !tables_inflight_ || cudaEventQuery(tables_ev_) != cudaErrorNotReady; }
 
   // maximizationAccelerationEnergy (BoltzmannMC.C:765-802)
   double max_accel_energy(double e0, double dt) const {
