@@ -65,6 +65,16 @@ def case_gases(name):
         synth.assign_sampler(o2, "Ionization", "momentumConservationIonization")
         synth.assign_sampler(n2, "Ionization", "isotropic")
         return [n2, o2], dict(N=3.22e22, red_field=100.0, max_e=120.0, sharing="equalSharing")
+    if name == "screen":
+        # screened-Coulomb scattering with the screening energy taken after the
+        # energy loss (params[0] = 1) on inelastic processes, where the energy
+        # after differs from the incident one (AngularScatteringFunctions.h:56-74)
+        n2 = synth.n2_like_gas(fraction=0.8)
+        o2 = synth.o2_like_gas(fraction=0.2)
+        synth.assign_sampler(n2, "Vibrational", "coulombScreen", (1.0, 1.3))
+        synth.assign_sampler(n2, "Excitation", "coulombScreen", (1.0, 2.7))
+        synth.assign_sampler(o2, "Excitation", "coulombScreen", (0.0, 0.8))
+        return [n2, o2], dict(N=3.22e22, red_field=150.0, max_e=120.0, sharing="equalSharing")
     raise KeyError(name)
 
 
@@ -294,7 +304,7 @@ def main():
     ap.add_argument("--ne", type=float, default=1e4)
     a = ap.parse_args()
     jobs = []
-    for i, name in enumerate(("atomic", "n2", "mix")):
+    for i, name in enumerate(("atomic", "n2", "mix", "screen")):
         if a.only and name != a.only:
             continue
         jobs.append(("kin", name, os.path.join(HERE, f"kin_{name}.npz"), 1000 + i, 0))

@@ -5,7 +5,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("atomic", "n2", "mix")
+CASES = ("atomic", "n2", "mix", "screen")
 BRANCHES = ("dc", "ac", "b", "ecr", "acb")
 
 
