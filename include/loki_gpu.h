@@ -6,8 +6,9 @@
  * The reference has no foreign-function interface: the engine is a template
  * parameter of Setup<T> and Output<T> (Code/LoKI-MC/Sources/lokimc.C:14-41,
  * 78-80). Each entry point below names the reference routine or data it
- * stands in for; a C++ adapter class (BoltzmannMCGPU)
- * calls them from the reference's host code.
+ * stands in for; a C++ adapter class (BoltzmannMCGPU,
+ * loki-mc_gb300/adapter/BoltzmannMCGPU.h) calls them from the reference's host
+ * code.
  *
  * Conventions: plain C types, host pointers with explicit sizes, int status
  * returns (LGPU_OK = 0). A context owns all device memory; no pointer passed
@@ -238,6 +239,15 @@ int lgpu_replay_flights(lgpu_ctx* ctx, int n, const double* t, const double* dt,
 int lgpu_replay_collisions(lgpu_ctx* ctx, int n, const double* nu_trial, const double* vel, const double* energy,
                            const double* uniforms, int u_stride, double* out, int* used);
 
+/* The same events through the null test the advance kernels run
+ * (BoltzmannMC.C:1033-1052 with a shortcut of this backend): the random
+ * frequency is compared first with an upper bound of the total frequency over
+ * a block of table rows, and the table row is read only when it lies below.
+ * A bound below an interpolated frequency would turn a real collision into a
+ * null one, so the outputs must equal lgpu_replay_collisions'. */
+int lgpu_replay_collisions_coarse(lgpu_ctx* ctx, int n, const double* nu_trial, const double* vel,
+                                  const double* energy, const double* uniforms, int u_stride, double* out, int* used);
+
 /* ---- free flights without device allocation ----
  *
  * No counterpart in the reference. For callers that cannot allocate device
@@ -247,11 +257,14 @@ int lgpu_replay_collisions(lgpu_ctx* ctx, int n, const double* nu_trial, const d
  * kernel as lgpu_replay_flights without a context: inputs and outputs are the
  * caller's host arrays, staged through a static device array of at most 4096
  * flights (512 KiB, held on every GPU that loads the library until exit).
- * More than 4096 flights return LGPU_ERR_BAD_ARG. The first call on a device
- * looks the array's address up (cudaGetSymbolAddress), so make it before any
- * stream capture. Calls share the array: calls that overlap on the GPU (from
- * several host threads or streams) race. Synchronous: returns when the outputs
- * are written. The field arguments are those of lgpu_set_field_raw. */
+ * More than 4096 flights, or a device index outside [0, device count),
+ * return LGPU_ERR_BAD_ARG. The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress) and keeps it for the process, so make that
+ * call before any stream capture, and do not call this on a device after a
+ * cudaDeviceReset there. Calls share the array: calls that overlap on the GPU
+ * (from several host threads or streams) race. The caller's current device is
+ * restored before returning. Synchronous: returns when the outputs are
+ * written. The field arguments are those of lgpu_set_field_raw. */
 int lgpu_replay_flights_noalloc(int device, const double e_field[3], double freq_hz, double red_mag_hx,
                                 double cyclotron, int n, const double* t, const double* dt, const double* pos,
                                 const double* vel, double* pos_out, double* vel_out, double* energy_out,

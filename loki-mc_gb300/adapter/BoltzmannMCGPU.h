@@ -11,8 +11,9 @@
 // unchanged on the members it fills.
 //
 // Build: compile with the reference's sources (and its Boost/GSL), add
-// -I<repo>/include and link libloki_gpu.so. Select it in lokimc.C as
-// INTEGRATION.md shows. Optional setup keys (ignored by the reference):
+// -I<repo>/include and link libloki_gpu.so. Select it in lokimc.C by the
+// setup key electronKinetics.numericsMC.backend: gpu, as lokimc_gpu_main.cpp
+// does. Optional setup keys (ignored by the reference):
 //   electronKinetics.numericsMC.gpuDevice: <int>   (default 0)
 //   electronKinetics.numericsMC.gpuSeed: <int>     (default 12345)
 #ifndef LOKI_GPU_BOLTZMANN_MC_GPU_H
@@ -100,9 +101,74 @@ class BoltzmannMCGPU : public BoltzmannMC {
     return 0;
   }
 
+  // The per-job host state of evaluateNonConstantVariables (BoltzmannMC.C:428-559)
+  // without its start ensemble and its FP64 tables: the device samples the
+  // ensemble and builds the tables itself, so the host does neither.
+  void prepareJob() {
+    gasTemperature = workCond->gasTemperature;
+    gasEnergy = 1.5 * Constant::boltzmann * gasTemperature / Constant::electronCharge;
+    totalGasDensity = workCond->gasDensity;
+    int k = 0;
+    for (auto& gas : gasArray) {
+      for (auto& collision : gas->collisionArray) {
+        if (collision->type == "Effective") continue;
+        relDensities[k] = collision->target->density;
+        thermalStdDeviations[k] = std::sqrt(Constant::boltzmann * gasTemperature / targetMasses[k]);
+        ++k;
+        if (collision->isReverse) {
+          relDensities[k] = collision->productArray[0]->density;
+          thermalStdDeviations[k] = std::sqrt(Constant::boltzmann * gasTemperature / targetMasses[k]);
+          ++k;
+        }
+      }
+    }
+    time = 0;
+    steadyStateTime = Constant::NON_DEF;
+    reducedElecField = workCond->reducedElecField;
+    electricFieldValue = workCond->reducedElecFieldSI * totalGasDensity;
+    elecFieldAngle = workCond->elecFieldAngle;
+    if (elecFieldAngle == 180) {
+      electricField[0] = 0;
+      electricField[1] = 0;
+      electricField[2] = -electricFieldValue;
+    } else {
+      electricField[0] = electricFieldValue * std::sin(elecFieldAngle / 180.0 * M_PI);
+      electricField[1] = 0;
+      electricField[2] = electricFieldValue * std::cos(elecFieldAngle / 180.0 * M_PI);
+    }
+    excitationFrequency = workCond->excitationFrequency;
+    excitationFrequencyRadians = excitationFrequency * 2.0 * M_PI;
+    if (excitationFrequency != 0) electricField *= std::sqrt(2);
+    reducedMagField = workCond->reducedMagField;
+    cyclotronFrequency = Constant::electronCharge * workCond->reducedMagFieldSI * totalGasDensity / Constant::electronMass;
+    isCylindricallySymmetric = workCond->isCylindricallySymmetric;
+    accelerationElecField = -Constant::electronCharge / Constant::electronMass * electricField;
+    if (excitationFrequencyRadians != 0) {
+      integrationPhaseStep = 2.0 * M_PI / nIntegrationPhases;
+      integrationPhases = Eigen::ArrayXd::LinSpaced(nIntegrationPhases, 0.5 * integrationPhaseStep,
+                                                    2.0 * M_PI - 0.5 * integrationPhaseStep);
+    }
+    averagedMeanEnergy = Constant::NON_DEF;
+    averagedFluxDiffusionCoeffs = Eigen::Matrix3d::Constant(Constant::NON_DEF);
+    averagedFluxDiffusionCoeffsError = Eigen::Matrix3d::Constant(Constant::NON_DEF);
+    averagedBulkDiffusionCoeffs = Eigen::Matrix3d::Constant(Constant::NON_DEF);
+    averagedBulkDiffusionCoeffsError = Eigen::Matrix3d::Constant(Constant::NON_DEF);
+    energyGainField = 0;
+    energyGrowth = 0;
+    totalCollisionCounter = 0;
+    nullCollisionCounter = 0;
+    for (int i = 0; i < nProcesses; ++i) {
+      energyGainProcesses[i] = 0;
+      energyLossProcesses[i] = 0;
+      collisionCounters[i] = 0;
+    }
+    goodStatisticalErrors = false;
+    failedCollisionDueToGrid = 0;
+  }
+
   void evaluateEEDFOnGPU() {
     // per-job variables, relative densities and fields (BoltzmannMC.C:428-559)
-    evaluateNonConstantVariables();
+    prepareJob();
 
     // the flattened processes of BoltzmannMC.C:29-271
     std::vector<lgpu_process> procs(nProcesses);

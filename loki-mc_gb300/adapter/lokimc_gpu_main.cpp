@@ -6,7 +6,8 @@
 // the reference's own Output class. When the setup sets
 // electronKinetics.numericsMC.backend to "gpu", the boltzmannMC engine is
 // BoltzmannMCGPU; otherwise the reference's engines run unchanged. Build it
-// with the reference's sources except lokimc.C.
+// with the reference's sources except lokimc.C (oracle/ref/Makefile, target
+// dropin).
 #include <omp.h>
 
 #include <cstdio>

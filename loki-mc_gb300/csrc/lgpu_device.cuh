@@ -92,9 +92,12 @@ struct PhiloxStream {
 // buffer refills.
 struct PcgStream {
   uint64_t state, inc;
-  __device__ __forceinline__ void init(uint32_t electron, uint64_t interval, uint64_t seed, uint32_t salt) {
+  // `tag` is the counter's last word: 0x5EED for ensemble electrons, the
+  // creating warp's index for secondaries (whose salt differs)
+  __device__ __forceinline__ void init(uint32_t electron, uint64_t interval, uint64_t seed, uint32_t salt,
+                                       uint32_t tag = 0x5EEDu) {
     Philox ph;
-    ph.ctr = make_uint4(electron, (uint32_t)interval, (uint32_t)(interval >> 32) ^ (salt << 16), 0x5EEDu);
+    ph.ctr = make_uint4(electron, (uint32_t)interval, (uint32_t)(interval >> 32) ^ (salt << 16), tag);
     ph.key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
     const uint4 w = ph.next();
     state = ((uint64_t)w.x << 32) | w.y;

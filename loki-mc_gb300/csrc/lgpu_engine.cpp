@@ -162,4 +162,11 @@ int lgpu_replay_collisions(lgpu_ctx* ctx, int n, const double* nu, const double*
   return ctx->e->replay_collisions(n, nu, vel, energy, u, stride, out, used);
 }
 
+int lgpu_replay_collisions_coarse(lgpu_ctx* ctx, int n, const double* nu, const double* vel, const double* energy,
+                                  const double* u, int stride, double* out, int* used) {
+  CTX_CHECK(ctx);
+  if (n < 0 || stride < 1 || (n > 0 && (!nu || !vel || !energy || !u || !out || !used))) return LGPU_ERR_BAD_ARG;
+  return ctx->e->replay_collisions(n, nu, vel, energy, u, stride, out, used, 1);
+}
+
 }  // extern "C"

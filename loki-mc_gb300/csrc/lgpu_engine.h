@@ -669,7 +669,7 @@ class Engine {
     s.half_me_over_e = (float)(0.5 * kMeD / kQeD);
     s.moments = d_sc_->moments;
     s.max_energy_bits = &d_sc_->sample_max_bits;
-    launch_sample(s, stream_);
+    launch_sample(s, sm_count_, stream_);
     ++launches_;
   }
 
@@ -1487,7 +1487,7 @@ class Engine {
   }
 
   int replay_collisions(int n, const double* nu, const double* vel, const double* energy, const double* u, int stride,
-                        double* out, int* used) {
+                        double* out, int* used, int coarse = 0) {
     if (n <= 0) return LGPU_OK;
     if (max_interp_ < 0) return fail(LGPU_ERR_STATE, "tables are not built");
     LGPU_TRY(upload_proc_consts());
@@ -1512,6 +1512,7 @@ class Engine {
     a.t = tables();
     a.procs = d_procf_;
     a.gases = d_gasf_;
+    a.coarse = coarse;
     launch_replay_collide(a, stream_);
     ++launches_;
     LGPU_CU(copy(out, d_rp_out_, (size_t)n * 11 * sizeof(double), cudaMemcpyDeviceToHost));

@@ -198,16 +198,19 @@ __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const I
   }
 }
 
-// a secondary, pushed from its creation time t_c = A.w
+// a secondary, pushed from its creation time t_c = A.w. Its random stream is
+// named by the warp that takes it (`warp_tag`) and that warp's running count of
+// secondaries (`id`), with a salt apart from the ensemble electrons' streams.
 __device__ __forceinline__ void lane_take_secondary(const AdvanceArgs& a, const IntervalView& iv, Lane& L,
-                                                    LaneTally& tl, float4 A, float4 B, uint32_t id) {
+                                                    LaneTally& tl, float4 A, float4 B, uint32_t warp_tag,
+                                                    uint32_t id) {
   L.slot = -1;
   L.p = make_float3(A.x, A.y, A.z);  // created from shifted positions already
   L.v = make_float3(B.x, B.y, B.z);
   L.s = -1.0f;
   L.t = A.w;
   tl.time_adj += iv.T - L.t;  // electron-time this secondary adds to the interval
-  L.rng.init(id, iv.interval, a.seed, a.salt + 1u);
+  L.rng.init(id, iv.interval, a.seed, a.salt + 1u, warp_tag);
   L.energy = energy_of(L.v, a.c.half_me_over_e);
   L.events = 0;
   L.pending = false;
@@ -218,15 +221,17 @@ __device__ __forceinline__ void lane_take_secondary(const AdvanceArgs& a, const 
 // returns the entries left
 __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const IntervalView& iv, AdvShared& sh, int wid,
                                                 int lane, unsigned lt_mask, Lane& L, LaneTally& tl, uint32_t& sec_id,
-                                                uint32_t id_hi, uint32_t id_mask) {
+                                                uint32_t warp_tag) {
   int qn = min(sh.qn[wid], kLocalQ);
   const unsigned idle = __ballot_sync(0xffffffffu, !L.have);
   const int r = __popc(idle & lt_mask);
   const int take = min(__popc(idle), qn);
   if (((idle >> lane) & 1u) && r < take) {
     const int e = qn - 1 - r;
-    lane_take_secondary(a, iv, L, tl, sh.qa[wid][e], sh.qb[wid][e], id_hi | ((sec_id + (uint32_t)r) & id_mask));
+    lane_take_secondary(a, iv, L, tl, sh.qa[wid][e], sh.qb[wid][e], warp_tag, sec_id + (uint32_t)r);
   }
+  // 2^32 secondaries taken by one warp in one interval would repeat streams
+  if (sec_id + (uint32_t)take < sec_id && lane == 0) atomicExch(a.error_flag, 3);
   sec_id += (uint32_t)take;
   qn -= take;
   __syncwarp();
@@ -403,7 +408,7 @@ __device__ __forceinline__ void block_flush(const AdvanceArgs& a, AdvShared& sh,
 // and the warp's queue are exhausted; the caller flushes the lane sums.
 template <int MODE>
 __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, const IntervalView& iv,
-                                          LaneTally& tl, uint32_t& sec_id, uint32_t id_hi, uint32_t id_mask) {
+                                          LaneTally& tl, uint32_t& sec_id, uint32_t warp_tag) {
   const bool drain = a.queue_only != 0;
   const int n_el = drain ? 0 : a.n;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -421,7 +426,7 @@ __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, c
     // first (the queue stays short, so it rarely spills), then the ensemble
     // chunk, then (drain) the spilled secondaries
     int qn = min(sh.qn[wid], kLocalQ);
-    if (qn > 0) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, id_hi, id_mask);
+    if (qn > 0) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, warp_tag);
     const unsigned need = __ballot_sync(0xffffffffu, !L.have);
     if (need && !exhausted) {
       const int n_need = __popc(need);
@@ -456,7 +461,7 @@ __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, c
         if (((idle2 >> lane) & 1u) && r2 < take2) {
           const int k = sp_next + r2;
           lane_take_secondary(a, iv, L, tl, __ldcg(&a.spill[2 * k]), __ldcg(&a.spill[2 * k + 1]),
-                              0xC0000000u | (uint32_t)k);
+                              0xFFFFFFFFu, (uint32_t)k);
         }
         sp_next += max(take2, 0);
       }
@@ -478,11 +483,12 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh
   __syncthreads();
   const IntervalView iv = interval_view<MODE>(a);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 12);
+  // drain launches: one block, whose warp tag stays below the spill's 0xFFFFFFFF
+  const uint32_t warp_tag = (uint32_t)(blockIdx.x * kAdvanceWarps + wid);
   LaneTally tl;
   reset_tally(tl);
   uint32_t sec_id = 0;
-  warp_loop<MODE>(a, sh, iv, tl, sec_id, id_hi, 0xFFFu);
+  warp_loop<MODE>(a, sh, iv, tl, sec_id, warp_tag);
   block_flush(a, sh, tl, lane, wid);
 }
 
@@ -527,8 +533,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
   const int s0 = b.hdr->mode_slot[MODE], s1 = b.hdr->mode_slot[MODE + 1];
   if (s0 >= s1) return;  // no slot with this field branch (uniform over the grid)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  // secondary ids: 13 bits of warp index (< 8192 warps), 18 bits of count
-  const uint32_t id_hi = 0x80000000u | ((uint32_t)(blockIdx.x * kAdvanceWarps + wid) << 18);
+  const uint32_t warp_tag = (uint32_t)(blockIdx.x * kAdvanceWarps + wid);
   const int n_slots = b.hdr->n_slots;
   if (threadIdx.x == 0) {
     const int c0 = b.hdr->mode_chunk[MODE], c1 = b.hdr->mode_chunk[MODE + 1];
@@ -547,7 +552,7 @@ __global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advanc
     if (threadIdx.x == 0) s_iv = interval_view<-1>(s_a);
     __syncthreads();
     reset_tally(tl);
-    warp_loop<MODE>(s_a, sh, s_iv, tl, sec_id, id_hi, 0x3FFFFu);
+    warp_loop<MODE>(s_a, sh, s_iv, tl, sec_id, warp_tag);
     __syncthreads();  // every warp is done with the slot
     block_flush(s_a, sh, tl, lane, wid);
     __syncthreads();  // the flush has read the shared tallies and arguments
@@ -1394,7 +1399,22 @@ __global__ void k_replay_collide(ReplayCollArgs a) {
   float energy = (float)a.energy[i];
   CollResult cr;
   cr.ej_v = make_float3(0.f, 0.f, 0.f);
-  collide(a.c, a.t, a.procs, a.gases, (float)a.nu[i], v, energy, rng, cr);
+  if (a.coarse) {
+    // the advance kernels' event: the null test tries the block bound of the
+    // total frequency first (lane_flight), then the rest of the collision
+    // (lane_real)
+    float r = 0.0f;
+    const float nu = (float)a.nu[i];
+    if (is_thermal(a.c, energy) || cold_real(a.t, nu, energy, rng, r, a.t.nu_coarse)) {
+      collide_pending(a.c, a.t, a.procs, a.gases, nu, r, v, energy, rng, cr);
+    } else {
+      cr.chosen = -1;
+      cr.dE = 0.0f;
+      cr.ionized = 0;
+    }
+  } else {
+    collide(a.c, a.t, a.procs, a.gases, (float)a.nu[i], v, energy, rng, cr);
+  }
   double* o = a.out + (size_t)i * 11;
   o[0] = cr.chosen;
   o[1] = v.x;
@@ -1447,9 +1467,9 @@ void launch_build_tables(const TableBuildArgs& a, cudaStream_t s) {
   if (a.nu_coarse) k_coarse_max<<<1, kMaxCoarse, 0, s>>>(a.nu_pair, a.M, a.coarse_shift, a.nu_coarse, a.n_coarse);
 }
 
-void launch_sample(const SampleArgs& a, cudaStream_t s) {
+void launch_sample(const SampleArgs& a, int sm_count, cudaStream_t s) {
   if (a.n <= 0) return;
-  const int grid = min(blocks_for(a.n, kSampleThreads), 152 * 4);
+  const int grid = min(blocks_for(a.n, kSampleThreads), max(1, sm_count) * 4);
   k_sample<<<grid, kSampleThreads, 0, s>>>(a);
 }
 

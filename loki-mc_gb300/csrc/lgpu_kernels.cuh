@@ -130,7 +130,8 @@ struct SampleArgs {
   double* moments;                 // [kMoments], accumulated (zeroed by the caller)
   unsigned int* max_energy_bits;
 };
-void launch_sample(const SampleArgs& a, cudaStream_t s);
+// grid: at most four blocks per SM (sm_count = the device's multiprocessors)
+void launch_sample(const SampleArgs& a, int sm_count, cudaStream_t s);
 
 // Distribution tallies of one sample (BoltzmannMC.C:1550-1571).
 struct HistArgs {
@@ -293,6 +294,7 @@ struct ReplayCollArgs {
   TablesF t;
   const ProcF* procs;
   const GasF* gases;
+  int coarse;             // 1: the null test of the advance kernels (block bounds first)
 };
 void launch_replay_collide(const ReplayCollArgs& a, cudaStream_t s);
 

@@ -14,7 +14,9 @@
 // it (512 KiB) until the process exits. Its host-side name is only a handle;
 // the device address is looked up once per device with cudaGetSymbolAddress
 // (the first call on a device does it, so that first call should come before
-// any stream capture). Every call shares the array and leaves its contents
+// any stream capture) and kept for the life of the process, so the entry point
+// must not be used on a device after cudaDeviceReset there. The caller's
+// current device is restored before the call returns. Every call shares the array and leaves its contents
 // behind; calls whose work overlaps on the GPU (two host threads, or two
 // streams) race on it.
 #include <cuda_runtime.h>
@@ -82,6 +84,10 @@ int scratch_for_device(int device, double** out) {
   return LGPU_OK;
 }
 
+int run_flights(int device, const double e_field[3], double freq_hz, double red_mag_hx, double cyclotron, int n,
+                const double* t, const double* dt, const double* pos, const double* vel, double* pos_out,
+                double* vel_out, double* energy_out, double* gain_out);
+
 }  // namespace
 
 extern "C" int lgpu_replay_flights_noalloc(int device, const double e_field[3], double freq_hz, double red_mag_hx,
@@ -98,8 +104,22 @@ extern "C" int lgpu_replay_flights_noalloc(int device, const double e_field[3], 
   if (!t || !dt || !pos || !vel || !pos_out || !vel_out || !energy_out || !gain_out) return LGPU_ERR_BAD_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return LGPU_ERR_NO_DEVICE;
-  if (device >= ndev) return LGPU_ERR_BAD_ARG;
+  if (device < 0 || device >= ndev) return LGPU_ERR_BAD_ARG;
+  // the caller's current device is put back on every return path
+  int prev_device = 0;
+  if (cudaGetDevice(&prev_device) != cudaSuccess) return LGPU_ERR_CUDA;
   if (cudaSetDevice(device) != cudaSuccess) return LGPU_ERR_CUDA;
+  const int rc = run_flights(device, e_field, freq_hz, red_mag_hx, cyclotron, n, t, dt, pos, vel, pos_out, vel_out,
+                             energy_out, gain_out);
+  if (cudaSetDevice(prev_device) != cudaSuccess && rc == LGPU_OK) return LGPU_ERR_CUDA;
+  return rc;
+}
+
+namespace {
+
+int run_flights(int device, const double e_field[3], double freq_hz, double red_mag_hx, double cyclotron, int n,
+                const double* t, const double* dt, const double* pos, const double* vel, double* pos_out,
+                double* vel_out, double* energy_out, double* gain_out) {
   double* scratch = nullptr;
   const int rc = scratch_for_device(device, &scratch);
   if (rc != LGPU_OK) return rc;
@@ -143,3 +163,5 @@ extern "C" int lgpu_replay_flights_noalloc(int device, const double e_field[3], 
     return LGPU_ERR_CUDA;
   return LGPU_OK;
 }
+
+}  // namespace

@@ -28,7 +28,7 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
             "lgpu_get_timing",
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
-            "lgpu_replay_flights_noalloc",
+            "lgpu_replay_collisions_coarse", "lgpu_replay_flights_noalloc",
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
             "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
@@ -150,6 +150,7 @@ def load(path: str | None = None):
     lib.lgpu_set_field_raw.argtypes = [ctypes.c_void_p, P_(D), D, D, D]
     lib.lgpu_replay_flights.argtypes = [ctypes.c_void_p, I] + [P_(D)] * 8
     lib.lgpu_replay_collisions.argtypes = [ctypes.c_void_p, I, P_(D), P_(D), P_(D), P_(D), I, P_(D), P_(I)]
+    lib.lgpu_replay_collisions_coarse.argtypes = lib.lgpu_replay_collisions.argtypes
     lib.lgpu_replay_flights_noalloc.argtypes = [I, P_(D), D, D, D, I] + [P_(D)] * 8
     VP = ctypes.c_void_p
     lib.lgpu_batch_create.argtypes = [I, I, P_(VP)]
@@ -362,7 +363,9 @@ class Context:
                                                 dptr(vo), dptr(eo), dptr(go)))
         return po, vo, eo, go
 
-    def replay_collisions(self, nu, vel, energy, uniforms):
+    def replay_collisions(self, nu, vel, energy, uniforms, coarse=False):
+        """lgpu_replay_collisions, or with coarse=True
+        lgpu_replay_collisions_coarse (the advance kernels' null test)."""
         n = len(nu)
         nu = np.ascontiguousarray(nu, np.float64)
         vel = np.ascontiguousarray(vel, np.float64).reshape(n, 3)
@@ -370,8 +373,9 @@ class Context:
         u = np.ascontiguousarray(uniforms, np.float64).reshape(n, -1)
         out = np.zeros((n, 11))
         used = np.zeros(n, np.int32)
-        self.check(self.lib.lgpu_replay_collisions(self.h, n, dptr(nu), dptr(vel), dptr(energy), dptr(u), u.shape[1],
-                                                   dptr(out), used.ctypes.data_as(P_(I))))
+        fn = self.lib.lgpu_replay_collisions_coarse if coarse else self.lib.lgpu_replay_collisions
+        self.check(fn(self.h, n, dptr(nu), dptr(vel), dptr(energy), dptr(u), u.shape[1], dptr(out),
+                      used.ctypes.data_as(P_(I))))
         return out, used
 
 

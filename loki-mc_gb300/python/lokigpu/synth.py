@@ -116,6 +116,20 @@ def maxwell_gas(nu: float, density: float, name: str = "M1", mass_ratio: float =
     return Gas(name, C.ELECTRON_MASS / mass_ratio, 1.0, [el], {f"{name}(gnd)": State(1.0)})
 
 
+def reid_ramp_gas(name: str = "A") -> Gas:
+    """Reid's ramp model gas (Reid 1979, Aust. J. Phys. 32, 231), the
+    reference's benchmark case 1: target mass 4 amu, constant isotropic elastic
+    cross section 6e-20 m^2, one excitation with threshold 0.2 eV and cross
+    section 1e-19 (eps - 0.2) m^2 (eps in eV), each tabulated at its two end
+    points (linear between them) up to 1000 eV."""
+    mass = 4.0 * 1.660539040e-27
+    el = Collision("Elastic", f"{name}(gnd)", f"{name}(gnd)", 0.0, np.array([0.0, 1000.0]),
+                   np.array([6e-20, 6e-20]))
+    ex = Collision("Excitation", f"{name}(gnd)", f"{name}(exc)", 0.2, np.array([0.2, 1000.0]),
+                   np.array([0.0, 1e-19 * (1000.0 - 0.2)]))
+    return Gas(name, mass, 1.0, [el, ex], {f"{name}(gnd)": State(1.0), f"{name}(exc)": State(0.0)})
+
+
 def _boltzmann(energies: Sequence[float], weights: Sequence[float], tg: float) -> List[float]:
     z = [w * math.exp(-en / (KB_EV * tg)) for en, w in zip(energies, weights)]
     s = sum(z)
@@ -389,7 +403,10 @@ def write_setup(path: str, lxcat_files: Sequence[str], gases: Sequence[Gas], *, 
                 tg: float = 300.0, red_field=100.0, red_mag=0.0, angle=180.0, freq=0.0,
                 n_electrons: float = 1e4, sharing: str = "equalSharing", gas_temp: str = "false",
                 extra_numerics: Optional[Dict[str, str]] = None, anis: Optional[List[str]] = None,
-                folder: str = "out", output: bool = False, kte_init_ev: Optional[float] = None) -> None:
+                folder: str = "out", output: bool = False, kte_init_ev: Optional[float] = None,
+                data_files: Sequence[str] = ("eedf", "swarmParameters", "rateCoefficients", "powerBalance",
+                                             "MCSimDetails"),
+                n_phases: Optional[int] = None) -> None:
     """A reference setup file (.in) for the mixture, gui off."""
     def vec(v):
         if isinstance(v, (list, tuple, np.ndarray)):
@@ -438,9 +455,11 @@ def write_setup(path: str, lxcat_files: Sequence[str], gases: Sequence[Gas], *, 
         L.append(f"    initialElecTempOverGasTemp: {_fmt(kte_init_ev / (KB_EV * tg))}")
     for k, v in (extra_numerics or {}).items():
         L.append(f"    {k}: {v}")
+    if n_phases is not None:
+        L.append(f"    nIntegrationPhases: {int(n_phases)}")
     L += ["gui:", "  isOn: false", "output:", f"  isOn: {'true' if output else 'false'}",
-          f"  folder: {folder}", "  dataFiles:", "    - eedf", "    - swarmParameters",
-          "    - rateCoefficients", "    - powerBalance", "    - MCSimDetails"]
+          f"  folder: {folder}", "  dataFiles:"]
+    L += [f"    - {d}" for d in data_files]
     with open(path, "w") as f:
         f.write("\n".join(L) + "\n")
 

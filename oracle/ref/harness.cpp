@@ -258,6 +258,75 @@ void ref_get_eedf(double* cells, double* eedf) {
   }
 }
 
+// Distributions and periodic averages after a solve (BoltzmannMC.C:1574-1605,
+// 1728-1741). sizes: energy cells, cos cells, radial cells, axial cells,
+// phases, cylindrical symmetry (EADF/EVDF exist), AC field (periodic outputs).
+void ref_dist_sizes(int* s) {
+  BoltzmannMC* m = g_mc;
+  s[0] = (int)m->nEnergyCells;
+  s[1] = (int)m->nCosAngleCells;
+  s[2] = (int)m->nRadialVelocityCells;
+  s[3] = (int)m->nAxialVelocityCells;
+  s[4] = (int)m->nIntegrationPhases;
+  s[5] = m->isCylindricallySymmetric ? 1 : 0;
+  s[6] = m->excitationFrequencyRadians != 0 ? 1 : 0;
+}
+
+// efadf, esadf [nE]; eadf [nE x nCos] and evdf [nR x nA] row-major; radial and
+// axial cell centres (cylindrical conditions only)
+void ref_get_anisotropic(double* f1, double* f2, double* eadf, double* evdf, double* rc, double* ac) {
+  BoltzmannMC* m = g_mc;
+  const int nE = (int)m->nEnergyCells, nC = (int)m->nCosAngleCells, nR = (int)m->nRadialVelocityCells,
+            nA = (int)m->nAxialVelocityCells;
+  for (int i = 0; i < nE; ++i) {
+    f1[i] = m->efadf[i];
+    f2[i] = m->esadf[i];
+    for (int k = 0; k < nC; ++k) eadf[(size_t)i * nC + k] = m->eadf(i, k);
+  }
+  for (int i = 0; i < nR; ++i) {
+    rc[i] = m->radialVelocityCells[i];
+    for (int k = 0; k < nA; ++k) evdf[(size_t)i * nA + k] = m->evdf(i, k);
+  }
+  for (int k = 0; k < nA; ++k) ac[k] = m->axialVelocityCells[k];
+}
+
+// per phase: samples, mean energy, flux and bulk velocity (x3), flux and bulk
+// diffusion (x9), EEDF [nPh x nE] (AC conditions only)
+void ref_get_periodic(double* n, double* me, double* fv, double* bv, double* fd, double* bd, double* eedf_per) {
+  BoltzmannMC* m = g_mc;
+  const int nPh = (int)m->nIntegrationPhases, nE = (int)m->nEnergyCells;
+  for (int q = 0; q < nPh; ++q) {
+    n[q] = m->nIntegrationPointsPerPhase[q];
+    me[q] = m->meanEnergies_periodic[q];
+    for (int k = 0; k < 3; ++k) {
+      fv[3 * q + k] = m->fluxVelocities_periodic(q, k);
+      bv[3 * q + k] = m->bulkVelocities_periodic(q, k);
+    }
+    for (int k = 0; k < 9; ++k) {
+      fd[9 * q + k] = m->fluxDiffusionCoeffs_periodic(q, k);
+      bd[9 * q + k] = m->bulkDiffusionCoeffs_periodic(q, k);
+    }
+    for (int c = 0; c < nE; ++c) eedf_per[(size_t)q * nE + c] = m->eedf_periodic(q, c);
+  }
+}
+
+// time-averaged power per process, gain and loss (BoltzmannMC.C:1640-1649)
+void ref_get_power(double* gain, double* loss) {
+  for (int i = 0; i < g_mc->nProcesses; ++i) {
+    gain[i] = g_mc->averagedPowerGainProcesses[i];
+    loss[i] = g_mc->averagedPowerLossProcesses[i];
+  }
+}
+
+// the mean-energy time series (samplingTimes, meanEnergies), its length first
+int ref_n_samples() { return g_mc->nSamplingPoints; }
+void ref_get_energy_series(double* t, double* e) {
+  for (int i = 0; i < g_mc->nSamplingPoints; ++i) {
+    t[i] = g_mc->samplingTimes[i];
+    e[i] = g_mc->meanEnergies[i];
+  }
+}
+
 // Statistical helpers used by the engine's host side.
 double ref_statistical_error(const double* a, int n, double nbins) {
   Eigen::ArrayXd arr(n);

@@ -9,10 +9,10 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/Code"
+REF = os.environ.get("LOKI_REFERENCE_CODE", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference source tree not present")
+@pytest.mark.skipif(not (REF and os.path.isdir(REF)), reason="LOKI_REFERENCE_CODE (the reference's Code/) not set")
 def test_dropin_reaches_the_backend(tmp_path):
     try:
         import torch

@@ -9,10 +9,14 @@ these vectors (tests/test_oracle_golden.py). The GPU computes in FP32, so:
 * free flights (every field branch): velocity within 1e-5 of |v| and
   position within 1e-5 of (|x| + |v dt|), energy and field gain within
   2e-5 of the energy (the FP32 tolerance of the per-electron kinematics);
-* collision events: the chosen process agrees except where the random
-  number falls within FP32 rounding of a boundary between processes (at
-  least 98% of events), and where it agrees the post-collision velocity,
-  energy, secondary and uniform count match to 1e-5 relative.
+* collision events: the chosen process agrees except where the event sits
+  within FP32 rounding of a boundary between processes (a relative
+  perturbation of the inputs of 1e-5 moves the oracle to the device's choice;
+  at most 0.5 % of events), and the post-collision velocity, energy,
+  secondary and uniform count match the oracle to 1e-5 relative (1e-4
+  against the perturbed oracle event on a boundary);
+* the production null test with its block bounds decides every event as the
+  plain one does.
 """
 import numpy as np
 import pytest
@@ -69,32 +73,61 @@ def test_free_flights(gpu_case, branch):
         assert abs(go[k] - ref_g[k]) <= 2e-5 * max(ref_e[k], g[f"acc_{branch}_energy"][k]), (branch, k)
 
 
-def _boundary_margin(pr, f, nu, vel, energy, u):
-    """Relative distance of the reference's random choice value from the
-    nearest cumulative boundary it is compared with (cold gas)."""
-    M, P = pr.M, pr.P
-    r = nu * u[0]
-    eos = energy / pr.s.step
-    i1 = int(min(eos, M - 1))
-    i2 = min(i1 + 1, M - 1)
-    w1 = max(i2 - eos, 0.0)
-    w2 = 1.0 - w1
-    tot = w1 * pr.nu_tot[i1] + w2 * pr.nu_tot[i2]
-    cum = w1 * pr.cum[i1 * P:(i1 + 1) * P] + w2 * pr.cum[i2 * P:(i2 + 1) * P]
-    rcs = r / f.N / np.linalg.norm(vel)
-    m1 = abs(r - tot) / max(tot, 1e-300)
-    m2 = np.min(np.abs(cum - rcs)) / max(cum[-1], 1e-300) if cum[-1] > 0 else 1.0
-    return min(m1, m2)
-
-
 def _f32(a):
-    return np.asarray(a, dtype=np.float32).astype(np.float64)
+    return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+# Relative size of the input perturbations that stand for the FP32 rounding of
+# the device's intermediate values (a few units in the last place of FP32,
+# i.e. ~1e-7, amplified by the few operations before a comparison).
+PERTURB = 1e-5
+
+
+def _perturbed_choices(pr, f, nu, vel, en, u, rng):
+    """Oracle outcomes of one event under small relative perturbations of its
+    inputs (trial frequency, velocity, energy, uniforms), each outcome with the
+    perturbed inputs' result: the processes the event can pick within the
+    FP32 rounding of the device arithmetic."""
+    out = []
+    for k in range(24):
+        if k < 8:  # one input at a time, both signs
+            which, sign = k // 2, 1.0 if k % 2 == 0 else -1.0
+            d = np.zeros(4)
+            d[which] = sign
+            dn, dv, de, du = d * PERTURB
+            dvv = np.full(3, dv)
+            duu = np.full(len(u), du)
+        else:  # all inputs at once, random signs
+            dn, de = rng.choice([-1.0, 1.0], 2) * PERTURB
+            dvv = rng.choice([-1.0, 1.0], 3) * PERTURB
+            duu = rng.choice([-1.0, 1.0], len(u)) * PERTURB
+        uu = np.clip(u * (1.0 + duu), 1e-300, 1.0)
+        res, used, _ = O.collide(pr, f, nu * (1.0 + dn), vel * (1.0 + dvv), en * (1.0 + de), uu)
+        out.append((res, used))
+    return out
+
+
+def _kinematics_agree(got, ref, en, tol):
+    vs = np.linalg.norm(ref[1:4])
+    es = np.linalg.norm(ref[7:10])
+    return (np.linalg.norm(got[1:4] - ref[1:4]) <= tol * max(vs, 1.0) and abs(got[4] - ref[4]) <= tol * max(en, 1e-3)
+            and abs(got[5] - ref[5]) <= tol * max(en, 1e-3) and
+            np.linalg.norm(got[7:10] - ref[7:10]) <= tol * max(es, 1.0))
 
 
 def test_collisions(gpu_case):
     """The kernel reads its inputs (trial frequency, velocity, energy and the
     recorded uniforms) as FP32; the oracle gets the same FP32-rounded values,
-    so the comparison measures the FP32 arithmetic of the kinematics alone."""
+    so the comparison measures the FP32 arithmetic of the device alone.
+
+    Every event, cold and thermal: where the device picks the oracle's
+    process, the post-collision velocity, energy, energy change, secondary and
+    uniform count agree to 1e-5 relative. Where it picks another one, that
+    process must be one the oracle picks under a relative perturbation of the
+    inputs of 1e-5 (the event sits on a boundary within FP32 rounding), and
+    the kinematics must agree with that perturbed oracle event to 1e-4. The
+    production null test (block bounds first, lgpu_replay_collisions_coarse)
+    takes the same decisions. The mismatch count per mode is printed."""
     name, g, ctx, ps = gpu_case
     sc = g["scalars_tab"]
     M = len(g["tab_grid"])
@@ -102,6 +135,7 @@ def test_collisions(gpu_case):
     pr.build_tables(O.make_fields(sc[0], sc[1]), sc[15])
     from lokigpu import capi
 
+    rng = np.random.default_rng(7)
     for m in range(gu.n_modes(g)):
         gte, shr, fac = g[f"col{m}_opts"]
         cfg = capi.default_config(n_electrons=1024, n_interp=M, gas_temperature_effect=int(gte), sharing=int(shr))
@@ -112,26 +146,59 @@ def test_collisions(gpu_case):
         c2.build_tables(sc[15], M, ps.n)
         nu, vel, en, U = (_f32(g[f"col{m}_{k}"]) for k in ("nu", "vel", "energy", "u"))
         out, used = c2.replay_collisions(nu, vel, en, U)
+        out_c, used_c = c2.replay_collisions(nu, vel, en, U, coarse=True)
         c2.close()
+        # same decisions and uniform counts; the kinematics inlined in the
+        # two replay paths may contract multiply-adds differently (thermal
+        # targets), so they agree to a few FP32 units in the last place
+        assert np.array_equal(out[:, 0], out_c[:, 0]) and np.array_equal(used, used_c), (name, m)
+        np.testing.assert_allclose(out_c, out, rtol=2e-6, atol=1e-6 * float(np.max(np.abs(out[:, 1:4]))))
         f = O.make_fields(sc[0], sc[1], gas_temp_effect=int(gte), sharing=int(shr), sharing_factor=fac)
-        mismatch, unexplained, compared = 0, 0, 0
+        mismatch, compared, real = 0, 0, 0
         for k in range(len(nu)):
             ref, ref_used, _ = O.collide(pr, f, nu[k], vel[k], en[k], U[k])
-            if out[k][0] != ref[0]:
-                mismatch += 1
-                if int(gte) == 0 and _boundary_margin(pr, f, nu[k], vel[k], en[k], U[k]) > 1e-5:
-                    unexplained += 1
+            if out[k][0] == ref[0]:
+                if ref[0] < 0:
+                    continue
+                real += 1
+                compared += 1
+                assert used[k] == ref_used, (name, m, k)
+                assert _kinematics_agree(out[k], ref, en[k], 1e-5), (name, m, k, out[k], ref)
                 continue
-            if ref[0] < 0:
-                continue
-            compared += 1
-            assert used[k] == ref_used, (name, m, k)
-            vs = np.linalg.norm(ref[1:4])
-            assert np.linalg.norm(out[k][1:4] - ref[1:4]) <= 1e-5 * max(vs, 1.0), (name, m, k, out[k], ref)
-            assert abs(out[k][4] - ref[4]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
-            assert abs(out[k][5] - ref[5]) <= 1e-5 * max(en[k], 1e-3), (name, m, k)
-            es = np.linalg.norm(ref[7:10])
-            assert np.linalg.norm(out[k][7:10] - ref[7:10]) <= 1e-5 * max(es, 1.0), (name, m, k)
+            mismatch += 1
+            alts = [(r, u_) for r, u_ in _perturbed_choices(pr, f, nu[k], vel[k], en[k], U[k], rng)
+                    if r[0] == out[k][0]]
+            assert alts, (f"{name} mode {m} event {k}: device picks {out[k][0]:.0f}, the oracle {ref[0]:.0f} "
+                          f"and no perturbation of 1e-5 moves it there")
+            if out[k][0] >= 0:
+                assert any(_kinematics_agree(out[k], r, en[k], 1e-4) for r, _ in alts), (name, m, k, out[k], alts[0][0])
+                compared += 1
+        print(f"{name} mode {m} (gas temperature {int(gte)}, sharing {int(shr)}): {len(nu)} events, "
+              f"{real} real collisions compared, {mismatch} process choices on a boundary")
         assert compared > 100, (name, m, compared)
-        assert mismatch <= 0.02 * len(nu), (name, m, mismatch)
-        assert unexplained <= 2, (name, m, unexplained)
+        assert mismatch <= 0.005 * len(nu), (name, m, mismatch)
+
+
+def test_coarse_null_test_never_changes_a_decision(gpu_case):
+    """The advance kernels' null test compares the random frequency with an
+    upper bound of the total frequency over a block of table rows before it
+    reads the row. Over random energies across the whole table and random
+    uniforms, the coarse and the plain null test decide alike, event by event."""
+    name, g, ctx, ps = gpu_case
+    sc = g["scalars_tab"]
+    M = len(g["tab_grid"])
+    ctx.build_tables(sc[15], M, ps.n)
+    rng = np.random.default_rng(11)
+    n = 200_000
+    en = _f32(rng.uniform(0.0, sc[15] * (M - 1) / M, n))
+    speed = np.sqrt(2.0 * en * 1.6021766208e-19 / 9.10938356e-31)
+    d = rng.normal(size=(n, 3))
+    vel = _f32(d / np.linalg.norm(d, axis=1)[:, None] * speed[:, None])
+    nu_max = float(np.max(g["tab_nu_max"]))
+    nu = _f32(np.full(n, nu_max))
+    U = _f32(rng.uniform(1e-7, 1.0, (n, 12)))
+    out, used = ctx.replay_collisions(nu, vel, en, U)
+    out_c, used_c = ctx.replay_collisions(nu, vel, en, U, coarse=True)
+    assert np.array_equal(out[:, 0], out_c[:, 0]), (name, np.flatnonzero(out[:, 0] != out_c[:, 0])[:10])
+    assert np.array_equal(used, used_c), name
+    assert np.count_nonzero(out[:, 0] >= 0) > 100, name
