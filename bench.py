@@ -36,7 +36,10 @@ first requests.
 
 --impl reference times the CPU implementation of the same path on the host
 cores (the C restatement of the reference's algorithm, oracle/) on a bounded
-sample of the same workload.
+sample of the same workload: the sweep's 64 conditions with their electron
+counts, one single-threaded condition per core at a time (a sweep's best use
+of a CPU), real collisions summed over time weighted by each condition's
+electrons.
 """
 from __future__ import annotations
 
@@ -177,63 +180,100 @@ def sweep_config(capi, device, n_e, seed, converge):
 
 
 # --------------------------------------------------------------------- CPU arm
-def cpu_sample(seconds: float, threads: int, workload: str, n_electrons: int = 100_000, warm_intervals: int = 300):
-    """Times the CPU restatement of the reference's path (oracle/) on the host
-    cores on a bounded sample of the workload: the sweep's mixture at 100 Td
-    (the sweep's midpoint decade), or the N2-like gas at 200 Td; n_electrons
-    electrons, rate measured after warm_intervals intervals."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+def _oracle_arrays(ps):
     import numpy as np
+
+    off = np.concatenate([[0], np.cumsum([len(e) for e in ps.raw_e])]).astype(np.int32)
+    return dict(ptype=ps.ptype, is_super=ps.is_super, sampler=ps.sampler, sampler_p0=ps.sampler_p0,
+                sampler_p1=ps.sampler_p1, superw=ps.superw, emin=ps.emin, emax=ps.emax, rel_dens=ps.rel_dens,
+                mass=ps.mass, red_mass=ps.red_mass, eloss=ps.eloss, wparam=ps.wparam, raw_off=off[:-1],
+                raw_len=np.array([len(e) for e in ps.raw_e], np.int32), raw_e=np.concatenate(ps.raw_e),
+                raw_v=np.concatenate(ps.raw_v), gas_first=ps.gas_first, gas_last=ps.gas_last,
+                gas_frac=ps.gas_fraction, energy_max_elastic=ps.energy_max_elastic)
+
+
+def cpu_condition(job):
+    """One condition on one host core: the CPU restatement of the reference's
+    path (oracle/) with `n` electrons started at kT = 1 eV, for `seconds` of
+    wall time; the second half is measured. Returns (electrons of the
+    condition in the workload, measured electron-intervals, real collisions,
+    seconds)."""
+    workload, td, n_cfg, n, seconds, seed = job
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "loki-mc_gb300", "python"))
     import oracle as O
 
     ps = sweep_processes() if workload == "sweep" else n2_processes()
-    en = 100.0 if workload == "sweep" else E_N
-    off = np.concatenate([[0], np.cumsum([len(e) for e in ps.raw_e])]).astype(np.int32)
-    arrays = dict(ptype=ps.ptype, is_super=ps.is_super, sampler=ps.sampler, sampler_p0=ps.sampler_p0,
-                  sampler_p1=ps.sampler_p1, superw=ps.superw, emin=ps.emin, emax=ps.emax, rel_dens=ps.rel_dens,
-                  mass=ps.mass, red_mass=ps.red_mass, eloss=ps.eloss, wparam=ps.wparam, raw_off=off[:-1],
-                  raw_len=np.array([len(e) for e in ps.raw_e], np.int32), raw_e=np.concatenate(ps.raw_e),
-                  raw_v=np.concatenate(ps.raw_v), gas_first=ps.gas_first, gas_last=ps.gas_last,
-                  gas_frac=ps.gas_fraction, energy_max_elastic=ps.energy_max_elastic)
-    pr = O.OracleProcs(arrays, 10000)
-    f = O.make_fields(N_GAS, T_GAS, E=(0.0, 0.0, -en * 1e-21 * N_GAS))
-    cfg = O.default_run_config(n_electrons, n_threads=threads, seed=3, max_seconds=seconds,
-                               mark_sync_step=warm_intervals, req_integration_points=1e12)
-    st, res, _ = O.run(pr, f, cfg)
-    what = "the sweep's mixture at 100 Td" if workload == "sweep" else "the N2-like gas at 200 Td"
-    if res.mark_elapsed > 0 and res.elapsed > res.mark_elapsed:
-        real = res.real_collisions - res.mark_real_collisions
-        dt = res.elapsed - res.mark_elapsed
-        sample = (f"{n_electrons} electrons, {what}, intervals {warm_intervals + 1}..{res.sync_steps} "
-                  f"({dt:.1f} s of a {seconds:.0f} s run, C restatement of the reference path)")
+    pr = O.OracleProcs(_oracle_arrays(ps), 10000)
+    f = O.make_fields(N_GAS, T_GAS, E=(0.0, 0.0, -td * 1e-21 * N_GAS))
+    cfg = O.default_run_config(n, n_threads=1, seed=seed, max_seconds=seconds, mark_seconds=0.5 * seconds,
+                               req_integration_points=1e12, init_temp_ratio=KT_INIT)
+    _, res, _ = O.run(pr, f, cfg)
+    if res.mark_elapsed <= 0:
+        return n_cfg, 0.0, 0.0, 0.0
+    steps = res.sync_steps - res.mark_sync_steps
+    return n_cfg, float(n * steps), res.real_collisions - res.mark_real_collisions, res.elapsed - res.mark_elapsed
+
+
+def cpu_sweep_rate(samples, cores):
+    """Real collisions per second of the whole workload on `cores` host cores
+    running one condition each: every condition advances its electrons
+    (n_cfg) each interval; a core spends n_cfg x (seconds per
+    electron-interval) on it and finds n_cfg x (real collisions per
+    electron-interval)."""
+    real_sum = sum(n_cfg * real / el for n_cfg, el, real, _ in samples if el > 0)
+    time_sum = sum(n_cfg * secs / el for n_cfg, el, _, secs in samples if el > 0)
+    return cores * real_sum / time_sum if time_sum > 0 else 0.0
+
+
+def cpu_sample(seconds: float, cores: int, workload: str, offset: int = 0, max_electrons: int = 10_000):
+    """Times the CPU restatement of the reference's path on the host cores on
+    a bounded sample of the workload. Sweep: the same 64 conditions (E/N and
+    electron counts) one per core at a time, each single-threaded for
+    `seconds` (as a sweep runs best on a CPU: one setup per condition and
+    core), with up to `max_electrons` electrons; a round takes the next `cores`
+    conditions from `offset`. n2_200td: the single condition on one core per
+    sample. Returns (real collisions/s of the workload, description, cores,
+    samples)."""
+    import multiprocessing as mp
+
+    if workload == "sweep":
+        conds = sweep_conditions()
+        picks = [conds[(offset + k) % len(conds)] for k in range(cores)]
     else:
-        real, dt = res.real_collisions, res.elapsed
-        sample = f"{n_electrons} electrons, {what}, first {res.sync_steps} intervals ({dt:.1f} s)"
-    return real / dt, sample, threads
+        picks = [(E_N, N_ELECTRONS)] * cores
+    jobs = [(workload, td, n_cfg, min(n_cfg, max_electrons), seconds, 3 + offset + k)
+            for k, (td, n_cfg) in enumerate(picks)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        samples = pool.map(cpu_condition, jobs)
+    what = "the sweep's 64 conditions" if workload == "sweep" else "the N2-like gas at 200 Td"
+    desc = (f"{what}, {len(jobs)} conditions per round on {cores} cores (one single-threaded run each, up to "
+            f"{max_electrons} electrons from kT = 1 eV, {seconds:.1f} s of which the second half is measured), "
+            f"weighted by the workload's electron counts; C restatement of the reference path")
+    return cpu_sweep_rate(samples, cores), desc, cores, samples
 
 
 def run_reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    threads = os.cpu_count() or 1
+    cores = os.cpu_count() or 1
     t0 = time.time()
-    rates = []
-    sample = ""
-    per_step = max(3.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    per_step = max(2.0, min(8.0, 150.0 / max(1, args.steps + args.warmup)))
+    samples, desc = [], ""
     for i in range(args.warmup + args.steps):
-        r, sample, _ = cpu_sample(per_step, threads, args.workload, warm_intervals=100)
+        _, desc, _, smp = cpu_sample(per_step, cores, args.workload, offset=i * cores)
         if i >= args.warmup:
-            rates.append(r)
-    v = sum(rates) / len(rates)
+            samples += smp
+    v = cpu_sweep_rate(samples, cores)
     workload = "sweep64_n2o2_1-1000Td" if args.workload == "sweep" else "n2_like_dc200Td_1e6e"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * (time.time() - t0) / (args.steps + args.warmup),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload, "electrons": 100_000,
-                       "impl_detail": "C restatement of the reference path (oracle/), OpenMP"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "config": {"workload": workload, "conditions": 64 if args.workload == "sweep" else 1,
+                       "impl_detail": "C restatement of the reference path (oracle/), one condition per core"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -473,6 +513,126 @@ def _accuracy(conds, batched, plain):
                          "(50-block batch means, BoltzmannMC.C:1743-1767)"}
 
 
+PRECISION_ELECTRONS = 1_000_000
+REPEAT_SEEDS = 8
+
+
+def _quantities(r):
+    """(name, value, error) of the swarm parameters the precision study
+    compares (E along -z: drift along +z)."""
+    return [("mean_energy", r.mean_energy, r.mean_energy_err), ("flux_v_z", r.flux_v[2], r.flux_v_err[2]),
+            ("bulk_v_z", r.bulk_v[2], r.bulk_v_err[2]), ("flux_D_xx", r.flux_d[0], r.flux_d_err[0]),
+            ("flux_D_zz", r.flux_d[8], r.flux_d_err[8]), ("bulk_D_xx", r.bulk_d[0], r.bulk_d_err[0]),
+            ("bulk_D_zz", r.bulk_d[8], r.bulk_d_err[8])]
+
+
+def _ref_quantities(x):
+    return [("mean_energy", x[0], x[1]), ("flux_v_z", x[4], x[7]), ("bulk_v_z", x[16], x[19]),
+            ("flux_D_xx", x[8], x[11]), ("flux_D_zz", x[10], x[13]), ("bulk_D_xx", x[20], x[23]),
+            ("bulk_D_zz", x[22], x[25])]
+
+
+def _precision_study(capi, ps, conds, local):
+    """The device's FP32 path against the reference's FP64 path on eight
+    points of the sweep (tests/golden/sweep_fp64.json, made by
+    tests/golden/make_sweep_fp64.py: the reference built from its sources,
+    1e5 electrons, 1e4 integration intervals): the same conditions solved in
+    one batch with 1e6 electrons and 1e4 integration intervals; per point and
+    quantity the relative error and its size in combined standard errors;
+    every rate coefficient with at least 1e4 counts in both runs. Plus seeded
+    repeats of the sweep's largest condition solved to its 0.5 % criterion:
+    the scatter of their mean energies against the batch-means errors they
+    report (short runs: 50 blocks of a few intervals each, far shorter than
+    the energy relaxation, so the reported errors understate the scatter)."""
+    import numpy as np
+
+    path = os.path.join(ROOT, "tests", "golden", "sweep_fp64.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        ref = json.load(f)["points"]
+    b = capi.Batch(local, len(ref) + REPEAT_SEEDS)
+    ctxs = []
+    for k, rec in enumerate(ref):
+        cfg = capi.default_config(device=local, seed=9100 + k, n_electrons=float(PRECISION_ELECTRONS), n_interp=10000,
+                                  init_temp_ratio=KT_INIT, req_integration_points=1e4, max_coll_before_ss=300.0,
+                                  max_seconds=300.0)
+        c = capi.Context(cfg)
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, rec["red_field"])
+        b.add(c)
+        ctxs.append(c)
+    big = max(range(len(conds)), key=lambda i: conds[i][1])
+    for k in range(REPEAT_SEEDS):
+        c = capi.Context(sweep_config(capi, local, conds[big][1], 9300 + k, converge=True))
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, T_GAS, conds[big][0])
+        b.add(c)
+        ctxs.append(c)
+    t0 = time.perf_counter()
+    res, st, _ = b.run()
+    wall = time.perf_counter() - t0
+    points, worst = [], {}
+    n_ok = n_all = 0
+    for k, rec in enumerate(ref):
+        r = res[k]
+        x = rec["result"]
+        cnt, rate, _, _ = ctxs[k].process_results()
+        pt = {"E/N_Td": rec["red_field"], "status": int(st[k])}
+        for (name, gv, ge), (_, rv, re) in zip(_quantities(r), _ref_quantities(x)):
+            if abs(rv) < 5.0 * re:
+                continue
+            rel = gv / rv - 1.0
+            sig = (gv - rv) / float(np.hypot(ge, re))
+            pt[name] = {"gpu": gv, "gpu_err": ge, "ref": rv, "ref_err": re, "rel_err": rel, "sigmas": sig}
+            ok = abs(rel) <= 5e-3 or abs(sig) <= 2.0
+            n_ok += ok
+            n_all += 1
+            w = worst.setdefault(name, {"max_abs_rel_err": 0.0, "max_abs_sigmas": 0.0})
+            w["max_abs_rel_err"] = max(w["max_abs_rel_err"], abs(rel))
+            w["max_abs_sigmas"] = max(w["max_abs_sigmas"], abs(sig))
+        rr = np.array(rec["rate"])
+        t_int = x[31] - x[30]
+        devs = []
+        for p in range(ps.n):
+            if rr[p] <= 0 or ps.rel_dens[p] <= 0:
+                continue
+            c_ref = rr[p] * t_int * rec["n_electrons"] * ps.rel_dens[p] * N_GAS
+            if c_ref < 1e4 or cnt[p] < 1e4:
+                continue
+            rel = rate[p] / rr[p] - 1.0
+            sig = rel / float(np.sqrt(1.0 / c_ref + 1.0 / float(cnt[p])))
+            devs.append((abs(rel), abs(sig)))
+            ok = abs(rel) <= 5e-3 or abs(sig) <= 2.0
+            n_ok += ok
+            n_all += 1
+        if devs:
+            pt["rates"] = {"compared": len(devs), "max_abs_rel_err": max(d[0] for d in devs),
+                           "max_abs_sigmas": max(d[1] for d in devs)}
+            w = worst.setdefault("rates", {"max_abs_rel_err": 0.0, "max_abs_sigmas": 0.0})
+            w["max_abs_rel_err"] = max(w["max_abs_rel_err"], pt["rates"]["max_abs_rel_err"])
+            w["max_abs_sigmas"] = max(w["max_abs_sigmas"], pt["rates"]["max_abs_sigmas"])
+        pt["power_balance_rel_err"] = {"gpu": r.power_balance_rel_err, "ref": x[29]}
+        points.append(pt)
+    rep_res = res[len(ref):]
+    me = np.array([r.mean_energy for r in rep_res])
+    errs = np.array([r.mean_energy_err for r in rep_res])
+    repeats = {"E/N_Td": conds[big][0], "electrons": conds[big][1], "seeds": REPEAT_SEEDS,
+               "mean_energy_scatter_eV": float(np.std(me, ddof=1)),
+               "median_reported_error_eV": float(np.median(errs)),
+               "scatter_over_reported": float(np.std(me, ddof=1) / np.median(errs)),
+               "median_integration_points": float(np.median([r.integration_points for r in rep_res]))}
+    for c in ctxs:
+        c.close()
+    del b
+    return {"reference": "FP64, the reference built from its sources, 1e5 electrons, 1e4 integration intervals "
+                         "(tests/golden/sweep_fp64.json)",
+            "device": f"FP32 push, FP64 tallies, {PRECISION_ELECTRONS} electrons, 1e4 integration intervals, batched",
+            "criterion": "|rel err| <= 0.5 % or |dev| <= 2 combined standard errors",
+            "within_criterion": f"{n_ok} of {n_all}", "worst": worst, "points": points,
+            "seeded_repeats": repeats, "wall_s": wall}
+
+
 def run_gpu_sweep(args):
     import torch
 
@@ -499,6 +659,11 @@ def run_gpu_sweep(args):
     e2e_b = _sweep_e2e_batched(capi, ps, conds, local, rank) if not args.no_e2e else None
     e2e_p = _sweep_e2e_plain(capi, ps, conds, local, rank) if not (args.no_e2e or args.no_plain) else None
     srv = _sweep_served(capi, ps, conds, local, rank, args) if not args.no_served else None
+    prec = _precision_study(capi, ps, conds, local) if (rank == 0 and not args.no_precision) else None
+    stream = None
+    if rank == 0 and not args.no_served and args.stream_requests > 0:
+        stream = serve_stream(capi, local, args.stream_requests, args.stream_arrival_ms, args.request_cap_s,
+                              args.slots, args.plain_requests)
 
     peak, peak_kind = measured_peaks()
     achieved = STATE_BYTES_PER_ELECTRON_STEP * tb["electron_steps"] / (tb["adv_ms"] * 1e-3) / 1e9 if tb["adv_ms"] > 0 else 0.0
@@ -507,8 +672,14 @@ def run_gpu_sweep(args):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample, cores = cpu_sample(args.cpu_seconds, os.cpu_count() or 1, "sweep")
-            cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+            cores = os.cpu_count() or 1
+            smp = []
+            rounds = (len(conds) + cores - 1) // cores
+            for k in range(rounds):
+                _, sample, _, got = cpu_sample(args.cpu_seconds / rounds, cores, "sweep", offset=k * cores)
+                smp += got
+            cpu = {"value": cpu_sweep_rate(smp, cores), "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": sample + f"; {rounds} rounds cover every condition"}
         e2e = None
         if e2e_b:
             rep = e2e_b["report"]
@@ -544,6 +715,8 @@ def run_gpu_sweep(args):
                 ratio["e2e"] = e2e["value"] / plain["e2e"]["value"]
                 if served:
                     ratio["served_over_plain_e2e"] = served["value"] / plain["e2e"]["value"]
+        if stream and stream.get("served_over_plain"):
+            ratio["served_stream_over_plain"] = stream["served_over_plain"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -559,8 +732,9 @@ def run_gpu_sweep(args):
                        "spilled_per_step": tb["spilled"] / args.steps,
                        "collision_turn_threshold": tb["real_batch"], "coarse_null_test": tb["coarse"],
                        "regrids_per_step": tb["regrids"] / max(args.steps, 1)},
-            "plain": plain, "batched_over_plain": ratio or None, "served": served,
+            "plain": plain, "batched_over_plain": ratio or None, "served": served, "served_stream": stream,
             "accuracy": _accuracy(conds, e2e_b, e2e_p) if (e2e_b and e2e_p) else None,
+            "precision": prec,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": SWEEP_DRAM_BYTES_PER_ELECTRON_STEP * electrons,
                          "traffic_source": "ncu dram__bytes_read+write of the batched DC advance, one sweep interval",
@@ -607,85 +781,102 @@ def serve_requests(n, seed=SWEEP_SEED + 7):
 SERVE_MAX_ELECTRONS = 4e6
 
 
-def run_gpu_serve(args):
-    """Served request stream: latency percentiles, throughput, and the plain
-    sequential path on the first requests for comparison."""
+def serve_stream(capi, local, n_requests, arrival_ms, cap_s, slots, plain_requests):
+    """The request stream of random mixtures through lgpu_server: every
+    request converged to 0.5 % mean-energy error (or stopped at cap_s of wall
+    time), Poisson arrivals with a mean gap of arrival_ms; then the first
+    plain_requests requests solved one after the other with lgpu_solve (the
+    plain path) for comparison. Returns the served block of the bench line."""
     import numpy as np
     import torch
 
-    from lokigpu import build as gbuild
-    from lokigpu import capi, synth
+    from lokigpu import synth
 
-    rank, world, local = _init_ranks()
-    if not os.path.exists(capi.library_path()):
-        gbuild.build()
-    reqs = serve_requests(args.requests)
+    reqs = serve_requests(n_requests)
     sets = [synth.flatten(r["gases"]) for r in reqs]
     rng = np.random.default_rng(SWEEP_SEED + 11)
-    gaps = rng.exponential(args.arrival_ms * 1e-3, len(reqs))
-    clocks = ClockSampler(local)
-    clocks.start()
-    srv = capi.Server(local, args.slots)
+    gaps = rng.exponential(arrival_ms * 1e-3, len(reqs))
+    srv = capi.Server(local, slots)
     ids = []
-    w0 = time.perf_counter()
     for r, ps, gap in zip(reqs, sets, gaps):
         time.sleep(float(gap))
         cfg = sweep_config(capi, local, r["ne"], r["seed"], converge=True)
         cfg.n_phases = 16
-        cfg.max_seconds = args.request_cap_s
+        cfg.max_seconds = cap_s
         ids.append(srv.submit(cfg, ps, ps.gas_first, ps.gas_last, ps.gas_fraction, N_GAS, T_GAS, r["en"],
                               r["angle"], r["freq"], r["red_mag"]))
-    sts = [srv.wait(j, 1800.0) for j in ids]
-    w1 = time.perf_counter()
+    sts = [srv.wait(j, 3600.0) for j in ids]
     rep = srv.report()
     srv.stop()
-    clk = clocks.stop()
     done = [s for s in sts if s.state == capi.JOB_DONE]
     capped = sum(1 for s in done if s.result.capped)
     lat = [s.end_time - s.submit_time for s in done]
+    svc = [s.end_time - s.start_time for s in done]
     real = sum(s.result.real_collisions for s in done)
     span = max(s.end_time for s in sts) - min(s.submit_time for s in sts)
     errors = [f"request {i}: status {s.status}: {s.error.decode(errors='replace')}"
               for i, s in enumerate(sts) if s.state != capi.JOB_DONE]
-    # the plain path, one request after the other, on the first requests
     torch.cuda.synchronize()
-    k = min(args.plain_requests, len(reqs))
+    k = min(plain_requests, len(reqs))
     p0 = time.perf_counter()
     real_p = 0.0
     for r, ps in zip(reqs[:k], sets[:k]):
         cfg = sweep_config(capi, local, r["ne"], r["seed"], converge=True)
         cfg.n_phases = 16
-        cfg.max_seconds = args.request_cap_s
+        cfg.max_seconds = cap_s
         c = capi.Context(cfg)
         c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
         c.set_conditions(N_GAS, T_GAS, r["en"], r["angle"], r["freq"], r["red_mag"])
         real_p += c.solve().real_collisions
         c.close()
     p1 = time.perf_counter()
-    real_k = sum(s.result.real_collisions for s in sts[:k] if s.state == capi.JOB_DONE)
+    served = real / span
+    plain = real_p / (p1 - p0) if k else None
+    return {"workload": "serve_random_mixtures", "requests": len(reqs),
+            "arrivals": f"Poisson, mean gap {arrival_ms} ms (faster than the device serves them: the rate "
+                        f"measures capacity)", "slots": slots,
+            "mixtures": "1-5 random gases, 10-40 processes each on 100-400-point grids",
+            "E/N_Td": [1.0, 1000.0], "fields": "DC, crossed B (20 %), AC (20 %)",
+            "electrons_range": [1e4, SERVE_MAX_ELECTRONS],
+            "convergence": f"mean-energy standard error < {SWEEP_ERR:.1%}",
+            "value": served, "unit": UNIT,
+            "p50_s": _percentile(lat, 50), "p99_s": _percentile(lat, 99),
+            "latency": "submit to results on the host (lgpu_server_wait): queueing plus service",
+            "service_p50_s": _percentile(svc, 50), "service_p99_s": _percentile(svc, 99),
+            "completed": len(done), "capped": capped, "cap_s": cap_s, "failed": len(reqs) - len(done),
+            "errors": errors[:10], "span_s": span, "intervals": rep.intervals, "busy_s": rep.busy_seconds,
+            "peak_footprint_gb": rep.peak_footprint_bytes / 1e9,
+            "plain_first_requests": {"requests": k, "value": plain, "unit": UNIT, "wall_s": p1 - p0,
+                                     "note": "the first requests solved one after the other with lgpu_solve"},
+            "served_over_plain": served / plain if plain else None}
+
+
+def run_gpu_serve(args):
+    """Served request stream: latency percentiles, throughput, and the plain
+    sequential path on the first requests for comparison."""
+    from lokigpu import build as gbuild
+    from lokigpu import capi
+
+    rank, world, local = _init_ranks()
+    if not os.path.exists(capi.library_path()):
+        gbuild.build()
+    clocks = ClockSampler(local)
+    clocks.start()
+    blk = serve_stream(capi, local, args.requests, args.arrival_ms, args.request_cap_s, args.slots,
+                       args.plain_requests)
+    clk = clocks.stop()
     if rank == 0:
-        value = real / span
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(reqs), "warmup": 0,
-            "ms_per_step": 1e3 * span / len(reqs), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "serve_random_mixtures", "requests": len(reqs),
-                       "arrivals": f"Poisson, mean gap {args.arrival_ms} ms", "slots": args.slots,
-                       "mixtures": "1-5 random gases, 10-40 processes each on 100-400-point grids",
-                       "E/N_Td": [1.0, 1000.0], "electrons_range": [1e4, SERVE_MAX_ELECTRONS],
-                       "convergence": f"mean-energy standard error < {SWEEP_ERR:.1%}"},
-            "served": {"p50_s": _percentile(lat, 50), "p99_s": _percentile(lat, 99), "completed": len(done),
-                       "capped": capped, "cap_s": args.request_cap_s,
-                       "failed": len(reqs) - len(done), "errors": errors[:10], "span_s": span,
-                       "intervals": rep.intervals, "busy_s": rep.busy_seconds,
-                       "peak_footprint_gb": rep.peak_footprint_bytes / 1e9},
-            "plain_first_requests": {"requests": k, "value": real_p / (p1 - p0), "unit": UNIT,
-                                     "wall_s": p1 - p0,
-                                     "note": "the same requests solved one after the other with lgpu_solve"},
-            "clocks": clk,
+            "metric": METRIC, "value": blk["value"], "unit": UNIT, "n_gpus": world, "steps": blk["requests"],
+            "warmup": 0, "ms_per_step": 1e3 * blk["span_s"] / blk["requests"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {k: blk[k] for k in ("workload", "requests", "arrivals", "slots", "mixtures", "E/N_Td",
+                                           "electrons_range", "convergence")},
+            "served": blk, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
+        import torch
         torch.distributed.destroy_process_group()
     return 0
 
@@ -783,7 +974,7 @@ def run_gpu_n2(args):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample, cores = cpu_sample(args.cpu_seconds, os.cpu_count() or 1, "n2_200td")
+            v, sample, cores, _ = cpu_sample(args.cpu_seconds, os.cpu_count() or 1, "n2_200td")
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -818,14 +1009,18 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="sweep", choices=["sweep", "n2_200td", "serve"])
     ap.add_argument("--requests", type=int, default=100, help="serve: requests in the stream")
+    ap.add_argument("--stream-requests", type=int, default=500,
+                    help="sweep: requests of the random-mixture stream served after the sweep (0: none)")
+    ap.add_argument("--stream-arrival-ms", type=float, default=2.0, help="sweep: mean gap of the stream's arrivals")
     ap.add_argument("--request-cap-s", type=float, default=60.0, help="serve: wall-time cap of one request")
     ap.add_argument("--slots", type=int, default=64, help="serve: jobs advanced together")
-    ap.add_argument("--plain-requests", type=int, default=16, help="serve: requests also solved one by one")
+    ap.add_argument("--plain-requests", type=int, default=8, help="serve: requests also solved one by one")
     ap.add_argument("--electrons", type=int, default=N_ELECTRONS, help="n2_200td only")
     ap.add_argument("--relax", type=int, default=None)
     ap.add_argument("--plain-steps", type=int, default=20, help="sweep: timed plain intervals per condition")
     ap.add_argument("--arrival-ms", type=float, default=20.0, help="sweep: mean gap of the served arrivals")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-precision", action="store_true", help="skip the study against the FP64 reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")

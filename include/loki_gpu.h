@@ -391,6 +391,11 @@ int lgpu_server_wait(lgpu_server* server, long long job_id, double timeout_s, lg
 int lgpu_server_job_rates(lgpu_server* server, long long job_id, unsigned long long* counts, double* rate, int n);
 /* A queued job is dropped; a running one stops at its next interval. */
 int lgpu_server_cancel(lgpu_server* server, long long job_id);
+/* Drops the record of a finished (done, failed or cancelled) job: its status,
+ * results and rates are no longer available (LGPU_ERR_STATE for a job still
+ * queued or running). A long-running server keeps the records of its last
+ * 65536 finished jobs in any case and drops older ones. */
+int lgpu_server_forget(lgpu_server* server, long long job_id);
 int lgpu_server_report_get(lgpu_server* server, lgpu_server_report* report);
 int lgpu_server_last_error(const lgpu_server* server, char* buf, size_t size);
 /* Cancels what is left, joins the thread, frees the device memory. */

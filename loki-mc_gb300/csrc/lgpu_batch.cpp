@@ -125,9 +125,7 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
   }
-  b.members_.clear();
-  b.active_.clear();
-  b.next_start_ = 0;
+  b.clear_members();
   return rc;
 }
 

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <deque>
 #include <map>
 #include <string>
 #include <vector>
@@ -76,12 +77,38 @@ class Batch {
   struct Member {
     Engine* e = nullptr;
     bool started = false, done = false;
+    bool released = false;  // done and no longer looked at by its owner
     int status = LGPU_OK;
     lgpu_result result{};
   };
-  std::vector<Member> members_;
-  std::vector<int> active_;  // started, unfinished members
-  size_t next_start_ = 0;    // first member not started yet
+  // Members by id, in the order added: member id k is members_[k - base_].
+  // A long-running owner (the server) releases finished members, and
+  // compact() drops released ones from the front, so the bookkeeping stays
+  // bounded by the members added during the longest running one's solve.
+  std::deque<Member> members_;
+  int base_ = 0;             // id of members_.front()
+  std::vector<int> active_;  // ids of started, unfinished members
+  int next_start_ = 0;       // id of the first member not started yet
+
+  Member& member(int id) { return members_[(size_t)(id - base_)]; }
+  int end_id() const { return base_ + (int)members_.size(); }
+  void release_member(int id) {
+    Member& m = member(id);
+    m.e = nullptr;
+    m.released = true;
+  }
+  void compact() {
+    while (!members_.empty() && members_.front().released && base_ < next_start_) {
+      members_.pop_front();
+      ++base_;
+    }
+  }
+  void clear_members() {
+    members_.clear();
+    active_.clear();
+    base_ = 0;
+    next_start_ = 0;
+  }
 
   ~Batch() { release(); }
 
@@ -131,8 +158,7 @@ class Batch {
     if (stream_) cudaStreamSynchronize(stream_);
     for (Member& m : members_)
       if (m.e && !m.done) m.e->leave_batch();
-    members_.clear();
-    active_.clear();
+    clear_members();
     for (auto& g : graphs_) cudaGraphExecDestroy(g.second.first);
     graphs_.clear();
     if (d_stage_) cudaFree(d_stage_);
@@ -222,21 +248,21 @@ class Batch {
 
   // starts waiting members while slots are free
   void admit() {
-    while ((int)active_.size() < max_slots_ && next_start_ < members_.size()) {
-      Member& m = members_[next_start_];
+    while ((int)active_.size() < max_slots_ && next_start_ < end_id()) {
+      Member& m = member(next_start_);
       m.started = true;
       const int rc = m.e->solve_begin();
       if (rc != LGPU_OK) finish(m, rc);
-      else active_.push_back((int)next_start_);
+      else active_.push_back(next_start_);
       ++next_start_;
     }
   }
 
-  bool idle() const { return active_.empty() && next_start_ >= members_.size(); }
+  bool idle() const { return active_.empty() && next_start_ >= end_id(); }
 
   // ends a running member between intervals with the given status
   void stop_member(int idx, int status) {
-    Member& m = members_[idx];
+    Member& m = member(idx);
     if (!m.started || m.done) return;
     m.e->sync("stop");
     m.status = status;
@@ -257,7 +283,7 @@ class Batch {
     std::vector<int> go, wait;
     go.reserve(active_.size());
     for (int idx : active_) {
-      Member& m = members_[idx];
+      Member& m = member(idx);
       bool done = false, ready = true;
       int rc = m.e->solve_next(&done);
       if (rc == LGPU_OK && !done) rc = m.e->interval_pre(&ready);
@@ -276,12 +302,12 @@ class Batch {
     if (go.empty()) {
       // only re-grids in flight: let them finish before the next step
       for (int idx : wait)
-        if (int rc = members_[idx].e->settle_tables()) return rc;
+        if (int rc = member(idx).e->settle_tables()) return rc;
       return LGPU_OK;
     }
     // slots ordered by field branch: one advance launch per branch
     std::stable_sort(go.begin(), go.end(),
-                     [&](int a, int b) { return members_[a].e->field_mode() < members_[b].e->field_mode(); });
+                     [&](int a, int b) { return member(a).e->field_mode() < member(b).e->field_mode(); });
     const int n = (int)go.size();
     auto* hdr = reinterpret_cast<BatchHeader*>(h_stage_);
     int* ap = reinterpret_cast<int*>(h_stage_ + batch_prefix_offset());
@@ -295,7 +321,7 @@ class Batch {
     double electrons = 0;
     const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
     for (int s = 0; s < n; ++s) {
-      Engine* e = members_[go[s]].e;
+      Engine* e = member(go[s]).e;
       e->fill_slot(&sl[s]);
       if (e->cfg_.advance_real_batch == 0) {
         sl[s].adv.real_batch = tune_threshold(cand);
@@ -319,7 +345,7 @@ class Batch {
     hdr->smp_chunks = smp.first + smp.second;
     if (hdr->smp_chunks) parts |= kPartSample;
     for (int m = 0, s = 0; m <= kFieldModes; ++m) {
-      while (s < n && members_[go[s]].e->field_mode() < m) ++s;
+      while (s < n && member(go[s]).e->field_mode() < m) ++s;
       hdr->mode_chunk[m] = ap[s];
       hdr->mode_slot[m] = s;
     }
@@ -362,7 +388,7 @@ class Batch {
     std::vector<int> still;
     still.reserve(go.size());
     for (int s = 0; s < n; ++s) {
-      Member& m = members_[go[s]];
+      Member& m = member(go[s]);
       real_ += (double)(h_gather_[s].real_count - m.e->h_sc_->real_count);
       null_ += (double)(h_gather_[s].null_count - m.e->h_sc_->null_count);
       secondaries_ += h_gather_[s].sec_count;
@@ -380,7 +406,7 @@ class Batch {
     }
     // re-grids end within the step that launched them (they ran beside it)
     for (int idx : wait)
-      if ((rc = members_[idx].e->settle_tables())) return rc;
+      if ((rc = member(idx).e->settle_tables())) return rc;
     still.insert(still.end(), wait.begin(), wait.end());
     active_ = still;
     const auto h3 = std::chrono::steady_clock::now();
@@ -404,7 +430,7 @@ class Batch {
     take_.clear();
     for (int idx : active_) {
       HistArgs h;
-      if (!members_[idx].e->take_pending_hist(&h)) continue;
+      if (!member(idx).e->take_pending_hist(&h)) continue;
       sl[n++].hist = h;
       n_.push_back(h.n);
       take_.push_back(h.cylindrical && !h.evdf_done ? 1 : 0);  // pass B: the EVDF not counted yet

@@ -29,7 +29,8 @@ namespace lgpu {
 struct JobRec {
   long long id = 0;
   lgpu_config cfg{};
-  std::vector<lgpu_process> procs;
+  int n_procs = 0;
+  std::vector<lgpu_process> procs;  // until admission (the context copies them)
   std::vector<std::vector<double>> raw_e, raw_v;
   std::vector<lgpu_gas> gases;
   double emax = 0;
@@ -60,8 +61,14 @@ class Server {
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
   std::deque<long long> queue_;
-  std::map<long long, std::unique_ptr<JobRec>> jobs_;
+  std::map<long long, std::shared_ptr<JobRec>> jobs_;  // a waiter keeps its record alive
   std::vector<JobRec*> running_;  // worker-only
+  // finished jobs in the order they finished: their records (results, rates)
+  // are kept until lgpu_server_forget or until more than kRetainFinished
+  // finished jobs are held, when the oldest go first
+  static constexpr size_t kRetainFinished = 1 << 16;
+  std::deque<long long> finished_;
+  long long running_count_ = 0;
   bool stop_ = false;
   long long next_id_ = 1;
   long long submitted_ = 0, completed_ = 0, failed_ = 0, intervals_ = 0;
@@ -96,8 +103,9 @@ class Server {
     if (j.n_procs < 1 || j.n_procs > kMaxProcesses || j.n_gases < 1 || j.n_gases > kMaxGases || !j.procs || !j.gases)
       return LGPU_ERR_BAD_ARG;
     if (j.config.n_electrons < 1) return LGPU_ERR_BAD_ARG;
-    auto r = std::make_unique<JobRec>();
+    auto r = std::make_shared<JobRec>();
     r->cfg = j.config;
+    r->n_procs = j.n_procs;
     r->cfg.device = device_;
     r->procs.assign(j.procs, j.procs + j.n_procs);
     r->raw_e.resize(j.n_procs);
@@ -155,7 +163,7 @@ class Server {
     std::unique_lock<std::mutex> lock(mu_);
     auto it = jobs_.find(id);
     if (it == jobs_.end()) return LGPU_ERR_BAD_ARG;
-    JobRec* r = it->second.get();
+    const std::shared_ptr<JobRec> r = it->second;
     auto pred = [&] { return final_state(r->state); };
     if (timeout_s > 0) {
       if (!cv_done_.wait_for(lock, std::chrono::duration<double>(timeout_s), pred)) {
@@ -175,6 +183,7 @@ class Server {
     if (it == jobs_.end()) return LGPU_ERR_BAD_ARG;
     const JobRec& r = *it->second;
     if (r.state != LGPU_JOB_DONE) return LGPU_ERR_STATE;
+    if (n != r.n_procs) return LGPU_ERR_BAD_ARG;
     if (n != (int)r.rate.size()) return LGPU_ERR_BAD_ARG;
     for (int p = 0; p < n; ++p) {
       if (counts) counts[p] = r.counts[p];
@@ -206,9 +215,7 @@ class Server {
     rep->completed = completed_;
     rep->failed = failed_;
     rep->queued = (long long)queue_.size();
-    long long running = 0;
-    for (auto& kv : jobs_) running += kv.second->state == LGPU_JOB_RUNNING;
-    rep->running = running;
+    rep->running = running_count_;
     rep->intervals = intervals_;
     rep->real_collisions = real_;
     rep->null_collisions = null_;
@@ -227,7 +234,24 @@ class Server {
 
   // ---------------------------------------------------------------- worker
   // (called with the mutex held) ends a job, frees its context
+  // drops the record of a finished job (lgpu_server_forget)
+  int forget(long long id) {
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return LGPU_ERR_BAD_ARG;
+    if (!final_state(it->second->state)) return LGPU_ERR_STATE;
+    jobs_.erase(it);
+    finished_.erase(std::remove(finished_.begin(), finished_.end(), id), finished_.end());
+    return LGPU_OK;
+  }
+
   void retire(JobRec* r, int state, int status) {
+    if (r->state == LGPU_JOB_RUNNING) --running_count_;
+    finished_.push_back(r->id);
+    while (finished_.size() > kRetainFinished) {
+      jobs_.erase(finished_.front());
+      finished_.pop_front();
+    }
     r->state = state;
     r->status = status;
     r->t_end = now();
@@ -244,7 +268,11 @@ class Server {
   }
 
   void destroy_engine(JobRec* r) {
-    if (r->member >= 0) batch_.members_[r->member].e = nullptr;
+    if (r->member >= 0) {
+      batch_.release_member(r->member);
+      batch_.compact();
+      r->member = -1;
+    }
     delete r->engine;
     r->engine = nullptr;
   }
@@ -259,9 +287,13 @@ class Server {
     if (rc == LGPU_OK) rc = e->set_conditions(r->cond);
     if (rc == LGPU_OK) rc = batch_.add(e);
     if (rc != LGPU_OK) return rc;
-    r->member = (int)batch_.members_.size() - 1;
+    r->member = batch_.end_id() - 1;
+    // the context holds its own copies of the inputs from here on
+    std::vector<lgpu_process>().swap(r->procs);
+    std::vector<std::vector<double>>().swap(r->raw_e);
+    std::vector<std::vector<double>>().swap(r->raw_v);
     batch_.admit();
-    const Batch::Member& m = batch_.members_[r->member];
+    const Batch::Member& m = batch_.member(r->member);
     if (m.done) return m.status == LGPU_OK ? LGPU_ERR_STATE : m.status;
     return LGPU_OK;
   }
@@ -292,6 +324,7 @@ class Server {
           r->holds = true;
           peak_ = std::max(peak_, held_);
           r->state = LGPU_JOB_RUNNING;
+          ++running_count_;
           r->t_start = now();
           admit.push_back(r);
         }
@@ -351,12 +384,12 @@ class Server {
         if (it == running_.end()) continue;
         JobRec* r = *it;
         running_.erase(it);
-        const Batch::Member& m = batch_.members_[idx];
+        const Batch::Member& m = batch_.member(idx);
         int status = m.status;
         std::vector<unsigned long long> counts;
         std::vector<double> rate;
         if (status == LGPU_OK) {
-          const int P = (int)r->procs.size();
+          const int P = r->n_procs;
           counts.resize(P);
           rate.resize(P);
           status = r->engine->process_results(counts.data(), rate.data(), nullptr, nullptr, P);
@@ -440,6 +473,11 @@ int lgpu_server_job_rates(lgpu_server* server, long long job_id, unsigned long l
 int lgpu_server_cancel(lgpu_server* server, long long job_id) {
   if (!server || !server->s) return LGPU_ERR_BAD_ARG;
   return server->s->cancel(job_id);
+}
+
+int lgpu_server_forget(lgpu_server* server, long long job_id) {
+  if (!server || !server->s) return LGPU_ERR_BAD_ARG;
+  return server->s->forget(job_id);
 }
 
 int lgpu_server_report_get(lgpu_server* server, lgpu_server_report* report) {

@@ -32,7 +32,7 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
             "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
-            "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_report_get", "lgpu_server_last_error",
+            "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_forget", "lgpu_server_report_get", "lgpu_server_last_error",
             "lgpu_server_stop")
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
@@ -168,6 +168,7 @@ def load(path: str | None = None):
     lib.lgpu_server_wait.argtypes = [VP, LL, D, P_(JobStatus)]
     lib.lgpu_server_job_rates.argtypes = [VP, LL, P_(ctypes.c_ulonglong), P_(D), I]
     lib.lgpu_server_cancel.argtypes = [VP, LL]
+    lib.lgpu_server_forget.argtypes = [VP, LL]
     lib.lgpu_server_report_get.argtypes = [VP, P_(ServerReport)]
     lib.lgpu_server_last_error.argtypes = [VP, ctypes.c_char_p, ctypes.c_size_t]
     lib.lgpu_server_stop.argtypes = [VP]
@@ -497,6 +498,11 @@ class Server:
         rc = self.lib.lgpu_server_cancel(self.h, int(jid))
         if rc != LGPU_OK:
             raise LokiGpuError(rc, "lgpu_server_cancel failed")
+
+    def forget(self, jid):
+        rc = self.lib.lgpu_server_forget(self.h, int(jid))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_forget failed")
 
     def report(self) -> ServerReport:
         r = ServerReport()

@@ -825,10 +825,12 @@ int lo_run(const lo_procs* pr_in, lo_fields* f, const lo_run_config* cfg, lo_run
     double t_sync = time + dt_sync;
     ++nSync;
     ++sync_steps;
-    if (cfg->mark_sync_step > 0 && sync_steps == cfg->mark_sync_step + 1) {
+    if ((cfg->mark_sync_step > 0 && sync_steps == cfg->mark_sync_step + 1) ||
+        (cfg->mark_seconds > 0 && res->mark_elapsed == 0 && now_s() - t_start > cfg->mark_seconds)) {
       res->mark_real_collisions = (double)(total_coll);
       res->mark_null_collisions = (double)null_coll;
       res->mark_elapsed = now_s() - t_start;
+      res->mark_sync_steps = sync_steps - 1;
     }
     memset(adv, 1, N);
     int any = 1;

@@ -132,6 +132,7 @@ typedef struct lo_run_config {
   double max_seconds;              /* wall-clock cap (<=0: none); used to bound baseline samples */
   long long max_sync_steps;        /* cap on synchronisation intervals (<=0: none) */
   long long mark_sync_step;        /* record collisions and wall time after this many intervals (<=0: none) */
+  double mark_seconds;             /* or at the first interval that starts after this wall time (<=0: none) */
 } lo_run_config;
 
 typedef struct lo_run_result {
@@ -147,6 +148,7 @@ typedef struct lo_run_result {
   double elapsed;
   long long sync_steps;
   double mark_real_collisions, mark_null_collisions, mark_elapsed;
+  long long mark_sync_steps;       /* intervals begun before the mark */
   int status;                      /* 0 ok, 1 energy above elastic table, 2 capped by time/steps */
 } lo_run_result;
 

@@ -61,7 +61,7 @@ class RunConfig(ctypes.Structure):
                 ("req_err_bulk_v", D), ("req_err_bulk_d", D), ("req_err_power", D), ("n_energy_cells", I),
                 ("n_cos_cells", I), ("n_radial_cells", I), ("n_axial_cells", I), ("n_phases", I),
                 ("cylindrical", I), ("max_seconds", D), ("max_sync_steps", ctypes.c_longlong),
-                ("mark_sync_step", ctypes.c_longlong)]
+                ("mark_sync_step", ctypes.c_longlong), ("mark_seconds", D)]
 
 
 class RunResult(ctypes.Structure):
@@ -72,7 +72,7 @@ class RunResult(ctypes.Structure):
                 ("integration_points", D), ("trial_freq", D), ("power_field", D), ("power_growth", D),
                 ("power_balance_rel_err", D), ("max_eedf_energy", D), ("elapsed", D),
                 ("sync_steps", ctypes.c_longlong), ("mark_real_collisions", D), ("mark_null_collisions", D),
-                ("mark_elapsed", D), ("status", I)]
+                ("mark_elapsed", D), ("mark_sync_steps", ctypes.c_longlong), ("status", I)]
 
 
 _lib = None

@@ -241,3 +241,32 @@ def test_batch_and_server_with_different_mixtures():
         fails += _statistically_equal(spec, a, (st.result, counts, rate))
     srv.stop()
     assert not fails, "\n".join(fails)
+
+
+def test_server_forgets_finished_jobs():
+    """A long-running server drops the records of finished jobs on request
+    (lgpu_server_forget) and recycles the batch's bookkeeping of finished
+    jobs, so many small jobs in a row run through a few slots."""
+    from lokigpu import capi
+    ps, arrays = _inputs("atomic")
+    cfg = _config(4096, 7)
+    cfg.req_integration_points = 50.0
+    cfg.max_coll_before_ss = 20.0
+    srv = capi.Server(0, 3)
+    ids = [srv.submit(cfg, ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"], N_GAS, 300.0,
+                      100.0 + k) for k in range(24)]
+    with pytest.raises(capi.LokiGpuError) as e:  # not finished yet: still queued
+        srv.forget(ids[-1])
+    assert e.value.code == 6
+    sts = [srv.wait(j, 300.0) for j in ids]
+    assert all(s.state == capi.JOB_DONE for s in sts), [(s.state, s.error) for s in sts]
+    counts, rate = srv.rates(ids[0], ps.n)
+    assert counts.sum() > 0
+    for j in ids[:12]:
+        srv.forget(j)
+    with pytest.raises(capi.LokiGpuError):
+        srv.poll(ids[0])
+    assert srv.poll(ids[12]).state == capi.JOB_DONE
+    rep = srv.report()
+    srv.stop()
+    assert rep.completed == 24 and rep.running == 0 and rep.queued == 0

@@ -150,9 +150,11 @@ def test_collisions(gpu_case):
         c2.close()
         # same decisions and uniform counts; the kinematics inlined in the
         # two replay paths may contract multiply-adds differently (thermal
-        # targets), so they agree to a few FP32 units in the last place
+        # targets, where a cancellation can amplify the last bit), so they
+        # agree to the kinematics tolerance
         assert np.array_equal(out[:, 0], out_c[:, 0]) and np.array_equal(used, used_c), (name, m)
-        np.testing.assert_allclose(out_c, out, rtol=2e-6, atol=1e-6 * float(np.max(np.abs(out[:, 1:4]))))
+        for k in range(len(nu)):
+            assert _kinematics_agree(out_c[k], out[k], en[k], 1e-5), (name, m, k, out_c[k], out[k])
         f = O.make_fields(sc[0], sc[1], gas_temp_effect=int(gte), sharing=int(shr), sharing_factor=fac)
         mismatch, compared, real = 0, 0, 0
         for k in range(len(nu)):
