@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference source tree (never on the GPU machine):
 
-    make -C oracle/ref                      # builds oracle/_ref/libref_harness.so
+    make -C oracle/ref REF=<reference Code/>   # builds oracle/_ref/libref_harness.so
     python tests/golden/make_golden.py      # writes tests/golden/*.npz
     python tests/golden/make_golden.py --stats   # also the long seeded solves
 
@@ -19,7 +19,10 @@ process, and records:
   recorded stream of uniforms, cold and thermal, for each ionization
   energy-sharing mode, with the number of uniforms consumed;
 * with --stats, full seeded solves (BoltzmannMC.C:273-297) whose swarm
-  parameters pin the statistical parity tests.
+  parameters, rate coefficients, power terms and distributions (EEDF, EADF,
+  anisotropies, EVDF, periodic averages, as cumulative probabilities on
+  sub-grids of the reference's own cells) pin the statistical parity tests;
+  --stats-only runs just those, --only NAME one case.
 """
 from __future__ import annotations
 
@@ -36,6 +39,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "loki-mc_gb300", "python"))
+sys.path.insert(0, os.path.dirname(HERE))
 from lokigpu import synth  # noqa: E402
 from lokigpu import constants as C  # noqa: E402
 
@@ -75,6 +79,12 @@ def case_gases(name):
         synth.assign_sampler(n2, "Excitation", "coulombScreen", (1.0, 2.7))
         synth.assign_sampler(o2, "Excitation", "coulombScreen", (0.0, 0.8))
         return [n2, o2], dict(N=3.22e22, red_field=150.0, max_e=120.0, sharing="equalSharing")
+    if name == "sweep":
+        # the 64-point E/N sweep's mixture (bench.py: sweep_processes): tables
+        # to 1e4 eV, default samplers
+        n2 = synth.n2_like_gas(fraction=0.8, e_max=1e4)
+        o2 = synth.o2_like_gas(fraction=0.2, e_max=1e4)
+        return [n2, o2], dict(N=3.22e22, red_field=100.0, max_e=120.0, sharing="equalSharing")
     raise KeyError(name)
 
 
@@ -254,22 +264,71 @@ def run_case(name, out_path, seed):
 # ------------------------------------------------------------------ seeded solves
 
 STAT_CASES = {
-    # name: (gas case, overrides, numerics)
-    "atomic_dc100": ("atomic", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "1E3"}),
-    "n2_dc200": ("n2", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
-    "mix_dc100": ("mix", {}, {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
-    # omega/N = 1e-14 m^3/s: a 20 ns field period, so the 3000 integration
-    # intervals (~0.1 ns each) average over some 15 periods
+    # name: (gas case, overrides, numerics); 1e4 integration intervals of 1e5
+    # electrons, so that the reference's own batch-means errors are a few
+    # 0.01 % on the mean energy and the drift velocities; the reference's
+    # default 1e4 table points (a coarser table moves the rates of processes
+    # whose cross section jumps at threshold by up to ~1 %, depending on where
+    # the threshold falls between the grid points of the run's own table)
+    "atomic_dc100": ("atomic", {}, {"nIntegrationPoints": "1E4", "nInterpPoints": "10000",
+                                    "maxCollisionsBeforeSteadyState": "1E3"}),
+    "n2_dc200": ("n2", {}, {"nIntegrationPoints": "1E4", "nInterpPoints": "10000",
+                            "maxCollisionsBeforeSteadyState": "300"}),
+    "mix_dc100": ("mix", {}, {"nIntegrationPoints": "1E4", "nInterpPoints": "10000",
+                              "maxCollisionsBeforeSteadyState": "300"}),
+    # omega/N = 1e-14 m^3/s: a 20 ns field period, so the 1e4 integration
+    # intervals (~0.1 ns each) average over some 50 periods
     "mix_ac150": ("mix", {"red_field": 150.0, "freq": 3.22e22 * 1e-14 / (2 * np.pi)},
-                  {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300", "nIntegrationPhases": "64"}),
+                  {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300",
+                   "nIntegrationPhases": "64"}),
     "mix_b100": ("mix", {"red_field": 100.0, "red_mag": 1000.0, "angle": 90.0},
-                 {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
+                 {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300"}),
     "n2_dc200_thermal": ("n2", {"gas_temp": "smartActivation"},
-                         {"nIntegrationPoints": "3000", "maxCollisionsBeforeSteadyState": "300"}),
+                         {"nIntegrationPoints": "1E4", "nInterpPoints": "10000",
+                          "maxCollisionsBeforeSteadyState": "300"}),
 }
 
 
+def dist_record(lib, cells, eedf):
+    """The reference's distributions as cumulative probabilities on sub-grids
+    of its own cell nodes (tests/golden_util.py: cdf_at, eadf_mass,
+    legendre_mass, evdf_cdf), compact enough to commit."""
+    import golden_util as gu
+
+    sz = np.zeros(7, np.int32)
+    lib.ref_dist_sizes(sz.ctypes.data_as(VP))
+    nE, nC, nR, nA, nPh, cyl, ac = (int(x) for x in sz)
+    nodes = gu.energy_nodes(cells)
+    e_edges = nodes[::5]
+    rec = dict(e_edges=e_edges, eedf_cdf=gu.cdf_at(nodes, gu.eedf_mass(cells, eedf), e_edges))
+    if cyl:
+        f1, f2 = np.zeros(nE), np.zeros(nE)
+        eadf, evdf = np.zeros(nE * nC), np.zeros(nR * nA)
+        rc, acc = np.zeros(nR), np.zeros(nA)
+        lib.ref_get_anisotropic(ptr(f1), ptr(f2), ptr(eadf), ptr(evdf), ptr(rc), ptr(acc))
+        rec["eadf_cdf"] = gu.cdf_at(nodes, gu.eadf_mass(cells, eadf.reshape(nE, nC), 10), e_edges)
+        rec["f1_cdf"] = gu.cdf_at(nodes, gu.legendre_mass(cells, f1, 1), e_edges)
+        rec["f2_cdf"] = gu.cdf_at(nodes, gu.legendre_mass(cells, f2, 2), e_edges)
+        dr, dz = rc[1] - rc[0], acc[1] - acc[0]
+        r_edges = (np.arange(nR + 1) * dr)[::4]
+        z_edges = (acc[0] - 0.5 * dz + np.arange(nA + 1) * dz)[::4]
+        rec.update(r_edges=r_edges, z_edges=z_edges,
+                   evdf_cdf=gu.evdf_cdf(rc, acc, evdf.reshape(nR, nA), r_edges, z_edges))
+    if ac:
+        n, me = np.zeros(nPh), np.zeros(nPh)
+        fv, bv, fd, bd = np.zeros(3 * nPh), np.zeros(3 * nPh), np.zeros(9 * nPh), np.zeros(9 * nPh)
+        per = np.zeros(nPh * nE)
+        lib.ref_get_periodic(ptr(n), ptr(me), ptr(fv), ptr(bv), ptr(fd), ptr(bd), ptr(per))
+        per = per.reshape(nPh, nE)
+        pe = e_edges[::2]
+        rec.update(per_n=n, per_mean_energy=me, per_flux_v=fv.reshape(nPh, 3), per_bulk_v=bv.reshape(nPh, 3),
+                   per_flux_d=fd.reshape(nPh, 9), per_bulk_d=bd.reshape(nPh, 9), per_e_edges=pe,
+                   per_eedf_cdf=np.stack([gu.cdf_at(nodes, gu.eedf_mass(cells, per[q]), pe) for q in range(nPh)]))
+    return rec
+
+
 def run_stats(name, out_path, seed, n_electrons):
+    out_path = os.path.abspath(out_path)  # open_ref changes the working directory
     case, over, numerics = STAT_CASES[name]
     tmp = tempfile.mkdtemp(prefix=f"stats_{name}_")
     gases, meta, setup = write_inputs(case, tmp, n_electrons=n_electrons, extra=numerics, **over)
@@ -282,10 +341,14 @@ def run_stats(name, out_path, seed, n_electrons):
     nc = lib.ref_n_eedf_cells()
     cells, eedf = np.zeros(nc), np.zeros(nc)
     lib.ref_get_eedf(ptr(cells), ptr(eedf))
+    gain, loss = np.zeros(P), np.zeros(P)
+    lib.ref_get_power(ptr(gain), ptr(loss))
     rec = dict(case=case, overrides={k: v for k, v in over.items()}, numerics=numerics, n_electrons=n_electrons,
-               seed=seed, result=r.tolist(), rate=rate.tolist(), eedf_cells=cells.tolist(), eedf=eedf.tolist())
+               seed=seed, result=r.tolist(), rate=rate.tolist(), power_gain=gain.tolist(), power_loss=loss.tolist(),
+               eedf_cells=cells.tolist(), eedf=eedf.tolist())
     with open(out_path, "w") as f:
         json.dump(rec, f)
+    np.savez_compressed(out_path[:-5] + "_dist.npz", **dist_record(lib, cells, eedf))
 
 
 def _child(args):
@@ -300,12 +363,15 @@ def _child(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--stats", action="store_true")
+    ap.add_argument("--stats-only", action="store_true", help="only the seeded solves")
     ap.add_argument("--only", default=None)
-    ap.add_argument("--ne", type=float, default=1e4)
+    ap.add_argument("--ne", type=float, default=1e5)
     a = ap.parse_args()
+    if a.stats_only:
+        a.stats = True
     jobs = []
     for i, name in enumerate(("atomic", "n2", "mix", "screen")):
-        if a.only and name != a.only:
+        if a.stats_only or (a.only and name != a.only):
             continue
         jobs.append(("kin", name, os.path.join(HERE, f"kin_{name}.npz"), 1000 + i, 0))
     if a.stats:
@@ -313,8 +379,9 @@ def main():
             if a.only and name != a.only:
                 continue
             jobs.append(("stats", name, os.path.join(HERE, f"stats_{name}.json"), 77 + i, a.ne))
+    # the seeded solves use every core (OpenMP), one after the other
     ctx = mp.get_context("spawn")
-    with ctx.Pool(min(len(jobs), 4)) as pool:
+    with ctx.Pool(1 if a.stats else min(len(jobs), 4)) as pool:
         for p in pool.imap_unordered(_child, jobs):
             print("wrote", os.path.relpath(p, ROOT))
 
