@@ -336,6 +336,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
     h2d = d2h = host_ms = secondaries = spilled = regrids = 0.0
     real_batch = 0
     coarse = -1
+    shape = (0, 0, 0)
     for _ in range(args.steps):
         flush.add_(1.0)                    # L2 flush (256 MiB written), outside the timed region
         torch.cuda.synchronize()
@@ -361,12 +362,13 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         assert running == len(conds)
         real_batch = rep.real_batch
         coarse = rep.coarse_null_test
+        shape = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk)
     del b
     for c in ctxs:
         c.close()
     return dict(total_ms=total_ms, real=real, null=null, adv_ms=adv_ms, electron_steps=steps, launches=launches,
                 intervals=intervals, h2d=h2d, d2h=d2h, host_ms=host_ms, secondaries=secondaries, spilled=spilled,
-                real_batch=real_batch, coarse=coarse, regrids=regrids)
+                real_batch=real_batch, coarse=coarse, regrids=regrids, shape=shape)
 
 
 def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
@@ -730,6 +732,13 @@ def run_gpu_sweep(args):
                        "host_ms_per_step": tb["host_ms"] / args.steps,
                        "secondaries_per_step": tb["secondaries"] / args.steps,
                        "spilled_per_step": tb["spilled"] / args.steps,
+                       "autotuned": {"threads_per_block": tb["shape"][0], "blocks_per_sm": tb["shape"][1],
+                                     "electrons_per_warp_claim": tb["shape"][2],
+                                     "collision_turn_threshold": tb["real_batch"],
+                                     "table_staging": {1.0: "block bounds in shared memory, rows from L2",
+                                                       0.0: "rows from L2"}.get(tb["coarse"], "tuning"),
+                                     "scope": "on-line, per mixture (largest process count, table points, "
+                                              "field branches, thermal targets)"},
                        "collision_turn_threshold": tb["real_batch"], "coarse_null_test": tb["coarse"],
                        "regrids_per_step": tb["regrids"] / max(args.steps, 1)},
             "plain": plain, "batched_over_plain": ratio or None, "served": served, "served_stream": stream,

@@ -302,6 +302,10 @@ typedef struct lgpu_batch_report {
   double coarse_null_test;      /* 1: null tests try the block bounds first, 0: not, -1: being tuned */
   double regrids;               /* energy-grid re-builds, each overlapped with a batched interval the
                                    context sat out */
+  double advance_threads;       /* launch shape of the advance chosen by the on-line tuner (0 while it is
+                                   being tuned): threads per block, */
+  double advance_blocks_per_sm; /* blocks per SM (the register budget), */
+  double advance_chunk;         /* electrons a warp takes at a time */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);

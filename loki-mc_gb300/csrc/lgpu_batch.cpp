@@ -77,6 +77,11 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
     report->regrids = b.regrids_ - rg0;
     report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
+    int th = 0, bl = 0, ch = 0;
+    lgpu::advance_shape(b.shape_, &th, &bl, &ch);
+    report->advance_threads = b.tune_stage_ >= 1 ? th : 0;
+    report->advance_blocks_per_sm = b.tune_stage_ >= 1 ? bl : 0;
+    report->advance_chunk = b.tune_stage_ >= 1 ? ch : 0;
   }
   return rc;
 }
@@ -124,6 +129,11 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->regrids = b.regrids_ - rg0;
     report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
+    int th = 0, bl = 0, ch = 0;
+    lgpu::advance_shape(b.shape_, &th, &bl, &ch);
+    report->advance_threads = b.tune_stage_ >= 1 ? th : 0;
+    report->advance_blocks_per_sm = b.tune_stage_ >= 1 ? bl : 0;
+    report->advance_chunk = b.tune_stage_ >= 1 ? ch : 0;
   }
   b.clear_members();
   return rc;

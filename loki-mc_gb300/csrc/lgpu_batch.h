@@ -22,7 +22,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <array>
 #include <deque>
+#include <mutex>
 #include <map>
 #include <string>
 #include <vector>
@@ -58,21 +60,60 @@ class Batch {
   double real_ = 0, null_ = 0;  // collisions of the batched intervals
   double host_ms_ = 0, secondaries_ = 0, spilled_ = 0, attached_ = 0, regrids_ = 0;
 
-  // On-line tuning of two scheduling choices of the advance for members whose
-  // config leaves the threshold at 0: the collision-turn threshold
-  // (AdvanceArgs::real_batch) and whether the null test tries the block
-  // bounds first (AdvanceArgs::coarse). Neither changes what an electron
-  // draws or decides, so tuning intervals are ordinary intervals: the
-  // candidates take turns, kTuneRounds times each, and the one with the least
-  // advance time per electron-interval (median) is kept.
+  // On-line autotuner of the advance's scheduling, which changes no result
+  // (what an electron draws and decides does not depend on it), so tuning
+  // intervals are ordinary intervals. Two stages, each candidate taking
+  // kTuneRounds intervals and the least advance time per electron-interval
+  // (median) winning:
+  //  0. the launch shape (kAdvShapes: threads per block x blocks per SM, i.e.
+  //     the register budget, and the electrons a warp takes at a time);
+  //  1. for members whose config leaves the threshold at 0, the
+  //     collision-turn threshold (AdvanceArgs::real_batch) and the table
+  //     staging of the null test: block bounds of the total frequency staged
+  //     in shared memory first, or the table rows straight from L2
+  //     (AdvanceArgs::coarse).
+  // The choice is kept per mixture, keyed by (largest process count, table
+  // points, field branches in use, thermal targets), for the life of the
+  // process: a later batch or server interval with the same key starts tuned.
   static constexpr int kTuneThresholds[5] = {12, 16, 20, 24, 28};
   static constexpr int kTuneCandidates = 10;  // thresholds x coarse test off / on
+  static constexpr int kTuneDefault = 7;      // threshold 20 with the block bounds
   static constexpr int kTuneRounds = 3;
-  int tune_next_ = 0;   // intervals measured so far
-  int tuned_ = -1;      // chosen candidate, -1 while tuning
+  int tune_stage_ = 0;  // 0 launch shape, 1 threshold x staging, 2 tuned
+  int tune_next_ = 0;   // intervals measured in the current stage
+  int shape_ = 0;       // launch shape (from stage 0 on)
+  int tuned_ = -1;      // threshold x staging candidate, -1 while tuning
+  std::array<long long, 4> tune_key_{};
   std::vector<double> tune_cost_[kTuneCandidates];
   static int tune_threshold(int c) { return kTuneThresholds[c % 5]; }
   static int tune_coarse(int c) { return c / 5; }
+  struct TunePoint {
+    int shape, cand;
+  };
+  static std::map<std::array<long long, 4>, TunePoint>& tune_cache() {
+    static std::map<std::array<long long, 4>, TunePoint> m;
+    return m;
+  }
+  static std::mutex& tune_mutex() {
+    static std::mutex mu;
+    return mu;
+  }
+  // the median cost of each candidate: the cheapest
+  int tune_pick(int n) {
+    double best = 0;
+    int pick = 0;
+    for (int k = 0; k < n; ++k) {
+      std::vector<double> v = tune_cost_[k];
+      std::sort(v.begin(), v.end());
+      const double med = v[v.size() / 2];
+      if (k == 0 || med < best) {
+        best = med;
+        pick = k;
+      }
+    }
+    for (auto& c : tune_cost_) c.clear();
+    return pick;
+  }
 
   struct Member {
     Engine* e = nullptr;
@@ -194,6 +235,8 @@ class Batch {
   // the kernels of one interval (or of the distribution passes, kGraphHist),
   // captured once per set of launch groups: their sizes come from the staged
   // header, so one graph serves every interval and every membership
+  // graph keys: the launch groups (BatchParts) and, above bit 20, the shape
+  static constexpr int kGraphShapeShift = 20;
   int graph(unsigned parts, cudaGraphExec_t* out, int* kernels) {
     auto it = graphs_.find(parts);
     if (it == graphs_.end()) {
@@ -207,7 +250,7 @@ class Batch {
         const BatchArgs b = args(d_stage_);
         n = launch_batch_pre(b, sm_count_, max_slots_, parts, stream_);
         cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
-        n += launch_batch_advance(b, sm_count_, parts, stream_);
+        n += launch_batch_advance(b, sm_count_, parts, (int)(parts >> kGraphShapeShift), stream_);
         cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
         n += launch_batch_post(b, sm_count_, max_slots_, parts, stream_);
       }
@@ -319,7 +362,26 @@ class Batch {
     int na = 0;
     unsigned parts = 0;
     double electrons = 0;
-    const int cand = tuned_ >= 0 ? tuned_ : tune_next_ % kTuneCandidates;
+    if (tune_stage_ == 0 && tune_next_ == 0) {
+      // the mixture's key; a known one starts tuned
+      tune_key_ = {0, 0, 0, 0};
+      for (int s = 0; s < n; ++s) {
+        Engine* e = member(go[s]).e;
+        tune_key_[0] = std::max<long long>(tune_key_[0], e->P_);
+        tune_key_[1] = std::max<long long>(tune_key_[1], e->M_);
+        tune_key_[2] |= 1ll << e->field_mode();
+        tune_key_[3] |= e->cfg_.gas_temperature_effect != 0;
+      }
+      std::lock_guard<std::mutex> lock(tune_mutex());
+      auto it = tune_cache().find(tune_key_);
+      if (it != tune_cache().end()) {
+        shape_ = it->second.shape;
+        tuned_ = it->second.cand;
+        tune_stage_ = 2;
+      }
+    }
+    const int shape = tune_stage_ == 0 ? tune_next_ % kAdvShapes : shape_;
+    const int cand = tune_stage_ == 0 ? kTuneDefault : (tune_stage_ == 1 ? tune_next_ % kTuneCandidates : tuned_);
     for (int s = 0; s < n; ++s) {
       Engine* e = member(go[s]).e;
       e->fill_slot(&sl[s]);
@@ -351,7 +413,7 @@ class Batch {
     }
     cudaGraphExec_t ge;
     int rc, kernels = 0;
-    if ((rc = graph(parts, &ge, &kernels))) return rc;
+    if ((rc = graph(parts | ((unsigned)shape << kGraphShapeShift), &ge, &kernels))) return rc;
     const size_t up = batch_slots_offset() + (size_t)n * sizeof(BatchSlot);
     const size_t down = (size_t)n * sizeof(DevScalars);
     if ((rc = cuda(cudaMemcpyAsync(d_stage_, h_stage_, up, cudaMemcpyHostToDevice, stream_), "stage"))) return rc;
@@ -363,21 +425,21 @@ class Batch {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     adv_ms_ += ms;
-    if (tuned_ < 0 && electrons > 0) {
-      tune_cost_[cand].push_back(ms / electrons);
-      if (++tune_next_ >= kTuneCandidates * kTuneRounds) {
-        double best = 0;
-        int pick = 0;
-        for (int k = 0; k < kTuneCandidates; ++k) {
-          std::vector<double> v = tune_cost_[k];
-          std::sort(v.begin(), v.end());
-          const double med = v[v.size() / 2];
-          if (k == 0 || med < best) {
-            best = med;
-            pick = k;
-          }
+    if (tune_stage_ < 2 && electrons > 0) {
+      const int nc = tune_stage_ == 0 ? kAdvShapes : kTuneCandidates;
+      tune_cost_[tune_stage_ == 0 ? shape : cand].push_back(ms / electrons);
+      if (++tune_next_ >= nc * kTuneRounds) {
+        const int pick = tune_pick(nc);
+        tune_next_ = 0;
+        if (tune_stage_ == 0) {
+          shape_ = pick;
+          tune_stage_ = 1;
+        } else {
+          tuned_ = pick;
+          tune_stage_ = 2;
+          std::lock_guard<std::mutex> lock(tune_mutex());
+          tune_cache()[tune_key_] = TunePoint{shape_, tuned_};
         }
-        tuned_ = pick;
       }
     }
     electron_steps_ += electrons;

@@ -54,10 +54,26 @@ __device__ __forceinline__ int append_slot(int* counter) {
   return base + (int)g.thread_rank();
 }
 
-constexpr int kAdvanceThreads = 256;
-constexpr int kAdvanceBlocksPerSM = 4;
+// Launch shapes of the advance: threads per block, blocks per SM (which fix
+// the register budget: 65536 / (threads x blocks)) and the electrons a warp
+// takes from the work counter at a time (its chunk: chunk/32 electrons per
+// lane). The single-condition kernels use shape 0; the batched kernel is
+// built in every shape and the batch's tuner picks one per mixture.
+template <int S>
+struct AdvShape;
+template <>
+struct AdvShape<0> { static constexpr int kThreads = 256, kBlocksPerSM = 4, kChunk = 128; };
+template <>
+struct AdvShape<1> { static constexpr int kThreads = 512, kBlocksPerSM = 2, kChunk = 128; };
+template <>
+struct AdvShape<2> { static constexpr int kThreads = 256, kBlocksPerSM = 4, kChunk = 64; };
+template <>
+struct AdvShape<3> { static constexpr int kThreads = 256, kBlocksPerSM = 4, kChunk = 256; };
+static_assert(kAdvShapes == 4, "one AdvShape per tuner candidate");
+
+constexpr int kAdvanceThreads = AdvShape<0>::kThreads;
+constexpr int kAdvanceBlocksPerSM = AdvShape<0>::kBlocksPerSM;
 constexpr int kAdvanceWarps = kAdvanceThreads / 32;
-constexpr int kChunk = 128;  // electrons a warp takes from the global work counter at a time
 
 // ---------------------------------------------------------------- advance
 // Every electron is flown and collided until the synchronisation time
@@ -75,21 +91,25 @@ constexpr int kLocalQ = 32;
 
 // Shared memory of an advance block: constants and per-process tallies of the
 // block's current condition, the warps' secondary queues, reduction scratch.
-struct AdvShared {
+template <int WARPS, int CHUNK>
+struct AdvSharedT {
+  static constexpr int kWarps = WARPS, kChunk = CHUNK;
   float nu_coarse[kMaxCoarse];  // block bounds of the total frequency of the current condition
   unsigned int count[kMaxProcesses];
   float gain[kMaxProcesses];
   float loss[kMaxProcesses];
   ProcF proc[kMaxProcesses];
   GasF gas[kMaxGases];
-  float4 qa[kAdvanceWarps][kLocalQ];  // (x, y, z, t_c)
-  float4 qb[kAdvanceWarps][kLocalQ];  // (vx, vy, vz, 0)
-  int qn[kAdvanceWarps];
-  double red[kAdvanceWarps];
-  double redt[kAdvanceWarps];
-  unsigned long long redn[kAdvanceWarps];
-  unsigned long long redr[kAdvanceWarps];
+  float4 qa[WARPS][kLocalQ];  // (x, y, z, t_c)
+  float4 qb[WARPS][kLocalQ];  // (vx, vy, vz, 0)
+  int qn[WARPS];
+  double red[WARPS];
+  double redt[WARPS];
+  unsigned long long redn[WARPS];
+  unsigned long long redr[WARPS];
 };
+using AdvShared = AdvSharedT<kAdvanceWarps, AdvShape<0>::kChunk>;
+
 
 // The values of one interval: launch arguments, overridden by the control block.
 struct IntervalView {
@@ -167,7 +187,8 @@ __device__ __forceinline__ void reset_tally(LaneTally& tl) {
 }
 
 // process constants to shared memory, tallies and queues cleared
-__device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, AdvShared& sh) {
+template <class Sh>
+__device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, Sh& sh) {
   for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
     sh.count[q] = 0u;
     sh.gain[q] = 0.0f;
@@ -175,7 +196,7 @@ __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, AdvShare
     sh.proc[q] = a.procs[q];
   }
   if (threadIdx.x < a.c.G) sh.gas[threadIdx.x] = a.gases[threadIdx.x];
-  if (threadIdx.x < kAdvanceWarps) sh.qn[threadIdx.x] = 0;
+  if (threadIdx.x < Sh::kWarps) sh.qn[threadIdx.x] = 0;
   if (a.t.nu_coarse)
     for (int b = threadIdx.x; b < a.t.n_coarse; b += blockDim.x) sh.nu_coarse[b] = a.t.nu_coarse[b];
 }
@@ -219,7 +240,8 @@ __device__ __forceinline__ void lane_take_secondary(const AdvanceArgs& a, const 
 
 // idle lanes take secondaries from their warp's queue (newest first);
 // returns the entries left
-__device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const IntervalView& iv, AdvShared& sh, int wid,
+template <class Sh>
+__device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const IntervalView& iv, Sh& sh, int wid,
                                                 int lane, unsigned lt_mask, Lane& L, LaneTally& tl, uint32_t& sec_id,
                                                 uint32_t warp_tag) {
   int qn = min(sh.qn[wid], kLocalQ);
@@ -267,8 +289,8 @@ __device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneT
 // the warp takes once enough of its lanes have one: the long collision code
 // then runs on most of the warp's lanes instead of a few. Each electron draws
 // its random numbers in the same order either way.
-template <int MODE>
-__device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const AdvShared& sh, const IntervalView& iv, Lane& L,
+template <int MODE, class Sh>
+__device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const Sh& sh, const IntervalView& iv, Lane& L,
                                             LaneTally& tl) {
   if (L.s < 0.0f) L.s = -__logf(L.rng.oo());
   const float tau = L.s * iv.inv_nu;
@@ -301,7 +323,8 @@ __device__ __forceinline__ void lane_flight(const AdvanceArgs& a, const AdvShare
 
 // The collision turn: process choice, kinematics, tallies, secondaries and
 // attachment (BoltzmannMC.C:907-1280).
-__device__ __forceinline__ void lane_real(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
+template <class Sh>
+__device__ __forceinline__ void lane_real(const AdvanceArgs& a, Sh& sh, int wid, const IntervalView& iv,
                                           Lane& L, LaneTally& tl) {
   L.pending = false;
   CollResult cr;
@@ -351,8 +374,8 @@ __device__ __forceinline__ void lane_real(const AdvanceArgs& a, AdvShared& sh, i
 
 // One turn of a warp: the collision turn when a.real_batch lanes (or every
 // lane with an electron) have a pending collision, else the flight turn.
-template <int MODE>
-__device__ __forceinline__ void warp_turn(const AdvanceArgs& a, AdvShared& sh, int wid, const IntervalView& iv,
+template <int MODE, class Sh>
+__device__ __forceinline__ void warp_turn(const AdvanceArgs& a, Sh& sh, int wid, const IntervalView& iv,
                                           Lane& L, LaneTally& tl, unsigned live) {
   const unsigned pend = __ballot_sync(0xffffffffu, L.pending);
   if (__popc(pend) >= a.real_batch || pend == live) {
@@ -364,7 +387,8 @@ __device__ __forceinline__ void warp_turn(const AdvanceArgs& a, AdvShared& sh, i
 
 // block reductions of the lane sums and the per-process tallies -> the
 // condition's global tallies (every thread of the block calls this)
-__device__ __forceinline__ void block_flush(const AdvanceArgs& a, AdvShared& sh, const LaneTally& tl, int lane,
+template <class Sh>
+__device__ __forceinline__ void block_flush(const AdvanceArgs& a, Sh& sh, const LaneTally& tl, int lane,
                                             int wid) {
   const double g = warp_sum((double)tl.gain);
   const double ta = warp_sum((double)tl.time_adj);
@@ -406,8 +430,8 @@ __device__ __forceinline__ void block_flush(const AdvanceArgs& a, AdvShared& sh,
 // from the condition's work counter, then each warp's queued secondaries (or,
 // drain, only the spilled secondaries). Returns when the condition's counter
 // and the warp's queue are exhausted; the caller flushes the lane sums.
-template <int MODE>
-__device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, const IntervalView& iv,
+template <int MODE, class Sh>
+__device__ __forceinline__ void warp_loop(const AdvanceArgs& a, Sh& sh, const IntervalView& iv,
                                           LaneTally& tl, uint32_t& sec_id, uint32_t warp_tag) {
   const bool drain = a.queue_only != 0;
   const int n_el = drain ? 0 : a.n;
@@ -437,13 +461,13 @@ __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, c
       next += take;
       if (n_need > take) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(a.work_counter, kChunk);
+        if (lane == 0) base = atomicAdd(a.work_counter, Sh::kChunk);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_el) {
           exhausted = true;
         } else {
           next = base;
-          end = min(base + kChunk, n_el);
+          end = min(base + Sh::kChunk, n_el);
           const int r2 = r - take;
           const int take2 = min(n_need - take, end - next);
           if (!L.have && r2 >= 0 && r2 < take2) idx = next + r2;
@@ -477,14 +501,14 @@ __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, AdvShared& sh, c
 }
 
 // One condition per launch (or, drain, its spilled secondaries).
-template <int MODE>
-__device__ __forceinline__ void advance_body(const AdvanceArgs& a, AdvShared& sh) {
+template <int MODE, class Sh>
+__device__ __forceinline__ void advance_body(const AdvanceArgs& a, Sh& sh) {
   load_block_consts(a, sh);
   __syncthreads();
   const IntervalView iv = interval_view<MODE>(a);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // drain launches: one block, whose warp tag stays below the spill's 0xFFFFFFFF
-  const uint32_t warp_tag = (uint32_t)(blockIdx.x * kAdvanceWarps + wid);
+  const uint32_t warp_tag = (uint32_t)(blockIdx.x * Sh::kWarps + wid);
   LaneTally tl;
   reset_tally(tl);
   uint32_t sec_id = 0;
@@ -524,16 +548,18 @@ __device__ __forceinline__ void load_slot_args(const AdvanceArgs* src, AdvanceAr
 // electrons; a block whose slot runs dry flushes its tallies and moves to the
 // next slot of the branch that still has electrons, so the block synchronises
 // only when it changes slot and idle blocks help finish large slots.
-template <int MODE>
-__global__ void __launch_bounds__(kAdvanceThreads, kAdvanceBlocksPerSM) k_advance_batch(BatchArgs b) {
-  __shared__ AdvShared sh;
+template <int MODE, int SHAPE>
+__global__ void __launch_bounds__(AdvShape<SHAPE>::kThreads, AdvShape<SHAPE>::kBlocksPerSM)
+    k_advance_batch(BatchArgs b) {
+  using Sh = AdvSharedT<AdvShape<SHAPE>::kThreads / 32, AdvShape<SHAPE>::kChunk>;
+  __shared__ Sh sh;
   __shared__ AdvanceArgs s_a;
   __shared__ IntervalView s_iv;
   __shared__ int s_slot;
   const int s0 = b.hdr->mode_slot[MODE], s1 = b.hdr->mode_slot[MODE + 1];
   if (s0 >= s1) return;  // no slot with this field branch (uniform over the grid)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t warp_tag = (uint32_t)(blockIdx.x * kAdvanceWarps + wid);
+  const uint32_t warp_tag = (uint32_t)(blockIdx.x * Sh::kWarps + wid);
   const int n_slots = b.hdr->n_slots;
   if (threadIdx.x == 0) {
     const int c0 = b.hdr->mode_chunk[MODE], c1 = b.hdr->mode_chunk[MODE + 1];
@@ -1449,7 +1475,7 @@ void launch_advance(const AdvanceArgs& a, cudaStream_t s) {
   } else {
     // persistent grid: at most kAdvanceBlocksPerSM blocks per SM, fewer when
     // the electrons do not fill them (one chunk per warp)
-    const int warps_needed = (a.n + kChunk - 1) / kChunk;
+    const int warps_needed = (a.n + AdvShape<0>::kChunk - 1) / AdvShape<0>::kChunk;
     const int grid = max(1, min(a.sm_count * kAdvanceBlocksPerSM, (warps_needed + 7) / 8));
     LGPU_ADVANCE(k_advance, grid, kAdvanceThreads)
   }
@@ -1522,15 +1548,35 @@ int launch_batch_hist(const BatchArgs& b, int sm_count, unsigned parts, cudaStre
   return n;
 }
 
-int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s) {
-  const int grid = sm_count * kAdvanceBlocksPerSM;
+template <int SHAPE>
+int launch_batch_advance_shape(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s) {
+  constexpr int kT = AdvShape<SHAPE>::kThreads;
+  const int grid = sm_count * AdvShape<SHAPE>::kBlocksPerSM;
   int n = 0;
-  if (parts & (1u << kFieldDC)) k_advance_batch<kFieldDC><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
-  if (parts & (1u << kFieldAC)) k_advance_batch<kFieldAC><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
-  if (parts & (1u << kFieldB)) k_advance_batch<kFieldB><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
-  if (parts & (1u << kFieldECR)) k_advance_batch<kFieldECR><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
-  if (parts & (1u << kFieldACB)) k_advance_batch<kFieldACB><<<grid, kAdvanceThreads, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldDC)) k_advance_batch<kFieldDC, SHAPE><<<grid, kT, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldAC)) k_advance_batch<kFieldAC, SHAPE><<<grid, kT, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldB)) k_advance_batch<kFieldB, SHAPE><<<grid, kT, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldECR)) k_advance_batch<kFieldECR, SHAPE><<<grid, kT, 0, s>>>(b), ++n;
+  if (parts & (1u << kFieldACB)) k_advance_batch<kFieldACB, SHAPE><<<grid, kT, 0, s>>>(b), ++n;
   return n;
+}
+
+int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, int shape, cudaStream_t s) {
+  switch (shape) {
+    case 1: return launch_batch_advance_shape<1>(b, sm_count, parts, s);
+    case 2: return launch_batch_advance_shape<2>(b, sm_count, parts, s);
+    case 3: return launch_batch_advance_shape<3>(b, sm_count, parts, s);
+    default: return launch_batch_advance_shape<0>(b, sm_count, parts, s);
+  }
+}
+
+void advance_shape(int shape, int* threads, int* blocks_per_sm, int* chunk) {
+  switch (shape) {
+    case 1: *threads = AdvShape<1>::kThreads, *blocks_per_sm = AdvShape<1>::kBlocksPerSM, *chunk = AdvShape<1>::kChunk; break;
+    case 2: *threads = AdvShape<2>::kThreads, *blocks_per_sm = AdvShape<2>::kBlocksPerSM, *chunk = AdvShape<2>::kChunk; break;
+    case 3: *threads = AdvShape<3>::kThreads, *blocks_per_sm = AdvShape<3>::kBlocksPerSM, *chunk = AdvShape<3>::kChunk; break;
+    default: *threads = AdvShape<0>::kThreads, *blocks_per_sm = AdvShape<0>::kBlocksPerSM, *chunk = AdvShape<0>::kChunk;
+  }
 }
 
 int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s) {

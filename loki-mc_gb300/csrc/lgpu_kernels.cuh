@@ -261,7 +261,11 @@ enum BatchParts : unsigned {
 };
 int launch_batch_pre(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 int launch_batch_hist(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
-int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
+// The batched advance in one of kAdvShapes launch shapes (threads per block,
+// blocks per SM, electrons a warp takes at a time); advance_shape() names them.
+constexpr int kAdvShapes = 4;
+int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, int shape, cudaStream_t s);
+void advance_shape(int shape, int* threads, int* blocks_per_sm, int* chunk);
 int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 
 // Replay kernels for the parity tests: the production device functions

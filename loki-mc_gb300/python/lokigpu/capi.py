@@ -93,7 +93,8 @@ class BatchReport(ctypes.Structure):
     _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
                 ("d2h_bytes", D), ("host_ms", D), ("secondaries", D), ("spilled", D), ("attached", D),
-                ("real_batch", D), ("coarse_null_test", D), ("regrids", D)]
+                ("real_batch", D), ("coarse_null_test", D), ("regrids", D), ("advance_threads", D),
+                ("advance_blocks_per_sm", D), ("advance_chunk", D)]
 
 
 class Job(ctypes.Structure):

@@ -270,3 +270,41 @@ def test_server_forgets_finished_jobs():
     rep = srv.report()
     srv.stop()
     assert rep.completed == 24 and rep.running == 0 and rep.queued == 0
+
+
+def test_autotuner_picks_a_launch_shape_and_keeps_it_per_mixture():
+    """The batch tunes the advance's launch shape, then the collision-turn
+    threshold and the table staging, and keeps the choice for the mixture: a
+    second batch of the same mixture starts tuned."""
+    from lokigpu import capi
+    ps, arrays = _inputs("atomic")
+
+    def batch_of(seed0):
+        b = capi.Batch(0, 4)
+        ctxs = []
+        for k in range(3):
+            cfg = _config(20000, seed0 + k)
+            cfg.req_integration_points = 1e9  # timed intervals only
+            c = capi.Context(cfg)
+            c.set_processes(ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
+            c.set_conditions(N_GAS, 300.0, 60.0 + 20.0 * k)
+            b.add(c)
+            ctxs.append(c)
+        b.start()
+        return b, ctxs
+
+    b, ctxs = batch_of(100)
+    _, rep = b.step(60)  # 4 shapes x 3 rounds, then 10 candidates x 3 rounds
+    assert rep.advance_threads in (256.0, 512.0) and rep.advance_chunk in (64.0, 128.0, 256.0)
+    assert rep.real_batch in (12.0, 16.0, 20.0, 24.0, 28.0) and rep.coarse_null_test in (0.0, 1.0)
+    first = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.real_batch, rep.coarse_null_test)
+    b.close()
+    for c in ctxs:
+        c.close()
+    b, ctxs = batch_of(200)
+    _, rep = b.step(1)
+    assert (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.real_batch,
+            rep.coarse_null_test) == first
+    b.close()
+    for c in ctxs:
+        c.close()
