@@ -1,10 +1,14 @@
 """GPU statistical parity: full solves against seeded FP64 solves of the
 reference built from its own sources (tests/golden/stats_*.json and
 stats_*_dist.npz, made by tests/golden/make_golden.py --stats: 1e5
-electrons, 1e4 integration intervals, 1e4 table points).
+electrons, 1e4 integration intervals, 1e4 table points): the atomic gas, the
+N2-like gas (cold and thermal targets), the N2/O2-like mixture under DC, AC
+and crossed B, and the field-complex batch's branches (crossed B at 500 and
+2000 Hx, AC at omega/N = 1e-15 m^3/s) on the sweep's mixture.
 
 The GPU solve uses the reference's own parsed inputs (the per-process arrays
-of the matching kin_*.npz), the same numerics keys and 1e6 electrons, so
+of the matching kin_*.npz; the product's flattening for the sweep's
+mixture), the same numerics keys and 1e6 electrons, so
 that the combined error is close to the reference's own. Criteria, for every
 swarm parameter the reference resolves (mean energy, flux and bulk drift
 velocity, flux and bulk diffusion along the axes; components below five of
@@ -48,7 +52,21 @@ pytestmark = pytest.mark.gpu
 KB_EV = 1.38064852e-23 / 1.6021766208e-19
 CASES = sorted(os.path.basename(p)[6:-5] for p in glob.glob(os.path.join(gu.GOLDEN, "stats_*.json")))
 META = {"atomic": dict(N=3.22e22, red_field=100.0), "n2": dict(N=3.22e22, red_field=200.0),
-        "mix": dict(N=3.22e22, red_field=100.0)}
+        "mix": dict(N=3.22e22, red_field=100.0), "sweep": dict(N=3.22e22, red_field=100.0)}
+
+
+def _inputs(case):
+    """Per-process arrays of a case: the reference's own (kin_*.npz), or for
+    the sweep's mixture the product's flattening of the same synthetic gases
+    (pinned to the reference's flattening by test_flatten.py)."""
+    if case == "sweep":
+        from lokigpu import synth
+        ps = synth.flatten([synth.n2_like_gas(fraction=0.8, e_max=1e4), synth.o2_like_gas(fraction=0.2, e_max=1e4)])
+        return ps, dict(gas_first=ps.gas_first, gas_last=ps.gas_last, gas_frac=ps.gas_fraction)
+    arrays = gu.proc_arrays(gu.load(case))
+    return gu.processes(arrays), arrays
+
+
 GAS_TEMP = {"false": 0, "true": 1, "smartActivation": 2}
 N_GPU = 1_000_000
 
@@ -56,9 +74,7 @@ N_GPU = 1_000_000
 def run_gpu(rec, n_electrons=N_GPU):
     from lokigpu import capi
 
-    g = gu.load(rec["case"])
-    arrays = gu.proc_arrays(g)
-    ps = gu.processes(arrays)
+    ps, arrays = _inputs(rec["case"])
     meta = dict(META[rec["case"]], **rec["overrides"])
     num = rec["numerics"]
     cfg = capi.default_config(n_electrons=float(n_electrons), n_interp=int(num.get("nInterpPoints", 10000)),
