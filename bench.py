@@ -156,21 +156,40 @@ def sweep_processes():
 
 
 def sweep_conditions():
-    """(E/N in Td, electrons) of the 64 sweep points."""
+    """(E/N in Td, electrons, field angle, frequency in Hz, B/N in Hx) of the
+    64 sweep points: DC at 180 degrees."""
     import numpy as np
 
     en = np.logspace(0.0, 3.0, SWEEP_POINTS)
     rng = np.random.default_rng(SWEEP_SEED)
     lo, hi = np.log10(SWEEP_NE_RANGE[0]), np.log10(SWEEP_NE_RANGE[1])
     ne = np.round(10.0 ** rng.uniform(lo, hi, SWEEP_POINTS)).astype(int)
-    return [(float(e), int(n)) for e, n in zip(en, ne)]
+    return [(float(e), int(n), 180.0, 0.0, 0.0) for e, n in zip(en, ne)]
 
 
-def sweep_config(capi, device, n_e, seed, converge):
+FIELD_ELECTRONS = 500_000
+FIELD_PHASES = 64
+PHASES = 100  # phase bins of the running workload's AC conditions (set by main)
+
+
+def field_conditions():
+    """The field-complex batch: the sweep's mixture at DC 100 Td with a crossed
+    magnetic field (E at 90 degrees to B along z), B/N 0..2000 Hx in 16 steps,
+    and an AC field of 150 Td rms at omega/N 1e-18..1e-14 m^3/s (16 log
+    steps, 64 phase bins); 5e5 electrons each."""
+    import numpy as np
+
+    b = [(100.0, FIELD_ELECTRONS, 90.0, 0.0, float(x)) for x in np.linspace(0.0, 2000.0, 16)]
+    ac = [(150.0, FIELD_ELECTRONS, 180.0, float(w * N_GAS / (2.0 * np.pi)), 0.0) for w in np.logspace(-18.0, -14.0, 16)]
+    return b + ac
+
+
+def sweep_config(capi, device, n_e, seed, converge, phases=100):
     """Numerics of a sweep condition: converged means the reference's stop
     criteria with relError meanEnergy 0.5% (BoltzmannMC.C:1743-1767), else a
     context that never stops by itself (timed intervals)."""
-    kw = dict(device=device, seed=seed, n_electrons=float(n_e), n_interp=10000, init_temp_ratio=KT_INIT)
+    kw = dict(device=device, seed=seed, n_electrons=float(n_e), n_interp=10000, init_temp_ratio=KT_INIT,
+              n_phases=phases)
     if converge:
         kw.update(errors_checked=1, req_err_mean_energy=SWEEP_ERR, req_integration_points=200.0,
                   max_coll_before_ss=SWEEP_SS_CAP, max_seconds=300.0)
@@ -198,14 +217,22 @@ def cpu_condition(job):
     wall time; the second half is measured. Returns (electrons of the
     condition in the workload, measured electron-intervals, real collisions,
     seconds)."""
-    workload, td, n_cfg, n, seconds, seed = job
+    workload, (td, n_cfg, angle, freq, red_mag), n, seconds, seed = job
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "loki-mc_gb300", "python"))
     import oracle as O
 
-    ps = sweep_processes() if workload == "sweep" else n2_processes()
+    import math
+
+    ps = n2_processes() if workload == "n2_200td" else sweep_processes()
     pr = O.OracleProcs(_oracle_arrays(ps), 10000)
-    f = O.make_fields(N_GAS, T_GAS, E=(0.0, 0.0, -td * 1e-21 * N_GAS))
+    # the field of BoltzmannMC.C:463-485: E at `angle` to z, sqrt(2) x rms for AC,
+    # cyclotron frequency e B / m with B = (B/N) N (1 Hx = 1e-27 T m^3)
+    e_abs = td * 1e-21 * N_GAS * (math.sqrt(2.0) if freq else 1.0)
+    E = (0.0, 0.0, -e_abs) if angle == 180.0 else (e_abs * math.sin(math.radians(angle)), 0.0,
+                                                   e_abs * math.cos(math.radians(angle)))
+    f = O.make_fields(N_GAS, T_GAS, E=E, freq_hz=freq, red_mag=red_mag,
+                      omega_c=1.6021766208e-19 * red_mag * 1e-27 * N_GAS / 9.10938356e-31)
     cfg = O.default_run_config(n, n_threads=1, seed=seed, max_seconds=seconds, mark_seconds=0.5 * seconds,
                                req_integration_points=1e12, init_temp_ratio=KT_INIT)
     _, res, _ = O.run(pr, f, cfg)
@@ -237,16 +264,16 @@ def cpu_sample(seconds: float, cores: int, workload: str, offset: int = 0, max_e
     samples)."""
     import multiprocessing as mp
 
-    if workload == "sweep":
-        conds = sweep_conditions()
+    if workload in ("sweep", "field"):
+        conds = sweep_conditions() if workload == "sweep" else field_conditions()
         picks = [conds[(offset + k) % len(conds)] for k in range(cores)]
     else:
-        picks = [(E_N, N_ELECTRONS)] * cores
-    jobs = [(workload, td, n_cfg, min(n_cfg, max_electrons), seconds, 3 + offset + k)
-            for k, (td, n_cfg) in enumerate(picks)]
+        picks = [(E_N, N_ELECTRONS, 180.0, 0.0, 0.0)] * cores
+    jobs = [(workload, cond, min(cond[1], max_electrons), seconds, 3 + offset + k) for k, cond in enumerate(picks)]
     with mp.get_context("spawn").Pool(cores) as pool:
         samples = pool.map(cpu_condition, jobs)
-    what = "the sweep's 64 conditions" if workload == "sweep" else "the N2-like gas at 200 Td"
+    what = {"sweep": "the sweep's 64 conditions", "field": "the field-complex batch's 32 conditions"}.get(
+        workload, "the N2-like gas at 200 Td")
     desc = (f"{what}, {len(jobs)} conditions per round on {cores} cores (one single-threaded run each, up to "
             f"{max_electrons} electrons from kT = 1 eV, {seconds:.1f} s of which the second half is measured), "
             f"weighted by the workload's electron counts; C restatement of the reference path")
@@ -266,12 +293,13 @@ def run_reference_arm(args):
         if i >= args.warmup:
             samples += smp
     v = cpu_sweep_rate(samples, cores)
-    workload = "sweep64_n2o2_1-1000Td" if args.workload == "sweep" else "n2_like_dc200Td_1e6e"
+    workload = {"sweep": "sweep64_n2o2_1-1000Td", "field": "field32_n2o2_crossedB_AC"}.get(
+        args.workload, "n2_like_dc200Td_1e6e")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * (time.time() - t0) / (args.steps + args.warmup),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload, "conditions": 64 if args.workload == "sweep" else 1,
+            "config": {"workload": workload, "conditions": {"sweep": 64, "field": 32}.get(args.workload, 1),
                        "impl_detail": "C restatement of the reference path (oracle/), one condition per core"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -318,10 +346,10 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
 
     b = capi.Batch(local, len(conds))
     ctxs = []
-    for i, (en, ne) in enumerate(conds):
-        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False))
+    for i, (en, ne, ang, fr, bm) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False, phases=PHASES))
         c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
-        c.set_conditions(N_GAS, T_GAS, en)
+        c.set_conditions(N_GAS, T_GAS, en, ang, fr, bm)
         b.add(c)
         ctxs.append(c)
     b.start()
@@ -377,10 +405,10 @@ def _sweep_timed_plain(capi, ps, conds, local, rank, args, flush):
     import torch
 
     total_ms = real = null = 0.0
-    for i, (en, ne) in enumerate(conds):
-        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False))
+    for i, (en, ne, ang, fr, bm) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 5000 + 100 * rank + i, converge=False, phases=PHASES))
         c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
-        c.set_conditions(N_GAS, T_GAS, en)
+        c.set_conditions(N_GAS, T_GAS, en, ang, fr, bm)
         c.init_ensemble()
         c.advance(args.relax)
         flush.add_(1.0)
@@ -412,10 +440,10 @@ def _sweep_e2e_batched(capi, ps, conds, local, rank):
     w0 = time.perf_counter()
     b = capi.Batch(local, len(conds))
     ctxs = []
-    for i, (en, ne) in enumerate(conds):
-        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True))
+    for i, (en, ne, ang, fr, bm) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True, phases=PHASES))
         c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
-        c.set_conditions(N_GAS, T_GAS, en)
+        c.set_conditions(N_GAS, T_GAS, en, ang, fr, bm)
         b.add(c)
         ctxs.append(c)
     res, st, rep = b.run()
@@ -433,10 +461,10 @@ def _sweep_e2e_plain(capi, ps, conds, local, rank):
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     res, rates, h2d, d2h, steps = [], [], 0.0, 0.0, 0
-    for i, (en, ne) in enumerate(conds):
-        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True))
+    for i, (en, ne, ang, fr, bm) in enumerate(conds):
+        c = capi.Context(sweep_config(capi, local, ne, 7000 + 100 * rank + i, converge=True, phases=PHASES))
         c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
-        c.set_conditions(N_GAS, T_GAS, en)
+        c.set_conditions(N_GAS, T_GAS, en, ang, fr, bm)
         r = c.solve()
         rates.append(c.process_results()[:2])
         tm = c.timing()
@@ -460,9 +488,9 @@ def _sweep_served(capi, ps, conds, local, rank, args):
     w0 = time.perf_counter()
     for k, i in enumerate(order):
         time.sleep(float(gaps[k]))
-        en, ne = conds[i]
-        ids[i] = srv.submit(sweep_config(capi, local, ne, 7000 + 100 * rank + int(i), converge=True), ps,
-                            ps.gas_first, ps.gas_last, ps.gas_fraction, N_GAS, T_GAS, en)
+        en, ne, ang, fr, bm = conds[i]
+        ids[i] = srv.submit(sweep_config(capi, local, ne, 7000 + 100 * rank + int(i), converge=True, phases=PHASES),
+                            ps, ps.gas_first, ps.gas_last, ps.gas_fraction, N_GAS, T_GAS, en, ang, fr, bm)
     sts = {i: srv.wait(j, 600.0) for i, j in ids.items()}
     w1 = time.perf_counter()
     rep = srv.report()
@@ -483,7 +511,8 @@ def _largest_deviation(conds, batched, plain, zs):
     standard errors: E/N, electrons, both mean energies and errors."""
     i = max(range(len(zs)), key=lambda k: zs[k])
     rb, rp = batched["results"][i], plain["results"][i]
-    return {"E/N_Td": float(conds[i][0]), "electrons": int(conds[i][1]),
+    return {"E/N_Td": float(conds[i][0]), "electrons": int(conds[i][1]), "angle_deg": conds[i][2],
+            "freq_hz": conds[i][3], "B/N_Hx": conds[i][4],
             "batched_eV": [float(rb.mean_energy), float(rb.mean_energy_err)],
             "plain_eV": [float(rp.mean_energy), float(rp.mean_energy_err)]}
 
@@ -635,6 +664,42 @@ def _precision_study(capi, ps, conds, local):
             "seeded_repeats": repeats, "wall_s": wall}
 
 
+# FP32 + SFU operations the method needs (the algorithmic count of the
+# batched path's issue roofline): a free flight 1 lg2 + ~10 FP32 plus the
+# field's sin/cos (AC 2 pairs, crossed B 1 pair and a half-angle sine); a null
+# test ~6 FMA around its table loads; a real collision ~log2(P) x 2 FMA for the
+# process choice + 2 sqrt + 1 rcp + 1 sin/cos pair + ~25 FMA.
+OPS_FLIGHT = {"dc": 11.0, "ac": 15.0, "b": 14.0}
+OPS_NULL_TEST = 6.0
+
+
+def ops_real(n_processes):
+    import math
+    return 2.0 * math.ceil(math.log2(max(n_processes, 2))) + 2.0 + 1.0 + 2.0 + 25.0
+
+
+# ncu counters of one batched DC advance launch over the sweep (1.98e7
+# electrons, profiles/k_advance_batch_sweep64.md): warp instructions per
+# electron-interval issued to the FMA, ALU and XU (SFU) pipes, and the share
+# of the SMs' issue slots the FP32 + SFU pipes took
+NCU_PIPE_PER_ELECTRON = {"fma": 259531314 / 19795598, "alu": 266929018 / 19795598, "xu": 15700687 / 19795598}
+
+
+def issue_roofline(real, null, electron_steps, kernel_ms, n_processes, flight_ops, sm_mhz):
+    """Algorithmic FP32 + SFU operations of the advance over its device time,
+    against the lanes' nominal rate (152 SMs x 128 FP32 lanes x the SM clock
+    sampled during the run; no measured FP32 peak exists for this machine)."""
+    ops = (flight_ops + OPS_NULL_TEST) * (real + null) + ops_real(n_processes) * real + flight_ops * electron_steps
+    achieved = ops / (kernel_ms * 1e-3) / 1e12
+    peak = 152 * 128 * sm_mhz * 1e6 / 1e12
+    return {"bound": "issue (FP32 + SFU)", "achieved": achieved, "peak": peak, "unit": "Top/s",
+            "frac": achieved / peak, "ops_per_electron_interval": ops / max(electron_steps, 1.0),
+            "peak_source": "nominal: 152 SMs x 128 FP32 lanes x sampled SM clock",
+            "ncu_pipe_warp_instructions_per_electron_interval": NCU_PIPE_PER_ELECTRON,
+            "note": "the advance issues ~2x more ALU (integer: random numbers, lane bookkeeping) than FMA "
+                    "instructions at ~15 of 32 lanes active; its own FP32 + SFU work is a few % of the lanes' rate"}
+
+
 def run_gpu_sweep(args):
     import torch
 
@@ -645,7 +710,8 @@ def run_gpu_sweep(args):
     if not os.path.exists(capi.library_path()):
         gbuild.build()
     ps = sweep_processes()
-    conds = sweep_conditions()
+    field = args.workload == "field"
+    conds = field_conditions() if field else sweep_conditions()
     clocks = ClockSampler(local)
     clocks.start()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -661,15 +727,15 @@ def run_gpu_sweep(args):
     e2e_b = _sweep_e2e_batched(capi, ps, conds, local, rank) if not args.no_e2e else None
     e2e_p = _sweep_e2e_plain(capi, ps, conds, local, rank) if not (args.no_e2e or args.no_plain) else None
     srv = _sweep_served(capi, ps, conds, local, rank, args) if not args.no_served else None
-    prec = _precision_study(capi, ps, conds, local) if (rank == 0 and not args.no_precision) else None
+    prec = _precision_study(capi, ps, conds, local) if (rank == 0 and not (args.no_precision or field)) else None
     stream = None
-    if rank == 0 and not args.no_served and args.stream_requests > 0:
+    if rank == 0 and not (args.no_served or field) and args.stream_requests > 0:
         stream = serve_stream(capi, local, args.stream_requests, args.stream_arrival_ms, args.request_cap_s,
                               args.slots, args.plain_requests)
 
     peak, peak_kind = measured_peaks()
     achieved = STATE_BYTES_PER_ELECTRON_STEP * tb["electron_steps"] / (tb["adv_ms"] * 1e-3) / 1e9 if tb["adv_ms"] > 0 else 0.0
-    electrons = sum(n for _, n in conds)
+    electrons = sum(c[1] for c in conds)
     line = None
     if rank == 0:
         cpu = None
@@ -678,7 +744,7 @@ def run_gpu_sweep(args):
             smp = []
             rounds = (len(conds) + cores - 1) // cores
             for k in range(rounds):
-                _, sample, _, got = cpu_sample(args.cpu_seconds / rounds, cores, "sweep", offset=k * cores)
+                _, sample, _, got = cpu_sample(args.cpu_seconds / rounds, cores, args.workload, offset=k * cores)
                 smp += got
             cpu = {"value": cpu_sweep_rate(smp, cores), "unit": UNIT, "cores": cores, "kind": "port",
                    "sample": sample + f"; {rounds} rounds cover every condition"}
@@ -723,10 +789,14 @@ def run_gpu_sweep(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "sweep64_n2o2_1-1000Td", "conditions": len(conds), "electrons_total": electrons,
-                       "electrons_range": list(SWEEP_NE_RANGE), "E/N_Td": [1.0, 1000.0], "gas_density": N_GAS,
+            "config": {"workload": "field32_n2o2_crossedB_AC" if field else "sweep64_n2o2_1-1000Td",
+                       "conditions": len(conds), "electrons_total": electrons,
+                       "electrons_range": [FIELD_ELECTRONS] * 2 if field else list(SWEEP_NE_RANGE),
+                       "E/N_Td": [1.0, 1000.0], "gas_density": N_GAS,
+                       "fields": ("DC 100 Td at 90 degrees to B along z, B/N 0..2000 Hx (16); AC 150 Td rms at "
+                                  "omega/N 1e-18..1e-14 m^3/s (16), 64 phase bins") if field else "DC at 180 degrees",
                        "processes": int(ps.n), "mixture": "N2-like 0.8 + O2-like 0.2 (synthetic, seeded)",
-                       "method": "batched: one launch sequence per interval for all 64 conditions",
+                       "method": f"batched: one launch sequence per interval for all {len(conds)} conditions",
                        "relax_intervals": args.relax, "l2": "256 MiB flush before every timed step",
                        "null_collisions_per_s": null / (total_ms * 1e-3),
                        "host_ms_per_step": tb["host_ms"] / args.steps,
@@ -749,7 +819,10 @@ def run_gpu_sweep(args):
                          "traffic_source": "ncu dram__bytes_read+write of the batched DC advance, one sweep interval",
                          "kernel": "k_advance_batch", "peak_source": peak_kind,
                          "algorithmic_bytes": f"{STATE_BYTES_PER_ELECTRON_STEP} B per electron-interval",
-                         "kernel_ms_per_interval": tb["adv_ms"] / max(tb["intervals"], 1)},
+                         "kernel_ms_per_interval": tb["adv_ms"] / max(tb["intervals"], 1),
+                         "issue": issue_roofline(tb["real"], tb["null"], tb["electron_steps"], tb["adv_ms"], ps.n,
+                                                 0.5 * (OPS_FLIGHT["ac"] + OPS_FLIGHT["b"]) if field
+                                                 else OPS_FLIGHT["dc"], (clk or {}).get("sm_mhz") or 2070.0)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tb["launches"]), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -1016,7 +1089,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "n2_200td", "serve"])
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "field", "n2_200td", "serve"])
     ap.add_argument("--requests", type=int, default=100, help="serve: requests in the stream")
     ap.add_argument("--stream-requests", type=int, default=500,
                     help="sweep: requests of the random-mixture stream served after the sweep (0: none)")
@@ -1038,14 +1111,16 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.steps is None:
-        args.steps = 200 if args.workload == "sweep" else 2000
+        args.steps = 200 if args.workload in ("sweep", "field") else 2000
     if args.relax is None:
-        args.relax = 200 if args.workload == "sweep" else 400
+        args.relax = 200 if args.workload in ("sweep", "field") else 400
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.workload == "serve":
         return run_gpu_serve(args)
-    return run_gpu_sweep(args) if args.workload == "sweep" else run_gpu_n2(args)
+    global PHASES
+    PHASES = FIELD_PHASES if args.workload == "field" else 100
+    return run_gpu_sweep(args) if args.workload in ("sweep", "field") else run_gpu_n2(args)
 
 
 if __name__ == "__main__":
