@@ -633,13 +633,16 @@ def _precision_study(capi, ps, conds, local):
                 continue
             rel = rate[p] / rr[p] - 1.0
             sig = rel / float(np.sqrt(1.0 / c_ref + 1.0 / float(cnt[p])))
-            devs.append((abs(rel), abs(sig)))
+            devs.append((abs(rel), abs(sig), p, float(cnt[p]), c_ref, rel, sig, ps.eloss[p], int(ps.ptype[p])))
             ok = abs(rel) <= 5e-3 or abs(sig) <= 2.0
             n_ok += ok
             n_all += 1
         if devs:
             pt["rates"] = {"compared": len(devs), "max_abs_rel_err": max(d[0] for d in devs),
-                           "max_abs_sigmas": max(d[1] for d in devs)}
+                           "max_abs_sigmas": max(d[1] for d in devs),
+                           "largest": [{"process": d[2], "type": d[8], "threshold_eV": d[7], "gpu_counts": d[3],
+                                        "ref_counts": d[4], "rel_err": d[5], "sigmas": d[6]}
+                                       for d in sorted(devs, key=lambda d: -d[1])[:3]]}
             w = worst.setdefault("rates", {"max_abs_rel_err": 0.0, "max_abs_sigmas": 0.0})
             w["max_abs_rel_err"] = max(w["max_abs_rel_err"], pt["rates"]["max_abs_rel_err"])
             w["max_abs_sigmas"] = max(w["max_abs_sigmas"], pt["rates"]["max_abs_sigmas"])
