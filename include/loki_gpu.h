@@ -405,6 +405,33 @@ int lgpu_server_last_error(const lgpu_server* server, char* buf, size_t size);
 /* Cancels what is left, joins the thread, frees the device memory. */
 int lgpu_server_stop(lgpu_server* server);
 
+/* ---- requests: jobs from the reference's own input files ----
+ *
+ * The reference reads a setup file (.in) and the LXCat files it names
+ * (Parse.C:43-295, Setup.h:229-459) and flattens the collisions into its MC
+ * processes (BoltzmannMC.C:29-271). lgpu_request_parse does the same on the
+ * files' texts, with no file access and no reference code, so that a server
+ * can admit a request as a user of the reference writes it: working
+ * conditions (one of E/N, B/N, field angle, frequency may be a vector: one job
+ * per entry), numericsMC keys, gas masses, fractions and OPB parameters,
+ * state energies, statistical weights and populations (values or
+ * boltzmannPopulation@T over a family "G(X,v=*)"), anisotropic scattering
+ * "group;gas;type;law;params" lines. Values are arithmetic expressions as in
+ * the reference's setup files. An input it does not read (for instance a
+ * momentum-transfer cross section with an anisotropic law) fails with
+ * LGPU_ERR_BAD_ARG and a message in err. */
+typedef struct lgpu_request lgpu_request;
+int lgpu_request_parse(const char* setup_text, int n_files, const char* const* file_names,
+                       const char* const* file_texts, lgpu_request** out, char* err, size_t err_size);
+/* Number of jobs of the request. */
+int lgpu_request_jobs(const lgpu_request* req);
+/* The k-th job, ready for lgpu_server_submit (its pointers stay valid while
+ * the request lives). */
+int lgpu_request_job(const lgpu_request* req, int k, lgpu_job* job);
+void lgpu_request_free(lgpu_request* req);
+/* Submits every job of the request; job_ids has room for lgpu_request_jobs. */
+int lgpu_server_submit_request(lgpu_server* server, const lgpu_request* req, long long* job_ids, int max_ids);
+
 #ifdef __cplusplus
 }
 #endif

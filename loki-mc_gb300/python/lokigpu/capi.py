@@ -33,7 +33,9 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
             "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_forget", "lgpu_server_report_get", "lgpu_server_last_error",
-            "lgpu_server_stop")
+            "lgpu_server_stop",
+            "lgpu_request_parse", "lgpu_request_jobs", "lgpu_request_job", "lgpu_request_free",
+            "lgpu_server_submit_request")
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
 
@@ -173,6 +175,13 @@ def load(path: str | None = None):
     lib.lgpu_server_report_get.argtypes = [VP, P_(ServerReport)]
     lib.lgpu_server_last_error.argtypes = [VP, ctypes.c_char_p, ctypes.c_size_t]
     lib.lgpu_server_stop.argtypes = [VP]
+    CP = ctypes.c_char_p
+    lib.lgpu_request_parse.argtypes = [CP, I, P_(CP), P_(CP), P_(VP), CP, ctypes.c_size_t]
+    lib.lgpu_request_jobs.argtypes = [VP]
+    lib.lgpu_request_job.argtypes = [VP, I, P_(Job)]
+    lib.lgpu_request_free.argtypes = [VP]
+    lib.lgpu_request_free.restype = None
+    lib.lgpu_server_submit_request.argtypes = [VP, VP, P_(LL), I]
     _lib = lib
     return lib
 
@@ -472,6 +481,15 @@ class Server:
             raise LokiGpuError(rc, "lgpu_server_submit failed")
         return jid.value
 
+    def submit_request(self, req: "Request") -> list:
+        """lgpu_server_submit_request: every job of a parsed request."""
+        n = len(req)
+        ids = (LL * max(n, 1))()
+        rc = self.lib.lgpu_server_submit_request(self.h, req.h, ids, n)
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_submit_request failed")
+        return list(ids[:n])
+
     def poll(self, jid) -> JobStatus:
         st = JobStatus()
         rc = self.lib.lgpu_server_poll(self.h, int(jid), ctypes.byref(st))
@@ -518,5 +536,60 @@ class Server:
     def __del__(self):
         try:
             self.stop()
+        except Exception:
+            pass
+
+
+class Request:
+    """lgpu_request: the jobs of a setup file and its LXCat files, parsed by
+    the library (no file access: the texts are passed in)."""
+
+    def __init__(self, setup_text: str, files: dict):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        names = list(files)
+        n = len(names)
+        cn = (ctypes.c_char_p * max(n, 1))(*[k.encode() for k in names])
+        ct = (ctypes.c_char_p * max(n, 1))(*[files[k].encode() for k in names])
+        err = ctypes.create_string_buffer(1024)
+        rc = self.lib.lgpu_request_parse(setup_text.encode(), n, cn, ct, ctypes.byref(self.h), err, 1024)
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, err.value.decode(errors="replace"))
+
+    def __len__(self):
+        return self.lib.lgpu_request_jobs(self.h)
+
+    def job(self, k) -> Job:
+        j = Job()
+        rc = self.lib.lgpu_request_job(self.h, int(k), ctypes.byref(j))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_request_job failed")
+        return j
+
+    def processes(self, k=0):
+        """The flattened processes of job k as numpy arrays (the field names
+        of synth.ProcessSet)."""
+        j = self.job(k)
+        P = j.n_procs
+        q = [j.procs[p] for p in range(P)]
+        out = {f: np.array([getattr(x, f) for x in q]) for f in
+               ("type", "is_super", "is_elastic", "sampler", "sampler_p0", "sampler_p1", "superw", "emin", "emax",
+                "rel_dens", "mass", "eloss", "wparam", "raw_len")}
+        out["raw_e"] = [np.ctypeslib.as_array(x.raw_e, (x.raw_len,)).copy() if x.raw_len else np.zeros(0) for x in q]
+        out["raw_v"] = [np.ctypeslib.as_array(x.raw_v, (x.raw_len,)).copy() if x.raw_len else np.zeros(0) for x in q]
+        out["gas_first"] = np.array([j.gases[g].first for g in range(j.n_gases)])
+        out["gas_last"] = np.array([j.gases[g].last for g in range(j.n_gases)])
+        out["gas_frac"] = np.array([j.gases[g].fraction for g in range(j.n_gases)])
+        out["energy_max_elastic"] = j.emax_elastic
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.lgpu_request_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

@@ -308,3 +308,37 @@ def test_autotuner_picks_a_launch_shape_and_keeps_it_per_mixture():
     b.close()
     for c in ctxs:
         c.close()
+
+
+def test_server_admits_requests_from_input_files(tmp_path):
+    """A request written as for the reference (a setup file with a vector of
+    E/N and its LXCat file, parsed by lgpu_request_parse) runs one job per
+    entry, each equal to the job submitted from the flattened arrays: the
+    inputs are the same bits, so without ionization and attachment the
+    collision counts agree exactly."""
+    import os
+
+    from lokigpu import capi, synth
+
+    gas = synth.atomic_gas()
+    synth.write_case(str(tmp_path), [gas], pressure_pa=N_GAS * 1.38064852e-23 * 300.0, red_field=[80.0, 120.0],
+                     n_electrons=20000, kte_init_ev=1.0,
+                     extra_numerics={"nIntegrationPoints": "500", "nInterpPoints": "2000",
+                                     "maxCollisionsBeforeSteadyState": "100", "gpuSeed": "77"})
+    inp = os.path.join(str(tmp_path), "Input")
+    req = capi.Request(open(os.path.join(inp, "case.in")).read(),
+                       {"A1_LXCat.txt": open(os.path.join(inp, "A1_LXCat.txt")).read()})
+    assert len(req) == 2
+    srv = capi.Server(0, 4)
+    ids = srv.submit_request(req)
+    ps = synth.flatten([gas])
+    cfg = req.job(0).config
+    ids2 = [srv.submit(cfg, ps, ps.gas_first, ps.gas_last, ps.gas_fraction, req.job(k).conditions.gas_density,
+                       300.0, (80.0, 120.0)[k]) for k in range(2)]
+    a = [srv.wait(j, 300.0) for j in ids]
+    b = [srv.wait(j, 300.0) for j in ids2]
+    srv.stop()
+    for x, y in zip(a, b):
+        assert x.state == capi.JOB_DONE and y.state == capi.JOB_DONE
+        assert x.result.real_collisions == y.result.real_collisions
+        assert x.result.mean_energy == y.result.mean_energy
