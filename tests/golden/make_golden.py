@@ -285,12 +285,14 @@ STAT_CASES = {
                  {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300"}),
     # the field-complex batch's branches on the sweep's mixture: crossed DC
     # magnetic fields (E at 90 degrees to B along z) and an AC field of
-    # 150 Td rms (omega/N = 1e-15 m^3/s: a 0.2 us period, some 5 periods)
+    # 150 Td rms (omega/N = 1e-14 m^3/s: a 20 ns period, some 50 periods; at
+    # fewer periods the time averages depend on where each run's window ends
+    # within a period)
     "field_b500": ("sweep", {"red_field": 100.0, "red_mag": 500.0, "angle": 90.0},
                    {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300"}),
     "field_b2000": ("sweep", {"red_field": 100.0, "red_mag": 2000.0, "angle": 90.0},
                     {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300"}),
-    "field_ac1e-15": ("sweep", {"red_field": 150.0, "freq": 3.22e22 * 1e-15 / (2 * np.pi)},
+    "field_ac1e-14": ("sweep", {"red_field": 150.0, "freq": 3.22e22 * 1e-14 / (2 * np.pi)},
                       {"nIntegrationPoints": "1E4", "nInterpPoints": "10000", "maxCollisionsBeforeSteadyState": "300",
                        "nIntegrationPhases": "64"}),
     "n2_dc200_thermal": ("n2", {"gas_temp": "smartActivation"},
