@@ -4,7 +4,7 @@ stats_*_dist.npz, made by tests/golden/make_golden.py --stats: 1e5
 electrons, 1e4 integration intervals, 1e4 table points): the atomic gas, the
 N2-like gas (cold and thermal targets), the N2/O2-like mixture under DC, AC
 and crossed B, and the field-complex batch's branches (crossed B at 500 and
-2000 Hx, AC at omega/N = 1e-15 m^3/s) on the sweep's mixture.
+2000 Hx, AC at omega/N = 1e-14 m^3/s) on the sweep's mixture.
 
 The GPU solve uses the reference's own parsed inputs (the per-process arrays
 of the matching kin_*.npz; the product's flattening for the sweep's
@@ -25,14 +25,15 @@ its standard errors are not resolved) and every rate coefficient
 * every quantity within four combined standard errors or 0.5 % (a
   deviation that statistics alone would produce once in 16000);
 * per-process power gains and losses (BoltzmannMC.C:1640-1649) above 1 % of
-  the field's power within 1 %.
+  the field's power within 1 % or four Poisson errors of the process's counts.
 
 Distributions (BoltzmannMC.C:1492-1605), compared through cumulative
 probabilities at common edges (the two runs' grids follow their own largest
 energies; tests/golden_util.py): the EEDF's and each of ten cos(angle)
 groups of the EADF's cumulative probability within 0.005 at 20 energy
 edges, the cumulative first and second anisotropies (probability times P1,
-P2 of cos) within 0.002 + 1 % of their totals, the EVDF's 2-D cumulative
+P2 of cos) within 0.002 + 1 % of their totals (not the first under AC:
+it cancels over a period), the EVDF's 2-D cumulative
 probability within 0.005 on a 10 x 10 grid, the EEDF's mean energy within
 0.5 %. AC (BoltzmannMC.C:1468-1481, 1728-1741): the phases with samples,
 and per phase the mean energy within 1 %, the flux drift velocity within 2 %
@@ -153,12 +154,16 @@ def test_swarm_parameters_and_rates(solved):
             rows.append((f"rate[{p}]", rate[p], ref_rate[p], float(counts[p]), c_ref))
     lines, failures = compare_quantities(name, pairs, rows)
     if "power_gain" in rec:
+        # a process's power follows its collision count: within 1 % or four
+        # Poisson errors of the two runs' counts
         rg, rl = np.array(rec["power_gain"]), np.array(rec["power_loss"])
         field = abs(ref[36])
         for p in range(ps.n):
+            c_ref = ref_rate[p] * t_int * n_ref * ps.rel_dens[p] * META[rec["case"]]["N"]
+            tol = max(0.01, 4.0 * np.sqrt(1.0 / max(c_ref, 1.0) + 1.0 / max(float(counts[p]), 1.0)))
             for lab, gv, rv in (("gain", gain[p], rg[p]), ("loss", loss[p], rl[p])):
-                if abs(rv) > 0.01 * field and abs(gv / rv - 1.0) > 0.01:
-                    failures.append(f"power {lab}[{p}]: gpu {gv:.6g}, reference {rv:.6g}")
+                if abs(rv) > 0.01 * field and abs(gv / rv - 1.0) > tol:
+                    failures.append(f"power {lab}[{p}]: gpu {gv:.6g}, reference {rv:.6g} (bound {100 * tol:.2f} %)")
     print("\n".join(lines))
     assert not failures, f"{name}:\n" + "\n".join(failures)
 
@@ -194,7 +199,14 @@ def test_distributions(solved):
         print(f"{name} EADF (10 cos groups): largest cumulative difference {d:.4f}")
         if d > 0.005:
             failures.append(f"EADF cumulative probability differs by {d:.4f}")
+        # under an AC field the first anisotropy changes sign with the field,
+        # so its time average nearly cancels and rests on where each run's
+        # window ends within a period: it is compared phase by phase through
+        # the flux drift below instead
+        ac = per is not None
         for deg, key, fk in ((1, "f1_cdf", "efadf"), (2, "f2_cdf", "esadf")):
+            if ac and deg == 1:
+                continue
             gl = gu.cdf_at(nodes, gu.legendre_mass(cells, dist[fk], deg), e)
             rl = gu.cdf_at(ref_dist["e_edges"], np.diff(ref_dist[key]), e)
             tol = 0.002 + 0.01 * abs(rl[-1])
