@@ -390,7 +390,7 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         assert running == len(conds)
         real_batch = rep.real_batch
         coarse = rep.coarse_null_test
-        shape = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk)
+        shape = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.advance_stash)
     del b
     for c in ctxs:
         c.close()
@@ -807,6 +807,7 @@ def run_gpu_sweep(args):
                        "spilled_per_step": tb["spilled"] / args.steps,
                        "autotuned": {"threads_per_block": tb["shape"][0], "blocks_per_sm": tb["shape"][1],
                                      "electrons_per_warp_claim": tb["shape"][2],
+                                     "collision_stash_records_per_warp": tb["shape"][3],
                                      "collision_turn_threshold": tb["real_batch"],
                                      "table_staging": {1.0: "block bounds in shared memory, rows from L2",
                                                        0.0: "rows from L2"}.get(tb["coarse"], "tuning"),

@@ -305,7 +305,8 @@ typedef struct lgpu_batch_report {
   double advance_threads;       /* launch shape of the advance chosen by the on-line tuner (0 while it is
                                    being tuned): threads per block, */
   double advance_blocks_per_sm; /* blocks per SM (the register budget), */
-  double advance_chunk;         /* electrons a warp takes at a time */
+  double advance_chunk;         /* electrons a warp takes at a time, */
+  double advance_stash;         /* records of a warp's collision stash (0: none; -1 while being tuned) */
 } lgpu_batch_report;
 
 int lgpu_batch_create(int device, int max_slots, lgpu_batch** out);
@@ -332,6 +333,13 @@ int lgpu_batch_start(lgpu_batch* batch);
 int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* report);
 /* The cudaStream_t all of the batch's work runs on. */
 void* lgpu_batch_stream(lgpu_batch* batch);
+/* Pins the advance's schedule instead of tuning it on line: launch shape
+ * 0..4 (lgpu_batch_report's advance_threads .. advance_stash name it), the
+ * collision-turn threshold (12, 16, 20, 24 or 28; a stash shape always takes
+ * 32) and the coarse null test (0 or 1). shape -1 returns to on-line tuning.
+ * The schedule changes no result: what an electron draws and decides does
+ * not depend on it. */
+int lgpu_batch_set_schedule(lgpu_batch* batch, int shape, int real_batch, int coarse);
 
 /* ---- serving: continuous batching of swarm jobs ----
  *

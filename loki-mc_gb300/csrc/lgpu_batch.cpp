@@ -46,6 +46,11 @@ int lgpu_batch_start(lgpu_batch* batch) {
   return LGPU_OK;
 }
 
+int lgpu_batch_set_schedule(lgpu_batch* batch, int shape, int real_batch, int coarse) {
+  if (!batch || !batch->b) return LGPU_ERR_BAD_ARG;
+  return batch->b->set_schedule(shape, real_batch, coarse);
+}
+
 int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* report) {
   if (!batch || !batch->b || n < 0) return LGPU_ERR_BAD_ARG;
   lgpu::Batch& b = *batch->b;
@@ -75,13 +80,15 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
     report->regrids = b.regrids_ - rg0;
-    report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
+    int th = 0, bl = 0, ch = 0, st = 0;
+    lgpu::advance_shape(b.shape_, &th, &bl, &ch, &st);
+    // a stash shape's collision turn always takes 32 collisions
+    report->real_batch = b.tuned_ >= 0 ? (st ? 32 : lgpu::Batch::tune_threshold(b.tuned_)) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
-    int th = 0, bl = 0, ch = 0;
-    lgpu::advance_shape(b.shape_, &th, &bl, &ch);
     report->advance_threads = b.tune_stage_ >= 1 ? th : 0;
     report->advance_blocks_per_sm = b.tune_stage_ >= 1 ? bl : 0;
     report->advance_chunk = b.tune_stage_ >= 1 ? ch : 0;
+    report->advance_stash = b.tune_stage_ >= 1 ? st : -1;
   }
   return rc;
 }
@@ -127,13 +134,15 @@ int lgpu_batch_run(lgpu_batch* batch, lgpu_result* results, int* status, int n, 
     report->spilled = b.spilled_ - sp0;
     report->attached = b.attached_ - at0;
     report->regrids = b.regrids_ - rg0;
-    report->real_batch = b.tuned_ >= 0 ? lgpu::Batch::tune_threshold(b.tuned_) : 0;
+    int th = 0, bl = 0, ch = 0, st = 0;
+    lgpu::advance_shape(b.shape_, &th, &bl, &ch, &st);
+    // a stash shape's collision turn always takes 32 collisions
+    report->real_batch = b.tuned_ >= 0 ? (st ? 32 : lgpu::Batch::tune_threshold(b.tuned_)) : 0;
     report->coarse_null_test = b.tuned_ >= 0 ? lgpu::Batch::tune_coarse(b.tuned_) : -1;
-    int th = 0, bl = 0, ch = 0;
-    lgpu::advance_shape(b.shape_, &th, &bl, &ch);
     report->advance_threads = b.tune_stage_ >= 1 ? th : 0;
     report->advance_blocks_per_sm = b.tune_stage_ >= 1 ? bl : 0;
     report->advance_chunk = b.tune_stage_ >= 1 ? ch : 0;
+    report->advance_stash = b.tune_stage_ >= 1 ? st : -1;
   }
   b.clear_members();
   return rc;

@@ -71,7 +71,8 @@ class Batch {
   //     collision-turn threshold (AdvanceArgs::real_batch) and the table
   //     staging of the null test: block bounds of the total frequency staged
   //     in shared memory first, or the table rows straight from L2
-  //     (AdvanceArgs::coarse).
+  //     (AdvanceArgs::coarse). A stash shape's collision turn always takes
+  //     32 collisions, so for it only the staging is tuned.
   // The choice is kept per mixture, keyed by (largest process count, table
   // points, field branches in use, thermal targets), for the life of the
   // process: a later batch or server interval with the same key starts tuned.
@@ -87,6 +88,10 @@ class Batch {
   std::vector<double> tune_cost_[kTuneCandidates];
   static int tune_threshold(int c) { return kTuneThresholds[c % 5]; }
   static int tune_coarse(int c) { return c / 5; }
+  static_assert(kAdvShapes <= kTuneCandidates, "stage costs share tune_cost_");
+  // stage 1: the candidates of the chosen shape, and the k-th one's index
+  int stage1_count() const { return shape_ >= kFirstStashShape ? 2 : kTuneCandidates; }
+  int stage1_cand(int k) const { return shape_ >= kFirstStashShape ? 5 * k + 2 : k; }
   struct TunePoint {
     int shape, cand;
   };
@@ -97,6 +102,27 @@ class Batch {
   static std::mutex& tune_mutex() {
     static std::mutex mu;
     return mu;
+  }
+  // a pinned schedule (shape >= 0) or on-line tuning again (shape -1)
+  int set_schedule(int shape, int real_batch, int coarse) {
+    if (shape < 0) {
+      tune_stage_ = 0;
+      tune_next_ = 0;
+      tuned_ = -1;
+      for (auto& c : tune_cost_) c.clear();
+      return LGPU_OK;
+    }
+    int t = 0;
+    while (t < 5 && kTuneThresholds[t] != real_batch) ++t;
+    if (shape >= kAdvShapes || (coarse != 0 && coarse != 1) || (t == 5 && shape < kFirstStashShape))
+      return fail(LGPU_ERR_BAD_ARG, "schedule: shape " + std::to_string(shape) + " (0.." +
+                                        std::to_string(kAdvShapes - 1) + "), threshold " + std::to_string(real_batch) +
+                                        " (12, 16, 20, 24, 28), coarse " + std::to_string(coarse) + " (0, 1)");
+    shape_ = shape;
+    tuned_ = (t == 5 ? 2 : t) + 5 * coarse;
+    tune_stage_ = 2;
+    tune_next_ = 0;
+    return LGPU_OK;
   }
   // the median cost of each candidate: the cheapest
   int tune_pick(int n) {
@@ -381,7 +407,8 @@ class Batch {
       }
     }
     const int shape = tune_stage_ == 0 ? tune_next_ % kAdvShapes : shape_;
-    const int cand = tune_stage_ == 0 ? kTuneDefault : (tune_stage_ == 1 ? tune_next_ % kTuneCandidates : tuned_);
+    const int k1 = tune_stage_ == 1 ? tune_next_ % stage1_count() : 0;
+    const int cand = tune_stage_ == 0 ? kTuneDefault : (tune_stage_ == 1 ? stage1_cand(k1) : tuned_);
     for (int s = 0; s < n; ++s) {
       Engine* e = member(go[s]).e;
       e->fill_slot(&sl[s]);
@@ -426,8 +453,8 @@ class Batch {
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     adv_ms_ += ms;
     if (tune_stage_ < 2 && electrons > 0) {
-      const int nc = tune_stage_ == 0 ? kAdvShapes : kTuneCandidates;
-      tune_cost_[tune_stage_ == 0 ? shape : cand].push_back(ms / electrons);
+      const int nc = tune_stage_ == 0 ? kAdvShapes : stage1_count();
+      tune_cost_[tune_stage_ == 0 ? shape : k1].push_back(ms / electrons);
       if (++tune_next_ >= nc * kTuneRounds) {
         const int pick = tune_pick(nc);
         tune_next_ = 0;
@@ -435,7 +462,7 @@ class Batch {
           shape_ = pick;
           tune_stage_ = 1;
         } else {
-          tuned_ = pick;
+          tuned_ = stage1_cand(pick);
           tune_stage_ = 2;
           std::lock_guard<std::mutex> lock(tune_mutex());
           tune_cache()[tune_key_] = TunePoint{shape_, tuned_};

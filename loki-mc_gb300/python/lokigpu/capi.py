@@ -30,7 +30,7 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
             "lgpu_replay_collisions_coarse", "lgpu_replay_flights_noalloc",
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
-            "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream",
+            "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream", "lgpu_batch_set_schedule",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
             "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_forget", "lgpu_server_report_get", "lgpu_server_last_error",
             "lgpu_server_stop",
@@ -96,7 +96,7 @@ class BatchReport(ctypes.Structure):
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
                 ("d2h_bytes", D), ("host_ms", D), ("secondaries", D), ("spilled", D), ("attached", D),
                 ("real_batch", D), ("coarse_null_test", D), ("regrids", D), ("advance_threads", D),
-                ("advance_blocks_per_sm", D), ("advance_chunk", D)]
+                ("advance_blocks_per_sm", D), ("advance_chunk", D), ("advance_stash", D)]
 
 
 class Job(ctypes.Structure):
@@ -165,6 +165,7 @@ def load(path: str | None = None):
     lib.lgpu_batch_step.argtypes = [VP, I, P_(I), P_(BatchReport)]
     lib.lgpu_batch_stream.argtypes = [VP]
     lib.lgpu_batch_stream.restype = VP
+    lib.lgpu_batch_set_schedule.argtypes = [VP, I, I, I]
     lib.lgpu_server_start.argtypes = [I, I, D, P_(VP)]
     lib.lgpu_server_submit.argtypes = [VP, P_(Job), P_(LL)]
     lib.lgpu_server_poll.argtypes = [VP, LL, P_(JobStatus)]
@@ -429,6 +430,13 @@ class Batch:
 
     def stream(self) -> int:
         return self.lib.lgpu_batch_stream(self.h)
+
+    def set_schedule(self, shape, real_batch=20, coarse=1):
+        """Pins the advance's launch shape, collision-turn threshold and
+        coarse null test (shape -1: tune them on line again)."""
+        rc = self.lib.lgpu_batch_set_schedule(self.h, int(shape), int(real_batch), int(coarse))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, self.last_error())
 
     def run(self):
         """Solves every added context: (results, status codes, BatchReport)."""

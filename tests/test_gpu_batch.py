@@ -79,9 +79,11 @@ def _alone(specs):
     return out
 
 
-def _batched(specs, max_slots=64):
+def _batched(specs, max_slots=64, schedule=None):
     from lokigpu import capi
     b = capi.Batch(0, max_slots)
+    if schedule is not None:
+        b.set_schedule(*schedule)
     ctxs = [_context(s) for s in specs]
     for c in ctxs:
         b.add(c)
@@ -142,6 +144,52 @@ def test_batch_repeats_alone_without_ionization():
         assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < tol, spec
         if spec[4] == 0.0:
             assert abs(rb.bulk_v[k] / ra.bulk_v[k] - 1.0) < 1e-3, spec
+
+
+# pinned schedules: (launch shape, collision-turn threshold, coarse null test);
+# shape 4 parks pending collisions in a per-warp stash
+SCHEDULES = [(0, 20, 1), (1, 12, 0), (2, 28, 1), (3, 16, 1), (4, 20, 1), (4, 20, 0)]
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES, ids=[f"shape{s}_t{t}_c{c}" for s, t, c in SCHEDULES])
+def test_every_schedule_repeats_the_solve_alone(schedule):
+    """The schedule (launch shape, the stash, the collision-turn threshold,
+    the staging of the null test) changes no electron's draws or decisions."""
+    specs = [ATOMIC[1], ATOMIC[2], ATOMIC[3]]
+    alone = _alone(specs)
+    batched, rep = _batched(specs, schedule=schedule)
+    assert rep.advance_stash == (64.0 if schedule[0] == 4 else 0.0)
+    assert rep.real_batch == (32.0 if schedule[0] == 4 else schedule[1])
+    assert rep.coarse_null_test == schedule[2]
+    for spec, (ra, ca, _), (rb, cb, _) in zip(specs, alone, batched):
+        tol = 1e-4 if spec[4] == 0.0 else 1e-3
+        assert rb.sync_steps == ra.sync_steps, spec
+        assert abs(rb.real_collisions / ra.real_collisions - 1.0) < tol, spec
+        assert abs(rb.null_collisions / ra.null_collisions - 1.0) < tol, spec
+        assert abs(rb.mean_energy / ra.mean_energy - 1.0) < tol, spec
+        k = _drift_axis(spec)
+        assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < tol, spec
+
+
+def test_schedule_rejects_unknown_points():
+    from lokigpu import capi
+    b = capi.Batch(0, 4)
+    for bad in [(5, 20, 1), (0, 13, 1), (0, 20, 2)]:
+        with pytest.raises(capi.LokiGpuError):
+            b.set_schedule(*bad)
+    b.set_schedule(4, 0, 1)  # a stash shape ignores the threshold
+    b.set_schedule(-1, 0, 0)  # back to on-line tuning
+    b.close()
+
+
+def test_stash_schedule_matches_alone_with_ionization_and_attachment(mix_alone):
+    batched, rep = _batched(MIX, schedule=(4, 20, 1))
+    assert rep.advance_stash == 64.0 and rep.secondaries > 0 and rep.attached > 0
+    fails = []
+    for spec, a, b in zip(MIX, mix_alone, batched):
+        assert b[0].capped == 0 and b[0].integration_points >= 300
+        fails += _statistically_equal(spec, a, b)
+    assert not fails, "\n".join(fails)
 
 
 def test_batch_matches_alone_with_ionization_and_attachment(mix_alone):
@@ -294,16 +342,19 @@ def test_autotuner_picks_a_launch_shape_and_keeps_it_per_mixture():
         return b, ctxs
 
     b, ctxs = batch_of(100)
-    _, rep = b.step(60)  # 4 shapes x 3 rounds, then 10 candidates x 3 rounds
+    _, rep = b.step(60)  # 5 shapes x 3 rounds, then 10 (stash: 2) candidates x 3 rounds
     assert rep.advance_threads in (256.0, 512.0) and rep.advance_chunk in (64.0, 128.0, 256.0)
-    assert rep.real_batch in (12.0, 16.0, 20.0, 24.0, 28.0) and rep.coarse_null_test in (0.0, 1.0)
-    first = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.real_batch, rep.coarse_null_test)
+    assert rep.advance_stash in (0.0, 64.0)
+    assert rep.real_batch in ((32.0,) if rep.advance_stash else (12.0, 16.0, 20.0, 24.0, 28.0))
+    assert rep.coarse_null_test in (0.0, 1.0)
+    first = (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.advance_stash, rep.real_batch,
+             rep.coarse_null_test)
     b.close()
     for c in ctxs:
         c.close()
     b, ctxs = batch_of(200)
     _, rep = b.step(1)
-    assert (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.real_batch,
+    assert (rep.advance_threads, rep.advance_blocks_per_sm, rep.advance_chunk, rep.advance_stash, rep.real_batch,
             rep.coarse_null_test) == first
     b.close()
     for c in ctxs:
