@@ -352,6 +352,8 @@ def _sweep_timed_batched(capi, ps, conds, local, rank, args, flush):
         c.set_conditions(N_GAS, T_GAS, en, ang, fr, bm)
         b.add(c)
         ctxs.append(c)
+    if args.schedule:
+        b.set_schedule(*(int(x) for x in args.schedule.split(",")))
     b.start()
     b.step(args.relax)
     for _ in range(args.warmup):
@@ -1111,6 +1113,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--schedule", default="",
+                    help="sweep/field: pin the batched advance's schedule 'shape,threshold,coarse' (default: tuned)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

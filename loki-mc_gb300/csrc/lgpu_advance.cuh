@@ -215,13 +215,14 @@ __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, Sh& sh) 
 __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const IntervalView& iv, Lane& L, int idx) {
   const float4 A = a.state[2 * idx];
   const float4 B = a.state[2 * idx + 1];
+  // the stream's seeding needs no state: it runs while the loads are in flight
+  L.rng.init((uint32_t)idx, iv.interval, a.seed, a.salt);
   if (B.w == 0.0f) {
     L.slot = idx;
     L.p = make_float3(A.x - iv.shift.x, A.y - iv.shift.y, A.z - iv.shift.z);
     L.v = make_float3(B.x, B.y, B.z);
     L.s = A.w;  // remaining flight in units of 1/nu (exponential variate), <0: draw
     L.t = 0.0f;
-    L.rng.init((uint32_t)idx, iv.interval, a.seed, a.salt);
     L.energy = energy_of(L.v, a.c.half_me_over_e);
     L.events = 0;
     L.pending = false;
@@ -444,20 +445,25 @@ __device__ __forceinline__ void block_flush(const AdvanceArgs& a, Sh& sh, const 
   }
 }
 
-// Lanes without an electron (`need`) take the next ones of the warp's chunk,
-// and a new chunk from the work counter when it runs out; `next`, `end` and
-// `exhausted` are the warp-uniform cursors.
+// Bulk prefetch of [p, p + bytes) into L2 (p and bytes multiples of 16).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+constexpr bool kPrefetchChunk = true;  // a claimed chunk's states, at the claim
+constexpr bool kPrefetchRows = true;   // a parked collision's cumulative row (stash shapes)
+
+// The index of the ensemble electron a lane claims (-1: none): the `n_want`
+// claiming lanes (this one `wants` it, rank r among them) take the next
+// electrons of the warp's chunk, and of a new chunk from the work counter
+// when it runs out; `next`, `end` and `exhausted` are the warp-uniform cursors.
 template <int CHUNK>
-__device__ __forceinline__ void lane_take_chunk(const AdvanceArgs& a, const IntervalView& iv, Lane& L,
-                                                unsigned need, int lane, unsigned lt_mask, int n_el, int& next,
-                                                int& end, bool& exhausted) {
-  const int n_need = __popc(need);
-  const int r = __popc(need & lt_mask);
+__device__ __forceinline__ int lane_claim(const AdvanceArgs& a, int n_want, int r, bool wants, int lane, int n_el,
+                                          int& next, int& end, bool& exhausted) {
   int idx = -1;
-  const int take = min(n_need, end - next);
-  if (!L.have && r < take) idx = next + r;
+  const int take = min(n_want, end - next);
+  if (wants && r < take) idx = next + r;
   next += take;
-  if (n_need > take) {
+  if (n_want > take) {
     int base = 0;
     if (lane == 0) base = atomicAdd(a.work_counter, CHUNK);
     base = __shfl_sync(0xffffffffu, base, 0);
@@ -466,12 +472,23 @@ __device__ __forceinline__ void lane_take_chunk(const AdvanceArgs& a, const Inte
     } else {
       next = base;
       end = min(base + CHUNK, n_el);
+      if (kPrefetchChunk && lane == 0) prefetch_l2(a.state + 2 * base, (uint32_t)(end - base) * 2u * sizeof(float4));
       const int r2 = r - take;
-      const int take2 = min(n_need - take, end - next);
-      if (!L.have && r2 >= 0 && r2 < take2) idx = next + r2;
+      const int take2 = min(n_want - take, end - next);
+      if (wants && r2 >= 0 && r2 < take2) idx = next + r2;
       next += take2;
     }
   }
+  return idx;
+}
+
+// Lanes without an electron (`need`) take the next ones of the warp's chunk.
+template <int CHUNK>
+__device__ __forceinline__ void lane_take_chunk(const AdvanceArgs& a, const IntervalView& iv, Lane& L,
+                                                unsigned need, int lane, unsigned lt_mask, int n_el, int& next,
+                                                int& end, bool& exhausted) {
+  const int idx = lane_claim<CHUNK>(a, __popc(need), __popc(need & lt_mask), !L.have, lane, n_el, next, end,
+                                    exhausted);
   if (idx >= 0) lane_take_electron(a, iv, L, idx);
 }
 
@@ -662,6 +679,13 @@ __device__ __forceinline__ void warp_loop_stash(const AdvanceArgs& a, Sh& sh, fl
     const unsigned pend = __ballot_sync(0xffffffffu, L.pending);
     if (pend) {
       if (L.pending) {
+        if (kPrefetchRows && !is_thermal(a.c, L.energy)) {
+          // the process choice reads this row at the collision turn
+          int i1;
+          float w1, w2;
+          row_weights(L.energy * iv.tab.inv_step, iv.tab.M, i1, w1, w2);
+          prefetch_l2(iv.tab.cum_pair + (size_t)i1 * iv.tab.stride, (uint32_t)iv.tab.stride * (uint32_t)sizeof(float2));
+        }
         const int r = __popc(pend & lt_mask), e = np + r;
         if (r < nr) {
           stash_swap<NS>(wst, e, L);
