@@ -10,10 +10,12 @@
 // of uniforms, or run a full solve() (BoltzmannMC.C:273-297) with a seeded
 // generator. Its outputs become the golden vectors under tests/golden/.
 #include "LoKI-MC/Headers/BoltzmannMC.h"
+#include "LoKI-MC/Headers/Constant.h"
 #include "LoKI-MC/Headers/FieldInfo.h"
 #include "LoKI-MC/Headers/Parse.h"
 #include "LoKI-MC/Headers/Setup.h"
 
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -325,6 +327,61 @@ void ref_get_energy_series(double* t, double* e) {
     t[i] = g_mc->samplingTimes[i];
     e[i] = g_mc->meanEnergies[i];
   }
+}
+
+// ---- EEDF post-processing pins (after ref_solve): the collision behind each
+// MC process, as the reference's end-of-job routines read it
+// (BoltzmannMC.C:2186-2266, 2268-2384; Collision.C:355-397)
+int ref_twoterm_sizes(int i, int* n_int, int* n_mom) {
+  Collision* c = g_mc->realCollisionPointers[i];
+  *n_int = (int)c->rawIntegralCrossSection[0].size();
+  *n_mom = (int)c->rawMomTransfCrossSection[0].size();
+  return g_mc->isSuperElastic[i] ? 1 : 0;
+}
+// s: kind (0 elastic, 1 inelastic, 2 superelastic copy), density (target's, the
+// product's for the copy), threshold (eV), m_e / M of the target gas,
+// g_target / g_product (reversible collisions, else 0), 1 ionization / 2 attachment
+void ref_get_twoterm(int i, double* s, double* int_e, double* int_v, double* mom_e, double* mom_v) {
+  Collision* c = g_mc->realCollisionPointers[i];
+  const bool sup = g_mc->isSuperElastic[i];
+  s[0] = sup ? 2.0 : (c->type == "Elastic" ? 0.0 : 1.0);
+  s[1] = sup ? c->productArray[0]->density : c->target->density;
+  s[2] = c->threshold;
+  s[3] = Constant::electronMass / c->target->gas->mass;
+  s[4] = c->isReverse ? c->target->statisticalWeight / c->productArray[0]->statisticalWeight : 0.0;
+  s[5] = c->type == "Ionization" ? 1.0 : (c->type == "Attachment" ? 2.0 : 0.0);
+  for (size_t k = 0; k < c->rawIntegralCrossSection[0].size(); ++k) {
+    int_e[k] = c->rawIntegralCrossSection[0][k];
+    int_v[k] = c->rawIntegralCrossSection[1][k];
+  }
+  for (size_t k = 0; k < c->rawMomTransfCrossSection[0].size(); ++k) {
+    mom_e[k] = c->rawMomTransfCrossSection[0][k];
+    mom_v[k] = c->rawMomTransfCrossSection[1][k];
+  }
+}
+// the EEDF-convolved rate coefficient of each MC process: ineRateCoeff of its
+// collision, supRateCoeff for a superelastic copy
+void ref_get_eedf_rates(double* rate) {
+  for (int i = 0; i < g_mc->nProcesses; ++i) {
+    Collision* c = g_mc->realCollisionPointers[i];
+    rate[i] = g_mc->isSuperElastic[i] ? c->supRateCoeff : c->ineRateCoeff;
+  }
+}
+double ref_swarm_param(const char* key) {
+  auto it = g_mc->swarmParam.find(key);
+  return it == g_mc->swarmParam.end() ? NAN : it->second;
+}
+// omega, omega_c, gas density, energy-grid step and cell number
+void ref_get_twoterm_grid(double* s) {
+  s[0] = g_mc->excitationFrequencyRadians;
+  s[1] = g_mc->cyclotronFrequency;
+  s[2] = g_mc->totalGasDensity;
+  s[3] = g_mc->energyGrid->step;
+  s[4] = (double)g_mc->energyGrid->cellNumber;
+}
+// the total momentum-transfer cross section on the grid nodes
+void ref_get_total_mt(double* mt) {
+  for (int k = 0; k < (int)g_mc->totalMomTransfCrossSection.size(); ++k) mt[k] = g_mc->totalMomTransfCrossSection[k];
 }
 
 // Statistical helpers used by the engine's host side.
