@@ -341,6 +341,54 @@ void* lgpu_batch_stream(lgpu_batch* batch);
  * not depend on it. */
 int lgpu_batch_set_schedule(lgpu_batch* batch, int shape, int real_batch, int coarse);
 
+/* ---- EEDF post-processing on the device ----
+ *
+ * The reference's end-of-job routines that read the EEDF, run in FP64 on the
+ * device: the EEDF-convolved rate coefficient of every collision
+ * (Collision::evaluateRateCoeff, Collision.C:355-397; called from
+ * BoltzmannMC::evaluateRateCoeff, BoltzmannMC.C:2268-2384) and the two-term
+ * swarm parameters (BoltzmannMC::evaluateSwarmParameters,
+ * BoltzmannMC.C:2186-2266). They read each collision's own cross sections as
+ * the reference's Collision holds them (the raw LXCat table, and the
+ * momentum-transfer one its angular law gives, Collision.C:127-199), which
+ * lgpu_set_twoterm takes per MC process, in the lgpu_set_processes order. */
+typedef struct lgpu_twoterm_process {
+  int kind;          /* 0 elastic, 1 inelastic (excitation, ionization, attachment, ...), 2 superelastic copy */
+  int ion;           /* 1 ionization, 2 attachment, 0 otherwise */
+  double density;    /* relative density of the target (of the product, for a superelastic copy) */
+  double threshold;  /* eV (the forward collision's, for a superelastic copy) */
+  double mass_ratio; /* m_e / M of the target gas (used for elastic collisions) */
+  double stat_ratio; /* g_target / g_product of a reversible collision (used by its superelastic copy) */
+  int n_int, n_mom;  /* points of the raw integral and momentum-transfer tables (n_mom 0: the integral one) */
+  const double* int_e; /* eV, increasing */
+  const double* int_v; /* m^2 */
+  const double* mom_e;
+  const double* mom_v;
+} lgpu_twoterm_process;
+int lgpu_set_twoterm(lgpu_ctx* ctx, const lgpu_twoterm_process* p, int n);
+
+/* The two-term swarm parameters, named as the reference's swarmParam keys. */
+typedef struct lgpu_eedf_params {
+  double tot_ion_rate, tot_att_rate;       /* totalIonRateCoeff, totalAttRateCoeff (m^3/s) */
+  double mom_transf_freq;                  /* momTransfFreq (1/s) */
+  double energy_relax_freq;                /* energyRelaxFreq */
+  double energy_relax_freq_classic;        /* energyRelaxFreqClassic */
+  double red_diff_energy, red_mob_energy;  /* redDiffCoeffEnergy_eedf, redMobCoeffEnergy_eedf */
+  double red_diff, red_mob_dc;             /* redDiffCoeff_eedf, redMobCoeff_DC_eedf */
+  double charac_energy;                    /* characEnergy_eedf (eV) */
+  double red_mob_xx_re, red_mob_xx_im;     /* redMobCoeff_xx_{real,imag}_eedf */
+  double red_mob_xy_re, red_mob_xy_im;     /* redMobCoeff_xy_{real,imag}_eedf */
+  double red_mob_zz_re, red_mob_zz_im;     /* redMobCoeff_zz_{real,imag}_eedf */
+} lgpu_eedf_params;
+/* eedf NULL: the context's own time-averaged EEDF (after lgpu_solve or a
+ * batch); else n_cells values on cells of width max_energy / n_cells (the
+ * grid of Grid::updateMaxValue, Grid.C:44-53). The field frequencies and the
+ * gas density are the context's conditions. rate[n] (n = the process count;
+ * may be NULL): each MC process's EEDF-convolved rate coefficient (m^3/s),
+ * the superelastic one for a superelastic copy. */
+int lgpu_eedf_postprocess(lgpu_ctx* ctx, const double* eedf, int n_cells, double max_energy, lgpu_eedf_params* out,
+                          double* rate, int n);
+
 /* ---- serving: continuous batching of swarm jobs ----
  *
  * No counterpart in the reference. A server owns one device and one thread

@@ -114,6 +114,17 @@ int lgpu_get_distributions(lgpu_ctx* ctx, double* cells, double* eedf, double* e
   return ctx->e->distributions(cells, eedf, efadf, esadf, eadf, evdf, rcells, acells, eedf_per);
 }
 
+int lgpu_set_twoterm(lgpu_ctx* ctx, const lgpu_twoterm_process* p, int n) {
+  CTX_CHECK(ctx);
+  return ctx->e->set_twoterm(p, n);
+}
+
+int lgpu_eedf_postprocess(lgpu_ctx* ctx, const double* eedf, int n_cells, double max_energy, lgpu_eedf_params* out,
+                          double* rate, int n) {
+  CTX_CHECK(ctx);
+  return ctx->e->eedf_postprocess(eedf, n_cells, max_energy, out, rate, n);
+}
+
 int lgpu_get_periodic(lgpu_ctx* ctx, double* n, double* me, double* fv, double* bv, double* fd, double* bd) {
   CTX_CHECK(ctx);
   return ctx->e->periodic(n, me, fv, bv, fd, bd);

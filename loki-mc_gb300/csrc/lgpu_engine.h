@@ -166,7 +166,7 @@ class Engine {
                     d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_nu_coarse_, d_cum_pair_, d_sig_pair_, d_procf_,
                     d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
                     d_raw_e_, d_raw_v_, d_proc_count_, d_proc_gain_, d_proc_loss_, d_eedf_, d_eedf_per_, d_eadf_,
-                    d_evdf_, d_rp_in_, d_rp_out_};
+                    d_evdf_, d_rp_in_, d_rp_out_, d_tt_i_, d_tt_d_, d_tt_raw_, d_post_};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_sc_) cudaFreeHost(h_sc_);
@@ -1425,6 +1425,148 @@ class Engine {
     return LGPU_OK;
   }
 
+  // ------------------------------------------- EEDF post-processing
+  // The collisions behind the MC processes as the reference's end-of-job
+  // routines read them (lgpu_set_twoterm): 6 int columns of P (kind, ion,
+  // integral offset and length, momentum-transfer offset and length) and 4
+  // double columns (density, threshold, mass ratio, statistical-weight
+  // ratio); the raw tables back to back (integral energies, values,
+  // momentum-transfer energies, values).
+  int tt_n_ = 0;
+  int* d_tt_i_ = nullptr;
+  double* d_tt_d_ = nullptr;
+  double* d_tt_raw_ = nullptr;
+  size_t tt_int_total_ = 0, tt_mom_total_ = 0;
+  double* d_post_ = nullptr;  // external EEDF, scratch, outputs
+  size_t post_cap_ = 0;
+
+  int set_twoterm(const lgpu_twoterm_process* q, int n) {
+    if (P_ <= 0) return fail(LGPU_ERR_STATE, "set the processes before their two-term inputs");
+    if (!q || n != P_) return fail(LGPU_ERR_BAD_ARG, "expected %d processes", P_);
+    std::vector<int> vi(6 * (size_t)n);
+    std::vector<double> vd(4 * (size_t)n), ie, iv, me, mv;
+    for (int p = 0; p < n; ++p) {
+      const lgpu_twoterm_process& c = q[p];
+      if (c.kind < 0 || c.kind > 2 || c.ion < 0 || c.ion > 2)
+        return fail(LGPU_ERR_BAD_ARG, "process %d: kind %d / ion %d out of range", p, c.kind, c.ion);
+      if (c.kind == 2 && (p == 0 || q[p - 1].kind == 2))
+        return fail(LGPU_ERR_BAD_ARG, "process %d: a superelastic copy follows its forward collision", p);
+      if (c.n_int < 2 || !c.int_e || !c.int_v || (c.n_mom != 0 && (c.n_mom < 2 || !c.mom_e || !c.mom_v)))
+        return fail(LGPU_ERR_BAD_ARG, "process %d: raw tables need at least 2 points", p);
+      if (!(c.threshold >= 0) || !(c.density >= 0) || !(c.mass_ratio >= 0) || !(c.stat_ratio >= 0))
+        return fail(LGPU_ERR_BAD_ARG, "process %d: negative or NaN threshold, density or ratio", p);
+      // momentum transfer defaults to the integral cross section (isotropic scattering)
+      const int nm = c.n_mom ? c.n_mom : c.n_int;
+      const double* e2 = c.n_mom ? c.mom_e : c.int_e;
+      const double* v2 = c.n_mom ? c.mom_v : c.int_v;
+      for (int k = 1; k < c.n_int; ++k)
+        if (!(c.int_e[k] > c.int_e[k - 1])) return fail(LGPU_ERR_BAD_ARG, "process %d: integral energies not increasing", p);
+      for (int k = 1; k < nm; ++k)
+        if (!(e2[k] > e2[k - 1])) return fail(LGPU_ERR_BAD_ARG, "process %d: momentum-transfer energies not increasing", p);
+      vi[0 * (size_t)n + p] = c.kind;
+      vi[1 * (size_t)n + p] = c.ion;
+      vi[2 * (size_t)n + p] = (int)ie.size();
+      vi[3 * (size_t)n + p] = c.n_int;
+      vi[4 * (size_t)n + p] = (int)me.size();
+      vi[5 * (size_t)n + p] = nm;
+      vd[0 * (size_t)n + p] = c.density;
+      vd[1 * (size_t)n + p] = c.threshold;
+      vd[2 * (size_t)n + p] = c.mass_ratio;
+      vd[3 * (size_t)n + p] = c.stat_ratio;
+      ie.insert(ie.end(), c.int_e, c.int_e + c.n_int);
+      iv.insert(iv.end(), c.int_v, c.int_v + c.n_int);
+      me.insert(me.end(), e2, e2 + nm);
+      mv.insert(mv.end(), v2, v2 + nm);
+    }
+    std::vector<double> raw;
+    raw.reserve(2 * (ie.size() + me.size()));
+    raw.insert(raw.end(), ie.begin(), ie.end());
+    raw.insert(raw.end(), iv.begin(), iv.end());
+    raw.insert(raw.end(), me.begin(), me.end());
+    raw.insert(raw.end(), mv.begin(), mv.end());
+    for (void* d : {(void*)d_tt_i_, (void*)d_tt_d_, (void*)d_tt_raw_})
+      if (d) cudaFree(d);
+    d_tt_i_ = nullptr;
+    d_tt_d_ = nullptr;
+    d_tt_raw_ = nullptr;
+    tt_n_ = 0;
+    LGPU_TRY(dalloc(&d_tt_i_, vi.size()));
+    LGPU_TRY(dalloc(&d_tt_d_, vd.size()));
+    LGPU_TRY(dalloc(&d_tt_raw_, raw.size()));
+    LGPU_CU(copy(d_tt_i_, vi.data(), vi.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LGPU_CU(copy(d_tt_d_, vd.data(), vd.size() * sizeof(double), cudaMemcpyHostToDevice));
+    LGPU_CU(copy(d_tt_raw_, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice));
+    tt_int_total_ = ie.size();
+    tt_mom_total_ = me.size();
+    tt_n_ = n;
+    return LGPU_OK;
+  }
+
+  bool has_twoterm() const { return tt_n_ > 0 && tt_n_ == P_; }
+
+  // the reference's end-of-job routines that read the EEDF
+  // (Collision.C:355-397, BoltzmannMC.C:2186-2266), on the device
+  int eedf_postprocess(const double* eedf, int nc, double max_e, lgpu_eedf_params* out, double* rate, int n) {
+    if (!has_twoterm()) return fail(LGPU_ERR_STATE, "no two-term inputs: call lgpu_set_twoterm first");
+    if (rate && n != P_) return fail(LGPU_ERR_BAD_ARG, "expected %d processes", P_);
+    if (!eedf) {
+      nc = cfg_.n_energy_cells;
+      max_e = max_eedf_;
+      if (!(max_e > 0)) return fail(LGPU_ERR_STATE, "no EEDF yet: the distributions start at the steady state");
+    } else if (nc < 2 || !(max_e > 0)) {
+      return fail(LGPU_ERR_BAD_ARG, "an EEDF needs at least 2 cells and a positive maximum energy");
+    }
+    const size_t need = (size_t)nc + 5 * ((size_t)nc + 1) + (size_t)P_ + 16;
+    if (need > post_cap_) {
+      if (d_post_) cudaFree(d_post_);
+      d_post_ = nullptr;
+      post_cap_ = 0;
+      LGPU_TRY(dalloc(&d_post_, need));
+      post_cap_ = need;
+    }
+    EedfPostArgs a{};
+    a.nc = nc;
+    a.P = P_;
+    a.max_energy = max_e;
+    a.gas_density = Ngas_;
+    a.omega = omega_;
+    a.omega_c = omega_c_;
+    a.eeh = d_eedf_;
+    if (eedf) {
+      LGPU_CU(cudaMemcpyAsync(d_post_, eedf, (size_t)nc * sizeof(double), cudaMemcpyHostToDevice, stream_));
+      a.eedf_in = d_post_;
+    }
+    a.scratch = d_post_ + nc;
+    a.rates = a.scratch + 5 * ((size_t)nc + 1);
+    a.params = a.rates + P_;
+    a.kind = d_tt_i_;
+    a.ion = d_tt_i_ + P_;
+    a.int_off = d_tt_i_ + 2 * P_;
+    a.int_len = d_tt_i_ + 3 * P_;
+    a.mom_off = d_tt_i_ + 4 * P_;
+    a.mom_len = d_tt_i_ + 5 * P_;
+    a.dens = d_tt_d_;
+    a.thr = d_tt_d_ + P_;
+    a.mass_ratio = d_tt_d_ + 2 * P_;
+    a.stat = d_tt_d_ + 3 * P_;
+    a.raw_ie = d_tt_raw_;
+    a.raw_iv = d_tt_raw_ + tt_int_total_;
+    a.raw_me = d_tt_raw_ + 2 * tt_int_total_;
+    a.raw_mv = d_tt_raw_ + 2 * tt_int_total_ + tt_mom_total_;
+    launch_eedf_post(a, stream_);
+    ++launches_;
+    LGPU_CU(cudaGetLastError());
+    std::vector<double> res((size_t)P_ + 16);
+    LGPU_CU(cudaMemcpyAsync(res.data(), a.rates, res.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LGPU_TRY(sync("eedf post-processing"));
+    if (rate) std::copy(res.begin(), res.begin() + P_, rate);
+    if (out) {
+      const double* v = res.data() + P_;
+      *out = lgpu_eedf_params{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12],
+                              v[13], v[14], v[15]};
+    }
+    return LGPU_OK;
+  }
   // ------------------------------------------------------------ replay
   double* d_rp_in_ = nullptr;
   double* d_rp_out_ = nullptr;

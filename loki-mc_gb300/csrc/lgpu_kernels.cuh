@@ -274,6 +274,34 @@ void advance_shape(int shape, int* threads, int* blocks_per_sm, int* chunk, int*
 cudaError_t prepare_advance_stash();
 int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 
+// End-of-job EEDF post-processing in FP64 (lgpu_post.cu): the EEDF-convolved
+// rate coefficient of every MC process (Collision.C:355-397) and the two-term
+// swarm parameters (BoltzmannMC.C:2186-2266), one block.
+struct EedfPostArgs {
+  int nc, P;
+  double max_energy, gas_density, omega, omega_c;
+  const double* eedf_in;   // normalised EEDF [nc], or null: normalise eeh
+  const double* eeh;       // histogram sums [nc]
+  const int* kind;         // per process: 0 elastic, 1 inelastic, 2 superelastic copy
+  const int* ion;          // 1 ionization, 2 attachment
+  const double* dens;      // target (product) relative density
+  const double* thr;       // threshold (eV)
+  const double* mass_ratio;
+  const double* stat;      // g_target / g_product
+  const int* int_off;
+  const int* int_len;
+  const int* mom_off;
+  const int* mom_len;
+  const double* raw_ie;
+  const double* raw_iv;
+  const double* raw_me;
+  const double* raw_mv;
+  double* scratch;         // 5 x (nc + 1)
+  double* rates;           // [P]
+  double* params;          // [16], lgpu_eedf_params order
+};
+void launch_eedf_post(const EedfPostArgs& a, cudaStream_t s);
+
 // Replay kernels for the parity tests: the production device functions
 // driven by given inputs and recorded uniforms.
 struct ReplayFlightArgs {

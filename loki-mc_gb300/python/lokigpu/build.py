@@ -20,6 +20,8 @@ BUILD = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libloki_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+# per-file flags: the EEDF post-processing rounds every step as the reference does
+FILE_FLAGS = {"lgpu_post.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -53,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append([nvcc()] + ARCH + FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc()] + ARCH + FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:

@@ -26,7 +26,7 @@ STATUS = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ENERGY_ABOVE_TABLE", 4: "TIMEOUT"
 EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_stream",
             "lgpu_set_processes", "lgpu_set_conditions", "lgpu_init_ensemble", "lgpu_advance", "lgpu_solve",
             "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
-            "lgpu_get_timing",
+            "lgpu_get_timing", "lgpu_set_twoterm", "lgpu_eedf_postprocess",
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
             "lgpu_replay_collisions_coarse", "lgpu_replay_flights_noalloc",
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
@@ -91,6 +91,30 @@ class Timing(ctypes.Structure):
                 ("h2d_bytes", D), ("d2h_bytes", D)]
 
 
+class TwotermProcess(ctypes.Structure):
+    _fields_ = [("kind", I), ("ion", I), ("density", D), ("threshold", D), ("mass_ratio", D), ("stat_ratio", D),
+                ("n_int", I), ("n_mom", I), ("int_e", P_(D)), ("int_v", P_(D)), ("mom_e", P_(D)),
+                ("mom_v", P_(D))]
+
+
+# lgpu_eedf_params, in field order, with the reference's swarmParam keys
+EEDF_PARAM_KEYS = ("totalIonRateCoeff", "totalAttRateCoeff", "momTransfFreq", "energyRelaxFreq",
+                   "energyRelaxFreqClassic", "redDiffCoeffEnergy_eedf", "redMobCoeffEnergy_eedf", "redDiffCoeff_eedf",
+                   "redMobCoeff_DC_eedf", "characEnergy_eedf", "redMobCoeff_xx_real_eedf",
+                   "redMobCoeff_xx_imag_eedf", "redMobCoeff_xy_real_eedf", "redMobCoeff_xy_imag_eedf",
+                   "redMobCoeff_zz_real_eedf", "redMobCoeff_zz_imag_eedf")
+
+
+class EedfParams(ctypes.Structure):
+    _fields_ = [(k, D) for k in ("tot_ion_rate", "tot_att_rate", "mom_transf_freq", "energy_relax_freq",
+                                 "energy_relax_freq_classic", "red_diff_energy", "red_mob_energy", "red_diff",
+                                 "red_mob_dc", "charac_energy", "red_mob_xx_re", "red_mob_xx_im", "red_mob_xy_re",
+                                 "red_mob_xy_im", "red_mob_zz_re", "red_mob_zz_im")]
+
+    def values(self):
+        return np.array([getattr(self, f[0]) for f in self._fields_])
+
+
 class BatchReport(ctypes.Structure):
     _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
@@ -145,6 +169,8 @@ def load(path: str | None = None):
     lib.lgpu_solve.argtypes = [ctypes.c_void_p, P_(Result)]
     lib.lgpu_get_process_results.argtypes = [ctypes.c_void_p, P_(ctypes.c_ulonglong), P_(D), P_(D), P_(D), I]
     lib.lgpu_get_distributions.argtypes = [ctypes.c_void_p] + [P_(D)] * 9
+    lib.lgpu_set_twoterm.argtypes = [ctypes.c_void_p, P_(TwotermProcess), I]
+    lib.lgpu_eedf_postprocess.argtypes = [ctypes.c_void_p, P_(D), I, D, P_(EedfParams), P_(D), I]
     lib.lgpu_get_periodic.argtypes = [ctypes.c_void_p] + [P_(D)] * 6
     lib.lgpu_get_series.argtypes = [ctypes.c_void_p, I, P_(D), LL]
     lib.lgpu_get_series.restype = LL
@@ -314,6 +340,44 @@ class Context:
         rate, gain, loss = np.zeros(P), np.zeros(P), np.zeros(P)
         self.check(self.lib.lgpu_get_process_results(self.h, cnt, dptr(rate), dptr(gain), dptr(loss), P))
         return np.array(cnt[:], dtype=np.uint64), rate, gain, loss
+
+    def set_twoterm(self, procs):
+        """The collision behind each MC process for the EEDF post-processing:
+        dicts with kind (0 elastic, 1 inelastic, 2 superelastic copy), ion
+        (1 ionization, 2 attachment), density, threshold, mass_ratio,
+        stat_ratio and the raw tables int_e, int_v, mom_e, mom_v (mom_* may be
+        absent: the integral table)."""
+        arr = (TwotermProcess * len(procs))()
+        keep = []
+        for k, q in enumerate(procs):
+            t = arr[k]
+            t.kind, t.ion = int(q["kind"]), int(q.get("ion", 0))
+            t.density, t.threshold = float(q["density"]), float(q["threshold"])
+            t.mass_ratio, t.stat_ratio = float(q.get("mass_ratio", 0.0)), float(q.get("stat_ratio", 0.0))
+            tabs = [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("int_e", "int_v")]
+            if q.get("mom_e") is not None:
+                tabs += [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("mom_e", "mom_v")]
+            keep.append(tabs)
+            t.n_int = len(tabs[0])
+            t.int_e, t.int_v = dptr(tabs[0]), dptr(tabs[1])
+            if len(tabs) == 4:
+                t.n_mom = len(tabs[2])
+                t.mom_e, t.mom_v = dptr(tabs[2]), dptr(tabs[3])
+        self.check(self.lib.lgpu_set_twoterm(self.h, arr, len(procs)))
+
+    def eedf_postprocess(self, eedf=None, max_energy=0.0):
+        """(EedfParams, rates): the EEDF-convolved rate coefficients and the
+        two-term swarm parameters, on the device, of the given EEDF or (None)
+        the context's own."""
+        out = EedfParams()
+        rate = np.zeros(self.P)
+        if eedf is None:
+            self.check(self.lib.lgpu_eedf_postprocess(self.h, None, 0, 0.0, ctypes.byref(out), dptr(rate), self.P))
+        else:
+            e = np.ascontiguousarray(eedf, dtype=np.float64)
+            self.check(self.lib.lgpu_eedf_postprocess(self.h, dptr(e), len(e), float(max_energy), ctypes.byref(out),
+                                                      dptr(rate), self.P))
+        return out, rate
 
     def distributions(self):
         c = self.cfg

@@ -58,10 +58,10 @@ def run(name, seed):
     lib = mg.open_ref(tmp, setup)
     lib.ref_swarm_param.restype = D
     lib.ref_rng_seed(ctypes.c_uint64(seed))
-    proc = mg.dump_processes(lib)
     P = lib.ref_n_processes()
     r = np.zeros(39)
     lib.ref_solve(mg.ptr(r), mg.ptr(np.zeros(P)))
+    proc = mg.dump_processes(lib)  # after the solve has set the relative densities (BoltzmannMC.C:439-455)
     nc = lib.ref_n_eedf_cells()
     cells, eedf = np.zeros(nc), np.zeros(nc)
     lib.ref_get_eedf(mg.ptr(cells), mg.ptr(eedf))

@@ -32,6 +32,9 @@ def test_fixtures_cover_the_cases():
         d = np.load(f)
         kinds |= {int(k) for k in d["twoterm_scalars"][:, 0]}
         kinds |= {10 + int(k) for k in d["twoterm_scalars"][:, 5]}
+        # the MC flattening's relative densities are the collisions' target
+        # (product, for a superelastic copy) densities
+        assert np.array_equal(d["proc_rel_dens"], d["twoterm_scalars"][:, 1])
     assert kinds >= {0, 1, 2, 11, 12}  # elastic, inelastic, superelastic, ionization, attachment
 
 
