@@ -410,6 +410,9 @@ typedef struct lgpu_job {
   int n_gases;
   double emax_elastic;            /* as lgpu_set_processes */
   lgpu_conditions conditions;
+  const lgpu_twoterm_process* twoterm; /* n_procs entries, copied at submission, or NULL: with them the
+                                          server post-processes the job's EEDF on the device at its end
+                                          (lgpu_server_job_eedf) */
 } lgpu_job;
 
 #define LGPU_JOB_QUEUED 0
@@ -449,6 +452,11 @@ int lgpu_server_wait(lgpu_server* server, long long job_id, double timeout_s, lg
 /* Per-process collision counts and rate coefficients of a finished job
  * (as lgpu_get_process_results; n = the job's process count). */
 int lgpu_server_job_rates(lgpu_server* server, long long job_id, unsigned long long* counts, double* rate, int n);
+/* The EEDF post-processing of a finished job submitted with two-term inputs
+ * (lgpu_job.twoterm; a request's jobs carry them): its two-term swarm
+ * parameters and each process's EEDF-convolved rate coefficient, computed on
+ * the device at the job's end. LGPU_ERR_STATE for other jobs. */
+int lgpu_server_job_eedf(lgpu_server* server, long long job_id, lgpu_eedf_params* params, double* rate, int n);
 /* A queued job is dropped; a running one stops at its next interval. */
 int lgpu_server_cancel(lgpu_server* server, long long job_id);
 /* Drops the record of a finished (done, failed or cancelled) job: its status,

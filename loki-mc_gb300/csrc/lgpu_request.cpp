@@ -31,6 +31,7 @@
 // a process with an anisotropic law (the reference converts them with an
 // angular integration, Collision.C:127-199), per-collision anisotropy lines,
 // state properties other than energy, statistical weight and population.
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -389,9 +390,69 @@ struct lgpu_request {
   std::vector<lgpu_gas> gases;
   double emax_elastic = 0;
   std::vector<lgpu_conditions> jobs;
+  // the collision behind each process for the EEDF post-processing, and its
+  // tables (integral energies, values, momentum-transfer energies, values)
+  std::vector<lgpu_twoterm_process> twoterm;
+  std::vector<std::array<std::vector<double>, 4>> twoterm_tabs;
 };
 
 namespace {
+
+// Angular distribution I(e, theta) of a scattering law, normalised so that
+// 2 pi Int_0^pi I sin(theta) dtheta = 1 (AngularDistributionFunctions.h:32-110):
+// Born dipole (Vialetto et al. 2021, eq. 23), Surendra (Vahedi and Surendra
+// 1995, eq. 7), screened Coulomb (Hagelaar et al. 2000, eqs. 21-23); the
+// isotropic law and the momentum-conserving ionization law are 1/(4 pi).
+double angular_distribution(int law, const std::vector<double>& par, double thr, double e, double th) {
+  const double iso = 1.0 / (4.0 * M_PI);
+  switch (law) {
+    case 2: {  // Born dipole
+      const double ea = e - thr;
+      if (ea <= 0) return iso;
+      const double q2 = ea + e - 2.0 * std::sqrt(e * ea) * std::cos(th);
+      const double se = std::sqrt(e), sa = std::sqrt(ea);
+      return 1.0 / (4.0 * M_PI) * se * sa / q2 / std::log((sa + se) / std::sqrt(thr));
+    }
+    case 3: {  // Surendra
+      if (e == 0) return iso;
+      return e / (4.0 * M_PI * (1.0 + e * std::pow(std::sin(th / 2.0), 2)) * std::log(1.0 + e));
+    }
+    case 4: {  // screened Coulomb: the incident energy (p0 = 0) or the energy after the loss
+      const double eps = (par.size() > 0 && par[0] != 0) ? e - thr : e;
+      if (eps <= 0) return iso;
+      const double sp = (par.size() > 1 ? par[1] : 0.0) / eps;
+      return (sp * (sp + 1.0)) / M_PI / std::pow(2.0 * sp + 1.0 - std::cos(th), 2);
+    }
+    default:
+      return iso;
+  }
+}
+
+// The momentum-transfer cross section a scattering law gives an integral one
+// (Collision.C:127-199): sigma_m = sigma (1 - 2 pi Int_0^pi I cos sin dtheta),
+// the integral by the trapezoidal rule over n_ang angles in [0, pi] laid out
+// as Eigen's LinSpaced lays them; isotropic: sigma_m = sigma; forward: 0.
+std::vector<double> momentum_transfer(int law, const std::vector<double>& par, double thr, int n_ang,
+                                      const std::vector<double>& e, const std::vector<double>& v) {
+  if (law == 0) return v;
+  if (law == 1) return std::vector<double>(v.size(), 0.0);
+  if (n_ang < 2) throw Error("anisotropicScattering.angleNumber must be at least 2");
+  const double step = M_PI / (n_ang - 1.0);
+  std::vector<double> ang(n_ang), aux(n_ang);
+  for (int j = 0; j < n_ang; ++j) {
+    ang[j] = j == n_ang - 1 ? M_PI : (double)j * step;
+    aux[j] = std::cos(ang[j]) * std::sin(ang[j]);
+  }
+  std::vector<double> m(v.size());
+  for (size_t i = 0; i < e.size(); ++i) {
+    double integ = aux[0] * angular_distribution(law, par, thr, e[i], ang[0]);
+    for (int j = 1; j < n_ang - 1; ++j) integ += 2.0 * aux[j] * angular_distribution(law, par, thr, e[i], ang[j]);
+    integ += aux[n_ang - 1] * angular_distribution(law, par, thr, e[i], ang[n_ang - 1]);
+    integ *= M_PI * step;
+    m[i] = v[i] * (1.0 - integ);
+  }
+  return m;
+}
 
 // a state family "G(X,v=*)" matches "G(X,v=3)"
 bool matches(const std::string& pattern, const std::string& name) {
@@ -584,8 +645,10 @@ void parse_request(const std::string& setup, const std::map<std::string, std::st
   };
   // angular scattering laws: "group;gas;type;law;params"
   std::map<std::pair<std::string, std::string>, std::pair<int, std::vector<double>>> laws;
+  int n_angles = 0;
   const Node* an = ek->child("anisotropicScattering");
   if (an && an->child("isOn") && an->child("isOn")->value == "true") {
+    if (an->child("angleNumber")) n_angles = (int)value_of(an->child("angleNumber")->value);
     const Node* lines = an->child("collisions");
     for (const std::string& it : lines ? lines->items : std::vector<std::string>()) {
       const auto f = split_top(no_spaces(it), ';');
@@ -622,6 +685,8 @@ void parse_request(const std::string& setup, const std::map<std::string, std::st
         e.insert(e.begin(), 0.0);
         v.insert(v.begin(), v[0]);
       }
+      // the collision's own tables, as the end-of-job routines read them
+      std::array<std::vector<double>, 4> tabs{e, v, e, momentum_transfer(sampler, sp_par, c.threshold, n_angles, e, v)};
       size_t below = 0;  // BoltzmannMC.C:139-147
       while (below < e.size() && e[below] < c.threshold) ++below;
       e.erase(e.begin(), e.begin() + (long)below);
@@ -647,12 +712,27 @@ void parse_request(const std::string& setup, const std::map<std::string, std::st
       r.procs.push_back(q);
       r.raw_e.push_back(e);
       r.raw_v.push_back(v);
+      lgpu_twoterm_process tt{};
+      tt.kind = c.type == "Elastic" ? 0 : 1;
+      tt.ion = q.type == 1 ? 1 : (q.type == 2 ? 2 : 0);
+      tt.density = q.rel_dens;
+      tt.threshold = c.threshold;
+      tt.mass_ratio = kElectronMass / g.mass;
+      r.twoterm.push_back(tt);
+      r.twoterm_tabs.push_back(tabs);
       ++it;
       if (c.reverse) {
         const StateProp& st = states[c.target];
         const StateProp& sp2 = states[c.product];
         if (!st.has_weight || !sp2.has_weight)
           throw Error("the reversible collision " + c.target + " <-> " + c.product + " needs both statistical weights");
+        r.twoterm.back().stat_ratio = st.weight / sp2.weight;
+        lgpu_twoterm_process ts = r.twoterm.back();
+        ts.kind = 2;
+        ts.ion = 0;
+        ts.density = density(g, c.product);
+        r.twoterm.push_back(ts);
+        r.twoterm_tabs.push_back(tabs);
         lgpu_process s = q;
         s.is_super = 1;
         s.is_elastic = 0;
@@ -677,6 +757,14 @@ void parse_request(const std::string& setup, const std::map<std::string, std::st
     r.procs[p].raw_len = (int)r.raw_e[p].size();
     r.procs[p].raw_e = r.raw_e[p].empty() ? nullptr : r.raw_e[p].data();
     r.procs[p].raw_v = r.raw_v[p].empty() ? nullptr : r.raw_v[p].data();
+    lgpu_twoterm_process& t = r.twoterm[p];
+    const auto& tb = r.twoterm_tabs[p];
+    t.n_int = (int)tb[0].size();
+    t.n_mom = (int)tb[2].size();
+    t.int_e = tb[0].data();
+    t.int_v = tb[1].data();
+    t.mom_e = tb[2].data();
+    t.mom_v = tb[3].data();
   }
 }
 
@@ -716,6 +804,7 @@ int lgpu_request_job(const lgpu_request* req, int k, lgpu_job* job) {
   job->n_gases = (int)req->gases.size();
   job->emax_elastic = req->emax_elastic;
   job->conditions = req->jobs[k];
+  job->twoterm = req->twoterm.data();
   return LGPU_OK;
 }
 

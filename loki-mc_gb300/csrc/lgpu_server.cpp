@@ -14,6 +14,8 @@
 //
 // Host threads: any number of submitters/pollers (one mutex), one worker that
 // owns every CUDA call.
+#include <algorithm>
+#include <array>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -46,6 +48,12 @@ struct JobRec {
   lgpu_result result{};
   std::vector<unsigned long long> counts;
   std::vector<double> rate;
+  // two-term inputs (until admission) and the EEDF post-processing's results
+  std::vector<lgpu_twoterm_process> twoterm;
+  std::vector<std::array<std::vector<double>, 4>> twoterm_tabs;
+  bool has_eedf = false;
+  lgpu_eedf_params eedf{};
+  std::vector<double> eedf_rate;
   // worker-only
   Engine* engine = nullptr;
   int member = -1;
@@ -124,6 +132,25 @@ class Server {
     r->gases.assign(j.gases, j.gases + j.n_gases);
     r->emax = j.emax_elastic;
     r->cond = j.conditions;
+    if (j.twoterm) {
+      r->twoterm.assign(j.twoterm, j.twoterm + j.n_procs);
+      r->twoterm_tabs.resize(j.n_procs);
+      for (int p = 0; p < j.n_procs; ++p) {
+        lgpu_twoterm_process& t = r->twoterm[p];
+        if (t.n_int < 2 || !t.int_e || !t.int_v || (t.n_mom && (!t.mom_e || !t.mom_v))) return LGPU_ERR_BAD_ARG;
+        auto& tb = r->twoterm_tabs[p];
+        tb[0].assign(t.int_e, t.int_e + t.n_int);
+        tb[1].assign(t.int_v, t.int_v + t.n_int);
+        if (t.n_mom) {
+          tb[2].assign(t.mom_e, t.mom_e + t.n_mom);
+          tb[3].assign(t.mom_v, t.mom_v + t.n_mom);
+        }
+        t.int_e = tb[0].data();
+        t.int_v = tb[1].data();
+        t.mom_e = t.n_mom ? tb[2].data() : nullptr;
+        t.mom_v = t.n_mom ? tb[3].data() : nullptr;
+      }
+    }
     r->footprint = Engine::footprint_bytes(r->cfg, j.n_procs, r->raw_points);
     std::lock_guard<std::mutex> lock(mu_);
     if (stop_) return LGPU_ERR_STATE;
@@ -174,6 +201,18 @@ class Server {
       cv_done_.wait(lock, pred);
     }
     if (st) fill_status(*r, st);
+    return LGPU_OK;
+  }
+
+  int eedf_results(long long id, lgpu_eedf_params* out, double* rate, int n) {
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return LGPU_ERR_BAD_ARG;
+    const JobRec& r = *it->second;
+    if (r.state != LGPU_JOB_DONE || !r.has_eedf) return LGPU_ERR_STATE;
+    if (rate && n != r.n_procs) return LGPU_ERR_BAD_ARG;
+    if (out) *out = r.eedf;
+    if (rate) std::copy(r.eedf_rate.begin(), r.eedf_rate.end(), rate);
     return LGPU_OK;
   }
 
@@ -285,6 +324,7 @@ class Server {
     int rc = e->init();
     if (rc == LGPU_OK) rc = e->set_processes(r->procs.data(), (int)r->procs.size(), r->gases.data(), (int)r->gases.size(), r->emax);
     if (rc == LGPU_OK) rc = e->set_conditions(r->cond);
+    if (rc == LGPU_OK && !r->twoterm.empty()) rc = e->set_twoterm(r->twoterm.data(), (int)r->twoterm.size());
     if (rc == LGPU_OK) rc = batch_.add(e);
     if (rc != LGPU_OK) return rc;
     r->member = batch_.end_id() - 1;
@@ -292,6 +332,8 @@ class Server {
     std::vector<lgpu_process>().swap(r->procs);
     std::vector<std::vector<double>>().swap(r->raw_e);
     std::vector<std::vector<double>>().swap(r->raw_v);
+    std::vector<lgpu_twoterm_process>().swap(r->twoterm);
+    std::vector<std::array<std::vector<double>, 4>>().swap(r->twoterm_tabs);
     batch_.admit();
     const Batch::Member& m = batch_.member(r->member);
     if (m.done) return m.status == LGPU_OK ? LGPU_ERR_STATE : m.status;
@@ -387,12 +429,20 @@ class Server {
         const Batch::Member& m = batch_.member(idx);
         int status = m.status;
         std::vector<unsigned long long> counts;
-        std::vector<double> rate;
+        std::vector<double> rate, eedf_rate;
+        lgpu_eedf_params eedf{};
+        bool has_eedf = false;
         if (status == LGPU_OK) {
           const int P = r->n_procs;
           counts.resize(P);
           rate.resize(P);
           status = r->engine->process_results(counts.data(), rate.data(), nullptr, nullptr, P);
+          // the end-of-job post-processing of the EEDF, on the device
+          if (status == LGPU_OK && r->engine->has_twoterm()) {
+            eedf_rate.resize(P);
+            status = r->engine->eedf_postprocess(nullptr, 0, 0.0, &eedf, eedf_rate.data(), P);
+            has_eedf = status == LGPU_OK;
+          }
         }
         const lgpu_result res = m.result;
         const std::string msg = status == LGPU_OK ? std::string() : r->engine->err_;
@@ -402,6 +452,9 @@ class Server {
         r->result = res;
         r->counts = std::move(counts);
         r->rate = std::move(rate);
+        r->has_eedf = has_eedf;
+        r->eedf = eedf;
+        r->eedf_rate = std::move(eedf_rate);
         retire(r, status == LGPU_OK ? LGPU_JOB_DONE : LGPU_JOB_FAILED, status);
       }
       if (running_.empty()) {
@@ -468,6 +521,11 @@ int lgpu_server_wait(lgpu_server* server, long long job_id, double timeout_s, lg
 int lgpu_server_job_rates(lgpu_server* server, long long job_id, unsigned long long* counts, double* rate, int n) {
   if (!server || !server->s) return LGPU_ERR_BAD_ARG;
   return server->s->rates(job_id, counts, rate, n);
+}
+
+int lgpu_server_job_eedf(lgpu_server* server, long long job_id, lgpu_eedf_params* params, double* rate, int n) {
+  if (!server || !server->s) return LGPU_ERR_BAD_ARG;
+  return server->s->eedf_results(job_id, params, rate, n);
 }
 
 int lgpu_server_cancel(lgpu_server* server, long long job_id) {

@@ -32,7 +32,7 @@ EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_err
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
             "lgpu_batch_start", "lgpu_batch_step", "lgpu_batch_stream", "lgpu_batch_set_schedule",
             "lgpu_server_start", "lgpu_server_submit", "lgpu_server_poll", "lgpu_server_wait",
-            "lgpu_server_job_rates", "lgpu_server_cancel", "lgpu_server_forget", "lgpu_server_report_get", "lgpu_server_last_error",
+            "lgpu_server_job_rates", "lgpu_server_job_eedf", "lgpu_server_cancel", "lgpu_server_forget", "lgpu_server_report_get", "lgpu_server_last_error",
             "lgpu_server_stop",
             "lgpu_request_parse", "lgpu_request_jobs", "lgpu_request_job", "lgpu_request_free",
             "lgpu_server_submit_request")
@@ -115,6 +115,31 @@ class EedfParams(ctypes.Structure):
         return np.array([getattr(self, f[0]) for f in self._fields_])
 
 
+def twoterm_array(procs):
+    """(lgpu_twoterm_process array, arrays it points into) from dicts with
+    kind (0 elastic, 1 inelastic, 2 superelastic copy), ion (1 ionization,
+    2 attachment), density, threshold, mass_ratio, stat_ratio and the raw
+    tables int_e, int_v, mom_e, mom_v (mom_* may be absent: the integral
+    table)."""
+    arr = (TwotermProcess * len(procs))()
+    keep = []
+    for k, q in enumerate(procs):
+        t = arr[k]
+        t.kind, t.ion = int(q["kind"]), int(q.get("ion", 0))
+        t.density, t.threshold = float(q["density"]), float(q["threshold"])
+        t.mass_ratio, t.stat_ratio = float(q.get("mass_ratio", 0.0)), float(q.get("stat_ratio", 0.0))
+        tabs = [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("int_e", "int_v")]
+        if q.get("mom_e") is not None:
+            tabs += [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("mom_e", "mom_v")]
+        keep.append(tabs)
+        t.n_int = len(tabs[0])
+        t.int_e, t.int_v = tabs[0].ctypes.data_as(P_(D)), tabs[1].ctypes.data_as(P_(D))
+        if len(tabs) == 4:
+            t.n_mom = len(tabs[2])
+            t.mom_e, t.mom_v = tabs[2].ctypes.data_as(P_(D)), tabs[3].ctypes.data_as(P_(D))
+    return arr, keep
+
+
 class BatchReport(ctypes.Structure):
     _fields_ = [("intervals", LL), ("kernel_launches", LL), ("elapsed", D), ("real_collisions", D),
                 ("null_collisions", D), ("advance_ms", D), ("electron_steps", D), ("h2d_bytes", D),
@@ -125,7 +150,7 @@ class BatchReport(ctypes.Structure):
 
 class Job(ctypes.Structure):
     _fields_ = [("config", Config), ("procs", P_(Process)), ("n_procs", I), ("gases", P_(Gas)), ("n_gases", I),
-                ("emax_elastic", D), ("conditions", Conditions)]
+                ("emax_elastic", D), ("conditions", Conditions), ("twoterm", P_(TwotermProcess))]
 
 
 class JobStatus(ctypes.Structure):
@@ -197,6 +222,7 @@ def load(path: str | None = None):
     lib.lgpu_server_poll.argtypes = [VP, LL, P_(JobStatus)]
     lib.lgpu_server_wait.argtypes = [VP, LL, D, P_(JobStatus)]
     lib.lgpu_server_job_rates.argtypes = [VP, LL, P_(ctypes.c_ulonglong), P_(D), I]
+    lib.lgpu_server_job_eedf.argtypes = [VP, LL, P_(EedfParams), P_(D), I]
     lib.lgpu_server_cancel.argtypes = [VP, LL]
     lib.lgpu_server_forget.argtypes = [VP, LL]
     lib.lgpu_server_report_get.argtypes = [VP, P_(ServerReport)]
@@ -342,28 +368,11 @@ class Context:
         return np.array(cnt[:], dtype=np.uint64), rate, gain, loss
 
     def set_twoterm(self, procs):
-        """The collision behind each MC process for the EEDF post-processing:
-        dicts with kind (0 elastic, 1 inelastic, 2 superelastic copy), ion
-        (1 ionization, 2 attachment), density, threshold, mass_ratio,
-        stat_ratio and the raw tables int_e, int_v, mom_e, mom_v (mom_* may be
-        absent: the integral table)."""
-        arr = (TwotermProcess * len(procs))()
-        keep = []
-        for k, q in enumerate(procs):
-            t = arr[k]
-            t.kind, t.ion = int(q["kind"]), int(q.get("ion", 0))
-            t.density, t.threshold = float(q["density"]), float(q["threshold"])
-            t.mass_ratio, t.stat_ratio = float(q.get("mass_ratio", 0.0)), float(q.get("stat_ratio", 0.0))
-            tabs = [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("int_e", "int_v")]
-            if q.get("mom_e") is not None:
-                tabs += [np.ascontiguousarray(q[n], dtype=np.float64) for n in ("mom_e", "mom_v")]
-            keep.append(tabs)
-            t.n_int = len(tabs[0])
-            t.int_e, t.int_v = dptr(tabs[0]), dptr(tabs[1])
-            if len(tabs) == 4:
-                t.n_mom = len(tabs[2])
-                t.mom_e, t.mom_v = dptr(tabs[2]), dptr(tabs[3])
+        """The collision behind each MC process for the EEDF post-processing
+        (see twoterm_array)."""
+        arr, keep = twoterm_array(procs)
         self.check(self.lib.lgpu_set_twoterm(self.h, arr, len(procs)))
+        del keep
 
     def eedf_postprocess(self, eedf=None, max_energy=0.0):
         """(EedfParams, rates): the EEDF-convolved rate coefficients and the
@@ -542,16 +551,33 @@ class Server:
         return buf.value.decode(errors="replace")
 
     def submit(self, cfg: Config, ps, gas_first, gas_last, gas_fraction, N, Tg=300.0, red_field=0.0, angle=180.0,
-               freq_hz=0.0, red_mag=0.0) -> int:
+               freq_hz=0.0, red_mag=0.0, twoterm=None) -> int:
+        """twoterm: per process dicts (twoterm_array) for the EEDF
+        post-processing at the job's end, or None."""
         arr, gs, keep = process_arrays(ps, gas_first, gas_last, gas_fraction)
+        tt = None
+        if twoterm is not None:
+            tt, tkeep = twoterm_array(twoterm)
+            keep = (keep, tkeep, tt)
         job = Job(cfg, ctypes.cast(arr, P_(Process)), ps.n, ctypes.cast(gs, P_(Gas)), len(gas_first),
-                  float(ps.energy_max_elastic), Conditions(N, Tg, red_field, angle, freq_hz, red_mag))
+                  float(ps.energy_max_elastic), Conditions(N, Tg, red_field, angle, freq_hz, red_mag),
+                  ctypes.cast(tt, P_(TwotermProcess)) if tt is not None else None)
         jid = LL()
         rc = self.lib.lgpu_server_submit(self.h, ctypes.byref(job), ctypes.byref(jid))
         del keep  # the server copied every array
         if rc != LGPU_OK:
             raise LokiGpuError(rc, "lgpu_server_submit failed")
         return jid.value
+
+    def job_eedf(self, job_id, n_procs):
+        """(EedfParams, EEDF-convolved rates) of a finished job submitted with
+        two-term inputs (lgpu_server_job_eedf)."""
+        out = EedfParams()
+        rates = np.zeros(n_procs)
+        rc = self.lib.lgpu_server_job_eedf(self.h, LL(job_id), ctypes.byref(out), dptr(rates), int(n_procs))
+        if rc != LGPU_OK:
+            raise LokiGpuError(rc, "lgpu_server_job_eedf failed")
+        return out, rates
 
     def submit_request(self, req: "Request") -> list:
         """lgpu_server_submit_request: every job of a parsed request."""
@@ -637,6 +663,21 @@ class Request:
         if rc != LGPU_OK:
             raise LokiGpuError(rc, "lgpu_request_job failed")
         return j
+
+    def twoterm(self, k=0):
+        """The collision behind each process of job k, as the EEDF
+        post-processing reads it: dicts of twoterm_array's fields."""
+        j = self.job(k)
+        out = []
+        for p in range(j.n_procs):
+            t = j.twoterm[p]
+            out.append(dict(kind=t.kind, ion=t.ion, density=t.density, threshold=t.threshold,
+                            mass_ratio=t.mass_ratio, stat_ratio=t.stat_ratio,
+                            int_e=np.ctypeslib.as_array(t.int_e, (t.n_int,)).copy(),
+                            int_v=np.ctypeslib.as_array(t.int_v, (t.n_int,)).copy(),
+                            mom_e=np.ctypeslib.as_array(t.mom_e, (t.n_mom,)).copy(),
+                            mom_v=np.ctypeslib.as_array(t.mom_v, (t.n_mom,)).copy()))
+        return out
 
     def processes(self, k=0):
         """The flattened processes of job k as numpy arrays (the field names

@@ -393,3 +393,51 @@ def test_server_admits_requests_from_input_files(tmp_path):
         assert x.state == capi.JOB_DONE and y.state == capi.JOB_DONE
         assert x.result.real_collisions == y.result.real_collisions
         assert x.result.mean_energy == y.result.mean_energy
+
+
+def test_server_postprocesses_the_eedf_of_a_request(tmp_path):
+    """A request's jobs carry the collisions behind their processes
+    (lgpu_job.twoterm), and the server runs the end-of-job EEDF
+    post-processing on the device as each job finishes
+    (lgpu_server_job_eedf): the same values as the same job's context
+    post-processing its own EEDF after a solve alone (without ionization and
+    attachment the two runs' EEDF histograms hold the same counts). A job
+    submitted without two-term inputs has none."""
+    import os
+
+    from lokigpu import capi, synth
+
+    gas = synth.atomic_gas()
+    synth.write_case(str(tmp_path), [gas], pressure_pa=N_GAS * 1.38064852e-23 * 300.0, red_field=[80.0],
+                     n_electrons=20000, kte_init_ev=1.0,
+                     extra_numerics={"nIntegrationPoints": "500", "nInterpPoints": "2000",
+                                     "maxCollisionsBeforeSteadyState": "100", "gpuSeed": "77"})
+    inp = os.path.join(str(tmp_path), "Input")
+    req = capi.Request(open(os.path.join(inp, "case.in")).read(),
+                       {"A1_LXCat.txt": open(os.path.join(inp, "A1_LXCat.txt")).read()})
+    srv = capi.Server(0, 4)
+    jid = srv.submit_request(req)[0]
+    ps = synth.flatten([gas])
+    j = req.job(0)
+    plain = srv.submit(j.config, ps, ps.gas_first, ps.gas_last, ps.gas_fraction, j.conditions.gas_density, 300.0, 80.0)
+    st = srv.wait(jid, 300.0)
+    assert st.state == capi.JOB_DONE
+    params, rates = srv.job_eedf(jid, ps.n)
+    assert srv.wait(plain, 300.0).state == capi.JOB_DONE
+    with pytest.raises(capi.LokiGpuError):
+        srv.job_eedf(plain, ps.n)
+    srv.stop()
+    cfg = j.config
+    ctx = capi.Context(cfg)
+    ctx.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+    c = j.conditions
+    ctx.set_conditions(c.gas_density, c.gas_temperature, c.reduced_field_td, c.field_angle_deg,
+                       c.excitation_freq_hz, c.reduced_mag_field_hx)
+    ctx.set_twoterm(req.twoterm(0))
+    r = ctx.solve()
+    assert r.real_collisions == st.result.real_collisions
+    p2, r2 = ctx.eedf_postprocess()
+    ctx.close()
+    np.testing.assert_allclose(rates, r2, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(params.values(), p2.values(), rtol=1e-13, atol=1e-300)
+    assert params.tot_ion_rate == 0.0 and params.mom_transf_freq > 0 and params.charac_energy > 0

@@ -5,7 +5,9 @@ reference's own flattening of the same files (the golden vectors from the
 reference built from source): the same processes, types, samplers,
 thresholds, masses, superelastic weights, relative densities and raw cross
 sections (1e-15: the reference reads numbers through its expression parser,
-whose text round trip can move the last bit, Parse.C:727-745). Also the
+whose text round trip can move the last bit, Parse.C:727-745), and the
+collision tables its end-of-job routines read (momentum transfer from the
+angular laws). Also the
 working-condition vector that makes one job per entry, expressions,
 boltzmannPopulation@T families, the errors for inputs this front end does
 not read, and the parse rate a server needs."""
@@ -142,3 +144,39 @@ def test_request_parse_rate(tmp_path):
     per = (time.perf_counter() - t0) / n
     print(f"request parse: {1e3 * per:.3f} ms per request ({1.0 / per:.0f} requests/s)")
     assert per < 0.05
+
+
+@pytest.mark.parametrize("name", ["atomic_dc100", "n2_dc200", "mix_dc300", "screen_dc100"])
+def test_request_twoterm_inputs_match_the_reference(name, tmp_path):
+    """The collision behind each process as the reference's end-of-job
+    routines read it (tests/golden/eedf_post_*.npz, from the reference built
+    from source): the raw integral cross section (the LXCat table, an elastic
+    one starting at zero energy, Collision.C:40-43), the momentum-transfer one
+    the angular law gives (the trapezoidal integration of Collision.C:127-199
+    over angleNumber angles, for the Born-dipole, Surendra, screened-Coulomb
+    and forward laws of these mixtures), target and product densities,
+    thresholds, mass and statistical-weight ratios."""
+    import make_eedf_post
+    from lokigpu import capi
+
+    case, over, numerics = make_eedf_post.CASES[name]
+    make_golden.write_inputs(case, str(tmp_path), n_electrons=2e4, extra=numerics, **over)
+    req = capi.Request(*_texts(str(tmp_path)))
+    got = req.twoterm(0)
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"eedf_post_{name}.npz"))
+    s = d["twoterm_scalars"]
+    oi = np.concatenate([[0], np.cumsum(d["int_len"])])
+    om = np.concatenate([[0], np.cumsum(d["mom_len"])])
+    assert len(got) == len(s)
+    for p, t in enumerate(got):
+        assert (t["kind"], t["ion"]) == (int(s[p, 0]), int(s[p, 5])), p
+        np.testing.assert_allclose([t["density"], t["threshold"], t["mass_ratio"]], s[p, 1:4], rtol=1e-14, atol=0)
+        if s[p, 4] != 0:
+            assert abs(t["stat_ratio"] / s[p, 4] - 1.0) < 1e-15, p
+        np.testing.assert_allclose(t["int_e"], d["int_e"][oi[p]:oi[p + 1]], rtol=1e-15, atol=0)
+        np.testing.assert_allclose(t["int_v"], d["int_v"][oi[p]:oi[p + 1]], rtol=1e-15, atol=0)
+        np.testing.assert_allclose(t["mom_e"], d["mom_e"][om[p]:om[p + 1]], rtol=1e-15, atol=0)
+        # 1 - (angular integral): for strongly forward laws at high energy the
+        # integral nears 1, so the last-bit differences of the cos x sin weights
+        # (the reference's come from its vector library) grow to ~1e-11
+        np.testing.assert_allclose(t["mom_v"], d["mom_v"][om[p]:om[p + 1]], rtol=1e-10, atol=1e-300)
