@@ -388,6 +388,12 @@ typedef struct lgpu_eedf_params {
  * the superelastic one for a superelastic copy. */
 int lgpu_eedf_postprocess(lgpu_ctx* ctx, const double* eedf, int n_cells, double max_energy, lgpu_eedf_params* out,
                           double* rate, int n);
+/* The EEDF-convolved rate coefficients alone, of n_eedf EEDFs given as rows
+ * of n_cells (rate[n_eedf * n]); eedf NULL: the context's per-phase EEDFs of
+ * an AC run (n_eedf = config.n_phases; BoltzmannMC.C:2276-2330, each phase's
+ * EEDF normalised as BoltzmannMC.C:1736-1740). */
+int lgpu_eedf_rates(lgpu_ctx* ctx, const double* eedf, int n_eedf, int n_cells, double max_energy, double* rate,
+                    int n);
 
 /* ---- serving: continuous batching of swarm jobs ----
  *

@@ -125,6 +125,12 @@ int lgpu_eedf_postprocess(lgpu_ctx* ctx, const double* eedf, int n_cells, double
   return ctx->e->eedf_postprocess(eedf, n_cells, max_energy, out, rate, n);
 }
 
+int lgpu_eedf_rates(lgpu_ctx* ctx, const double* eedf, int n_eedf, int n_cells, double max_energy, double* rate,
+                    int n) {
+  CTX_CHECK(ctx);
+  return ctx->e->eedf_rates(eedf, n_eedf, n_cells, max_energy, rate, n);
+}
+
 int lgpu_get_periodic(lgpu_ctx* ctx, double* n, double* me, double* fv, double* bv, double* fd, double* bd) {
   CTX_CHECK(ctx);
   return ctx->e->periodic(n, me, fv, bv, fd, bd);

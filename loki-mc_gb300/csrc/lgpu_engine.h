@@ -1507,16 +1507,36 @@ class Engine {
   // the reference's end-of-job routines that read the EEDF
   // (Collision.C:355-397, BoltzmannMC.C:2186-2266), on the device
   int eedf_postprocess(const double* eedf, int nc, double max_e, lgpu_eedf_params* out, double* rate, int n) {
-    if (!has_twoterm()) return fail(LGPU_ERR_STATE, "no two-term inputs: call lgpu_set_twoterm first");
-    if (rate && n != P_) return fail(LGPU_ERR_BAD_ARG, "expected %d processes", P_);
     if (!eedf) {
       nc = cfg_.n_energy_cells;
       max_e = max_eedf_;
       if (!(max_e > 0)) return fail(LGPU_ERR_STATE, "no EEDF yet: the distributions start at the steady state");
-    } else if (nc < 2 || !(max_e > 0)) {
-      return fail(LGPU_ERR_BAD_ARG, "an EEDF needs at least 2 cells and a positive maximum energy");
     }
-    const size_t need = (size_t)nc + 5 * ((size_t)nc + 1) + (size_t)P_ + 16;
+    return run_post(eedf, eedf ? nullptr : d_eedf_, 1, nc, max_e, false, out, rate, n);
+  }
+
+  // the rate coefficients of several EEDFs, or (eedf null) of the per-phase
+  // EEDFs of an AC run (BoltzmannMC.C:2276-2330, normalised as :1736-1740)
+  int eedf_rates(const double* eedf, int n_eedf, int nc, double max_e, double* rate, int n) {
+    if (!eedf) {
+      if (omega_ == 0) return fail(LGPU_ERR_STATE, "per-phase EEDFs exist only under an AC field");
+      nc = cfg_.n_energy_cells;
+      max_e = max_eedf_;
+      n_eedf = std::max(cfg_.n_phases, 1);
+      if (!(max_e > 0)) return fail(LGPU_ERR_STATE, "no EEDF yet: the distributions start at the steady state");
+    }
+    if (n_eedf < 1) return fail(LGPU_ERR_BAD_ARG, "no EEDF given");
+    return run_post(eedf, eedf ? nullptr : d_eedf_per_, n_eedf, nc, max_e, true, nullptr, rate, n);
+  }
+
+  int run_post(const double* eedf, const double* eeh, int n_eedf, int nc, double max_e, bool rates_only,
+               lgpu_eedf_params* out, double* rate, int n) {
+    if (!has_twoterm()) return fail(LGPU_ERR_STATE, "no two-term inputs: call lgpu_set_twoterm first");
+    if (rate && n != P_) return fail(LGPU_ERR_BAD_ARG, "expected %d processes", P_);
+    if (nc < 2 || !(max_e > 0))
+      return fail(LGPU_ERR_BAD_ARG, "an EEDF needs at least 2 cells and a positive maximum energy");
+    const size_t nn = (size_t)nc + 1;
+    const size_t need = (size_t)n_eedf * ((size_t)nc + 5 * nn + (size_t)P_) + 16;
     if (need > post_cap_) {
       if (d_post_) cudaFree(d_post_);
       d_post_ = nullptr;
@@ -1527,18 +1547,20 @@ class Engine {
     EedfPostArgs a{};
     a.nc = nc;
     a.P = P_;
+    a.n_eedf = n_eedf;
+    a.rates_only = rates_only ? 1 : 0;
     a.max_energy = max_e;
     a.gas_density = Ngas_;
     a.omega = omega_;
     a.omega_c = omega_c_;
-    a.eeh = d_eedf_;
+    a.eeh = eeh ? eeh : d_post_;  // unread when the EEDFs are given
     if (eedf) {
-      LGPU_CU(cudaMemcpyAsync(d_post_, eedf, (size_t)nc * sizeof(double), cudaMemcpyHostToDevice, stream_));
+      LGPU_CU(cudaMemcpyAsync(d_post_, eedf, (size_t)n_eedf * nc * sizeof(double), cudaMemcpyHostToDevice, stream_));
       a.eedf_in = d_post_;
     }
-    a.scratch = d_post_ + nc;
-    a.rates = a.scratch + 5 * ((size_t)nc + 1);
-    a.params = a.rates + P_;
+    a.scratch = d_post_ + (size_t)n_eedf * nc;
+    a.rates = a.scratch + (size_t)n_eedf * 5 * nn;
+    a.params = a.rates + (size_t)n_eedf * P_;
     a.kind = d_tt_i_;
     a.ion = d_tt_i_ + P_;
     a.int_off = d_tt_i_ + 2 * P_;
@@ -1556,17 +1578,18 @@ class Engine {
     launch_eedf_post(a, stream_);
     ++launches_;
     LGPU_CU(cudaGetLastError());
-    std::vector<double> res((size_t)P_ + 16);
+    std::vector<double> res((size_t)n_eedf * P_ + 16);
     LGPU_CU(cudaMemcpyAsync(res.data(), a.rates, res.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     LGPU_TRY(sync("eedf post-processing"));
-    if (rate) std::copy(res.begin(), res.begin() + P_, rate);
+    if (rate) std::copy(res.begin(), res.begin() + (size_t)n_eedf * P_, rate);
     if (out) {
-      const double* v = res.data() + P_;
+      const double* v = res.data() + (size_t)n_eedf * P_;
       *out = lgpu_eedf_params{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12],
                               v[13], v[14], v[15]};
     }
     return LGPU_OK;
   }
+
   // ------------------------------------------------------------ replay
   double* d_rp_in_ = nullptr;
   double* d_rp_out_ = nullptr;

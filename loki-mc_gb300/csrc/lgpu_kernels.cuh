@@ -275,13 +275,14 @@ cudaError_t prepare_advance_stash();
 int launch_batch_post(const BatchArgs& b, int sm_count, int max_slots, unsigned parts, cudaStream_t s);
 
 // End-of-job EEDF post-processing in FP64 (lgpu_post.cu): the EEDF-convolved
-// rate coefficient of every MC process (Collision.C:355-397) and the two-term
-// swarm parameters (BoltzmannMC.C:2186-2266), one block.
+// rate coefficient of every MC process (Collision.C:355-397) for each of
+// n_eedf EEDFs (one block each), and the two-term swarm parameters
+// (BoltzmannMC.C:2186-2266) of the first unless rates_only.
 struct EedfPostArgs {
-  int nc, P;
+  int nc, P, n_eedf, rates_only;
   double max_energy, gas_density, omega, omega_c;
-  const double* eedf_in;   // normalised EEDF [nc], or null: normalise eeh
-  const double* eeh;       // histogram sums [nc]
+  const double* eedf_in;   // normalised EEDFs [n_eedf][nc], or null: normalise eeh
+  const double* eeh;       // histogram sums [n_eedf][nc]
   const int* kind;         // per process: 0 elastic, 1 inelastic, 2 superelastic copy
   const int* ion;          // 1 ionization, 2 attachment
   const double* dens;      // target (product) relative density
@@ -296,8 +297,8 @@ struct EedfPostArgs {
   const double* raw_iv;
   const double* raw_me;
   const double* raw_mv;
-  double* scratch;         // 5 x (nc + 1)
-  double* rates;           // [P]
+  double* scratch;         // [n_eedf][5 x (nc + 1)]
+  double* rates;           // [n_eedf][P]
   double* params;          // [16], lgpu_eedf_params order
 };
 void launch_eedf_post(const EedfPostArgs& a, cudaStream_t s);

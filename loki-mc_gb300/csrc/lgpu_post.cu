@@ -65,9 +65,16 @@ __device__ double conv_sum(const PostGrid& g, const double* sig, const double* e
   return block_sum(s, red);
 }
 
+// One block per EEDF (row blockIdx.x of eedf_in or eeh); the two-term swarm
+// parameters from row 0 unless rates_only.
 __global__ void __launch_bounds__(kPostThreads) k_eedf_post(EedfPostArgs a) {
   __shared__ double red[kPostThreads / 32];
   const int nc = a.nc, nn = nc + 1;
+  const int row = blockIdx.x;
+  if (a.eedf_in) a.eedf_in += (size_t)row * nc;
+  a.eeh += (size_t)row * nc;
+  a.scratch += (size_t)row * 5 * nn;
+  a.rates += (size_t)row * a.P;
   PostGrid g;
   g.nc = nc;
   g.max = a.max_energy;
@@ -157,6 +164,7 @@ __global__ void __launch_bounds__(kPostThreads) k_eedf_post(EedfPostArgs a) {
     if (a.ion[p] == 2) k_att += dens * r;
     __syncthreads();
   }
+  if (a.rates_only) return;
   // two-term swarm parameters (BoltzmannMC.C:2220-2266)
   const double N = a.gas_density, w = a.omega, wc = a.omega_c;
   const double growth = k_ion - k_att;
@@ -227,6 +235,8 @@ __global__ void __launch_bounds__(kPostThreads) k_eedf_post(EedfPostArgs a) {
 
 }  // namespace
 
-void launch_eedf_post(const EedfPostArgs& a, cudaStream_t s) { k_eedf_post<<<1, kPostThreads, 0, s>>>(a); }
+void launch_eedf_post(const EedfPostArgs& a, cudaStream_t s) {
+  k_eedf_post<<<a.n_eedf, kPostThreads, 0, s>>>(a);
+}
 
 }  // namespace lgpu

@@ -398,56 +398,73 @@ struct lgpu_request {
 
 namespace {
 
-// Angular distribution I(e, theta) of a scattering law, normalised so that
-// 2 pi Int_0^pi I sin(theta) dtheta = 1 (AngularDistributionFunctions.h:32-110):
-// Born dipole (Vialetto et al. 2021, eq. 23), Surendra (Vahedi and Surendra
-// 1995, eq. 7), screened Coulomb (Hagelaar et al. 2000, eqs. 21-23); the
-// isotropic law and the momentum-conserving ionization law are 1/(4 pi).
-double angular_distribution(int law, const std::vector<double>& par, double thr, double e, double th) {
-  const double iso = 1.0 / (4.0 * M_PI);
-  switch (law) {
-    case 2: {  // Born dipole
-      const double ea = e - thr;
-      if (ea <= 0) return iso;
-      const double q2 = ea + e - 2.0 * std::sqrt(e * ea) * std::cos(th);
-      const double se = std::sqrt(e), sa = std::sqrt(ea);
-      return 1.0 / (4.0 * M_PI) * se * sa / q2 / std::log((sa + se) / std::sqrt(thr));
-    }
-    case 3: {  // Surendra
-      if (e == 0) return iso;
-      return e / (4.0 * M_PI * (1.0 + e * std::pow(std::sin(th / 2.0), 2)) * std::log(1.0 + e));
-    }
-    case 4: {  // screened Coulomb: the incident energy (p0 = 0) or the energy after the loss
-      const double eps = (par.size() > 0 && par[0] != 0) ? e - thr : e;
-      if (eps <= 0) return iso;
-      const double sp = (par.size() > 1 ? par[1] : 0.0) / eps;
-      return (sp * (sp + 1.0)) / M_PI / std::pow(2.0 * sp + 1.0 - std::cos(th), 2);
-    }
-    default:
-      return iso;
-  }
-}
-
 // The momentum-transfer cross section a scattering law gives an integral one
 // (Collision.C:127-199): sigma_m = sigma (1 - 2 pi Int_0^pi I cos sin dtheta),
 // the integral by the trapezoidal rule over n_ang angles in [0, pi] laid out
 // as Eigen's LinSpaced lays them; isotropic: sigma_m = sigma; forward: 0.
+// I(e, theta) is the law's angular distribution, normalised so that
+// 2 pi Int_0^pi I sin(theta) dtheta = 1 (AngularDistributionFunctions.h:32-110):
+// Born dipole (Vialetto et al. 2021, eq. 23), Surendra (Vahedi and Surendra
+// 1995, eq. 7), screened Coulomb (Hagelaar et al. 2000, eqs. 21-23); the
+// momentum-conserving ionization law is 1/(4 pi). The factors that depend on
+// the angle alone or on the energy alone are computed once; every term keeps
+// the order of operations of the distributions, so it rounds the same.
 std::vector<double> momentum_transfer(int law, const std::vector<double>& par, double thr, int n_ang,
                                       const std::vector<double>& e, const std::vector<double>& v) {
   if (law == 0) return v;
   if (law == 1) return std::vector<double>(v.size(), 0.0);
   if (n_ang < 2) throw Error("anisotropicScattering.angleNumber must be at least 2");
+  const double iso = 1.0 / (4.0 * M_PI);
   const double step = M_PI / (n_ang - 1.0);
-  std::vector<double> ang(n_ang), aux(n_ang);
+  std::vector<double> ang(n_ang), aux(n_ang), cs(n_ang), sh2(n_ang);
   for (int j = 0; j < n_ang; ++j) {
     ang[j] = j == n_ang - 1 ? M_PI : (double)j * step;
     aux[j] = std::cos(ang[j]) * std::sin(ang[j]);
+    cs[j] = std::cos(ang[j]);
+    const double sh = std::sin(ang[j] / 2.0);
+    sh2[j] = sh * sh;  // pow(x, 2) rounds as x * x
   }
+  std::vector<double> dist(n_ang);
   std::vector<double> m(v.size());
   for (size_t i = 0; i < e.size(); ++i) {
-    double integ = aux[0] * angular_distribution(law, par, thr, e[i], ang[0]);
-    for (int j = 1; j < n_ang - 1; ++j) integ += 2.0 * aux[j] * angular_distribution(law, par, thr, e[i], ang[j]);
-    integ += aux[n_ang - 1] * angular_distribution(law, par, thr, e[i], ang[n_ang - 1]);
+    const double en = e[i];
+    if (law == 2) {  // Born dipole
+      const double ea = en - thr;
+      if (ea <= 0) {
+        std::fill(dist.begin(), dist.end(), iso);
+      } else {
+        const double r = 2.0 * std::sqrt(en * ea), se = std::sqrt(en), sa = std::sqrt(ea);
+        const double lg = std::log((sa + se) / std::sqrt(thr));
+        for (int j = 0; j < n_ang; ++j) {
+          const double q2 = ea + en - r * cs[j];
+          dist[j] = 1.0 / (4.0 * M_PI) * se * sa / q2 / lg;
+        }
+      }
+    } else if (law == 3) {  // Surendra
+      if (en == 0) {
+        std::fill(dist.begin(), dist.end(), iso);
+      } else {
+        const double lg = std::log(1.0 + en);
+        for (int j = 0; j < n_ang; ++j) dist[j] = en / (4.0 * M_PI * (1.0 + en * sh2[j]) * lg);
+      }
+    } else if (law == 4) {  // screened Coulomb: the incident energy (p0 = 0) or the energy after the loss
+      const double eps = (par.size() > 0 && par[0] != 0) ? en - thr : en;
+      if (eps <= 0) {
+        std::fill(dist.begin(), dist.end(), iso);
+      } else {
+        const double sp = (par.size() > 1 ? par[1] : 0.0) / eps;
+        const double num = (sp * (sp + 1.0)) / M_PI, b = 2.0 * sp + 1.0;
+        for (int j = 0; j < n_ang; ++j) {
+          const double d = b - cs[j];
+          dist[j] = num / (d * d);
+        }
+      }
+    } else {
+      std::fill(dist.begin(), dist.end(), iso);
+    }
+    double integ = aux[0] * dist[0];
+    for (int j = 1; j < n_ang - 1; ++j) integ += 2.0 * aux[j] * dist[j];
+    integ += aux[n_ang - 1] * dist[n_ang - 1];
     integ *= M_PI * step;
     m[i] = v[i] * (1.0 - integ);
   }

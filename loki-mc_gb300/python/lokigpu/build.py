@@ -20,8 +20,13 @@ BUILD = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libloki_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
-# per-file flags: the EEDF post-processing rounds every step as the reference does
-FILE_FLAGS = {"lgpu_post.cu": ["-fmad=false"]}
+# No multiply-add contraction in the device code: every kernel that inlines
+# the same device function (single-condition, batched in each launch shape,
+# replay) computes the same bits, and every step rounds as the reference's
+# (whose build contracts nothing); where a fused multiply-add is meant, the
+# source spells it (__fmaf_rn).
+FILE_FLAGS = {name: ["-fmad=false"] for name in ("lgpu_post.cu", "lgpu_kernels.cu", "lgpu_advance_batch.cu",
+                                                 "lgpu_advance_stash.cu", "lgpu_noalloc.cu")}
 
 
 def nvcc() -> str:

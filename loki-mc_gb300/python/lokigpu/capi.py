@@ -26,7 +26,7 @@ STATUS = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ENERGY_ABOVE_TABLE", 4: "TIMEOUT"
 EXPORTED = ("lgpu_config_default", "lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_stream",
             "lgpu_set_processes", "lgpu_set_conditions", "lgpu_init_ensemble", "lgpu_advance", "lgpu_solve",
             "lgpu_get_process_results", "lgpu_get_distributions", "lgpu_get_periodic", "lgpu_get_series",
-            "lgpu_get_timing", "lgpu_set_twoterm", "lgpu_eedf_postprocess",
+            "lgpu_get_timing", "lgpu_set_twoterm", "lgpu_eedf_postprocess", "lgpu_eedf_rates",
             "lgpu_build_tables", "lgpu_set_field_raw", "lgpu_replay_flights", "lgpu_replay_collisions",
             "lgpu_replay_collisions_coarse", "lgpu_replay_flights_noalloc",
             "lgpu_batch_create", "lgpu_batch_destroy", "lgpu_batch_last_error", "lgpu_batch_add", "lgpu_batch_run",
@@ -196,6 +196,7 @@ def load(path: str | None = None):
     lib.lgpu_get_distributions.argtypes = [ctypes.c_void_p] + [P_(D)] * 9
     lib.lgpu_set_twoterm.argtypes = [ctypes.c_void_p, P_(TwotermProcess), I]
     lib.lgpu_eedf_postprocess.argtypes = [ctypes.c_void_p, P_(D), I, D, P_(EedfParams), P_(D), I]
+    lib.lgpu_eedf_rates.argtypes = [ctypes.c_void_p, P_(D), I, I, D, P_(D), I]
     lib.lgpu_get_periodic.argtypes = [ctypes.c_void_p] + [P_(D)] * 6
     lib.lgpu_get_series.argtypes = [ctypes.c_void_p, I, P_(D), LL]
     lib.lgpu_get_series.restype = LL
@@ -387,6 +388,20 @@ class Context:
             self.check(self.lib.lgpu_eedf_postprocess(self.h, dptr(e), len(e), float(max_energy), ctypes.byref(out),
                                                       dptr(rate), self.P))
         return out, rate
+
+    def eedf_rates(self, eedf=None, max_energy=0.0):
+        """EEDF-convolved rate coefficients [n_eedf, P] of the rows of eedf,
+        or (None) of the context's per-phase EEDFs under AC."""
+        if eedf is None:
+            n = max(self.cfg.n_phases, 1)
+            rate = np.zeros((n, self.P))
+            self.check(self.lib.lgpu_eedf_rates(self.h, None, 0, 0, 0.0, dptr(rate), self.P))
+            return rate
+        e = np.ascontiguousarray(np.atleast_2d(eedf), dtype=np.float64)
+        rate = np.zeros((e.shape[0], self.P))
+        self.check(self.lib.lgpu_eedf_rates(self.h, dptr(e), e.shape[0], e.shape[1], float(max_energy), dptr(rate),
+                                            self.P))
+        return rate
 
     def distributions(self):
         c = self.cfg

@@ -367,6 +367,23 @@ void ref_get_eedf_rates(double* rate) {
     rate[i] = g_mc->isSuperElastic[i] ? c->supRateCoeff : c->ineRateCoeff;
   }
 }
+// the per-phase ones of an AC run (rateCoeffAll_periodic, BoltzmannMC.C:2276-2330),
+// [phase][process], superelastic copies their collision's supRate
+void ref_get_eedf_rates_periodic(double* rate) {
+  BoltzmannMC* m = g_mc;
+  const int P = m->nProcesses;
+  for (size_t ph = 0; ph < m->rateCoeffAll_periodic.size(); ++ph) {
+    const auto& row = m->rateCoeffAll_periodic[ph];
+    size_t k = 0;
+    for (int i = 0; i < P; ++i) {
+      if (m->isSuperElastic[i]) continue;
+      const auto& rc = row[k++];
+      rate[ph * P + i] = rc.ineRate;
+      if (i + 1 < P && m->isSuperElastic[i + 1]) rate[ph * P + i + 1] = rc.supRate;
+    }
+  }
+}
+int ref_n_phases_periodic() { return (int)g_mc->rateCoeffAll_periodic.size(); }
 double ref_swarm_param(const char* key) {
   auto it = g_mc->swarmParam.find(key);
   return it == g_mc->swarmParam.end() ? NAN : it->second;

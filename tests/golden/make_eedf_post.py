@@ -14,8 +14,8 @@ every MC process as the end-of-job routines read it (raw integral and
 momentum-transfer cross sections, target or product density, threshold, mass
 ratio, statistical-weight ratio), the field frequencies and gas density, and
 what the reference computed from them: the EEDF-convolved rate coefficient of
-every process, the two-term swarm parameters and the total
-momentum-transfer cross section on the grid nodes. The comparison is
+every process (under AC also from each phase's EEDF), the two-term swarm
+parameters and the total momentum-transfer cross section on the grid nodes. The comparison is
 deterministic: the device post-processes the same EEDF.
 """
 from __future__ import annotations
@@ -44,7 +44,7 @@ CASES = {
     "n2_dc200": ("n2", {"red_field": 200.0}, SHORT),
     "mix_dc300": ("mix", {"red_field": 300.0}, SHORT),
     "mix_b100": ("mix", {"red_field": 100.0, "red_mag": 1000.0, "angle": 90.0}, SHORT),
-    "mix_ac150": ("mix", {"red_field": 150.0, "freq": 3.22e22 * 1e-15 / (2 * np.pi)},
+    "mix_ac150": ("mix", {"red_field": 150.0, "freq": 3.22e22 * 1e-14 / (2 * np.pi)},
                   dict(SHORT, nIntegrationPhases="16")),
     "screen_dc100": ("screen", {}, SHORT),
 }
@@ -84,7 +84,17 @@ def run(name, seed):
     swarm = np.array([lib.ref_swarm_param(k.encode()) for k in TWOTERM_KEYS])
     mt = np.zeros(int(grid[4]) + 1)
     lib.ref_get_total_mt(mg.ptr(mt))
-    np.savez_compressed(out_path, case=name, max_eedf_energy=r[38], mean_energy=r[0], cells=cells, eedf=eedf,
+    extra = {}
+    n_ph = lib.ref_n_phases_periodic()
+    if n_ph > 0:
+        # AC: the per-phase EEDFs and the rate coefficients from each (BoltzmannMC.C:2276-2330)
+        z = [np.zeros(n_ph) for _ in range(2)] + [np.zeros(3 * n_ph)] * 2 + [np.zeros(9 * n_ph)] * 2
+        per = np.zeros(n_ph * nc)
+        lib.ref_get_periodic(*[mg.ptr(x) for x in z], mg.ptr(per))
+        rp = np.zeros(n_ph * P)
+        lib.ref_get_eedf_rates_periodic(mg.ptr(rp))
+        extra = dict(eedf_periodic=per.reshape(n_ph, nc), rates_periodic=rp.reshape(n_ph, P))
+    np.savez_compressed(out_path, case=name, max_eedf_energy=r[38], mean_energy=r[0], cells=cells, eedf=eedf, **extra,
                         grid=grid, twoterm_scalars=scal, int_len=ni, mom_len=nm, int_e=np.concatenate(ie),
                         int_v=np.concatenate(iv), mom_e=np.concatenate(me), mom_v=np.concatenate(mv), rates=rates,
                         swarm_keys=np.array(TWOTERM_KEYS), swarm=swarm, total_mt=mt,

@@ -52,3 +52,16 @@ def test_oracle_repeats_the_reference_postprocessing(path):
     assert list(d["swarm_keys"]) == list(E.KEYS)
     bad = [(k, a, b) for k, a, b in zip(E.KEYS, swarm, d["swarm"]) if abs(a - b) > 1e-12 * abs(b)]
     assert not bad, bad
+
+
+def test_oracle_repeats_the_reference_periodic_rates():
+    """Under AC the reference also convolves every phase's EEDF
+    (BoltzmannMC.C:2276-2330)."""
+    d = np.load(os.path.join(HERE, "golden", "eedf_post_mix_ac150.npz"))
+    g = d["grid"]
+    assert g[0] > 0 and d["eedf_periodic"].shape[0] == 16
+    procs = E.procs_from_fixture(d)
+    for ph, row in enumerate(d["eedf_periodic"]):
+        rates, _, _ = E.postprocess(row, float(d["max_eedf_energy"]), g[0], g[1], g[2], procs)
+        ref = d["rates_periodic"][ph]
+        assert np.all(np.abs(rates - ref) <= 1e-12 * np.abs(ref)), ph

@@ -6,13 +6,11 @@ arrive while others run. Neither may change a result:
 
 * without ionization and attachment nothing couples the electrons and every
   electron's random stream is fixed by (seed, electron, interval), so a
-  batched solve repeats the solve alone up to rounding: the flights and
-  energies spell out their rounding, but the compiler may contract some
-  multiply-adds of the collision kinematics differently in the batched and
-  single-condition kernels, so a trajectory can part at a rounding difference.
-  Under DC and crossed B the collision counts and swarm parameters agree to
-  1e-4 relative (with the present build they are the same bits), under AC to
-  1e-3;
+  batched solve repeats the solve alone: the device code is built without
+  multiply-add contraction, so the single-condition kernel and the batched
+  one in every launch shape compute the same bits. The tests allow 1e-4
+  relative under DC and crossed B and 1e-3 under AC (time-dependent fields
+  through the sines and cosines of the phase);
 * with ionization and attachment the secondaries draw from streams named by
   the warp that pushes them and population control claims slots with
   atomics, so the runs are statistically equivalent: mean energy and drift

@@ -105,3 +105,42 @@ def test_refusals():
     with pytest.raises(capi.LokiGpuError):
         ctx.eedf_postprocess(d["eedf"][:1], 10.0)  # at least two cells
     ctx.close()
+
+
+def test_device_repeats_the_reference_periodic_rates():
+    """The rate coefficients of every phase's EEDF of an AC run
+    (lgpu_eedf_rates, BoltzmannMC.C:2276-2330), given the reference's
+    per-phase EEDFs; then a context's own per-phase EEDFs after an AC solve
+    against the oracle on the per-phase EEDFs it reports."""
+    from lokigpu import capi
+    d = dict(np.load(os.path.join(HERE, "golden", "eedf_post_mix_ac150.npz")))
+    ctx = _context(d)
+    procs = E.procs_from_fixture(d)
+    ctx.set_twoterm(procs)
+    rates = ctx.eedf_rates(d["eedf_periodic"], float(d["max_eedf_energy"]))
+    ref = d["rates_periodic"]
+    assert rates.shape == ref.shape
+    assert np.all(np.abs(rates - ref) <= 1e-12 * np.abs(ref))
+    with pytest.raises(capi.LokiGpuError):
+        ctx.eedf_rates()  # no EEDF yet
+    ctx.close()
+    # a context's own per-phase EEDFs (16 phases, omega/N = 1e-14 m^3/s)
+    w = float(d["grid"][0])
+    cfg = capi.default_config(n_electrons=20000.0, n_interp=2000, seed=9, n_phases=16,
+                              init_temp_ratio=1.0 / (8.617333262e-5 * 300.0), req_integration_points=500.0,
+                              max_coll_before_ss=100.0)
+    arrays = {k[5:]: v for k, v in d.items() if k.startswith("proc_")}
+    arrays["energy_max_elastic"] = float(np.min(arrays["emax"][arrays["is_elastic"] == 1]))
+    ctx = capi.Context(cfg)
+    ctx.set_processes(gu.processes(arrays), arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
+    ctx.set_conditions(float(d["grid"][2]), 300.0, 150.0, 180.0, w / (2.0 * np.pi))
+    ctx.set_twoterm(procs)
+    r = ctx.solve()
+    own = ctx.eedf_rates()
+    per = ctx.distributions()["eedf_periodic"]
+    for ph in range(per.shape[0]):
+        if not np.isfinite(per[ph]).all() or per[ph].sum() == 0:
+            continue
+        o, _, _ = E.postprocess(per[ph], r.max_eedf_energy, w, 0.0, float(d["grid"][2]), procs)
+        assert np.all(np.abs(own[ph] - o) <= 1e-10 * np.abs(o) + 1e-300), ph
+    ctx.close()

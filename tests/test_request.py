@@ -131,7 +131,9 @@ def test_request_errors_name_what_is_not_read(tmp_path):
 
 def test_request_parse_rate(tmp_path):
     """A server parses a request of the two-gas mixture (65 processes, 200-point
-    grids, ~40 KB of text) in a few milliseconds, beside solves of seconds."""
+    grids, ~40 KB of text; the momentum-transfer integration of its angular
+    laws over 1000 angles included) in some 10 milliseconds, beside solves of
+    seconds."""
     from lokigpu import capi
 
     make_golden.write_inputs("mix", str(tmp_path))
