@@ -169,6 +169,39 @@ def test_every_schedule_repeats_the_solve_alone(schedule):
         assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < tol, spec
 
 
+@pytest.mark.parametrize("gte", [1, 2], ids=["thermal", "smart"])
+def test_stash_repeats_the_warp_turn_shape_with_thermal_targets(gte):
+    """With thermal targets every trial event goes through the collision turn
+    (BoltzmannMC.C:916-1031): in the stash shape every one is parked in the
+    stash. Without ionization and attachment the stash shape and the
+    warp-turn shape give the same collision counts and swarm parameters, bit
+    for bit (the device code rounds every step alike in every shape)."""
+    from lokigpu import capi
+    spec = ("atomic", 30000, 20.0, 180.0, 0.0, 0.0, 71)
+    out = []
+    for shape in (0, 4):
+        b = capi.Batch(0, 4)
+        b.set_schedule(shape, 20, 1)
+        case, n_e, red_field, angle, freq, red_mag, seed = spec
+        ps, arrays = _inputs(case)
+        cfg = _config(n_e, seed)
+        cfg.gas_temperature_effect = gte
+        ctx = capi.Context(cfg)
+        ctx.set_processes(ps, arrays["gas_first"], arrays["gas_last"], arrays["gas_frac"])
+        ctx.set_conditions(N_GAS, 300.0, red_field, angle, freq, red_mag)
+        b.add(ctx)
+        res, st, rep = b.run()
+        assert st[0] == 0 and rep.advance_stash == (64.0 if shape == 4 else 0.0)
+        counts = ctx.process_results()[0]
+        out.append((res[0], counts))
+        ctx.close()
+        b.close()
+    (ra, ca), (rb, cb) = out
+    assert np.array_equal(ca, cb)
+    assert ra.real_collisions == rb.real_collisions and ra.null_collisions == rb.null_collisions
+    assert ra.mean_energy == rb.mean_energy and ra.flux_v[2] == rb.flux_v[2]
+
+
 def test_schedule_rejects_unknown_points():
     from lokigpu import capi
     b = capi.Batch(0, 4)
