@@ -153,8 +153,8 @@ SCHEDULES = [(0, 20, 1), (1, 12, 0), (2, 28, 1), (3, 16, 1), (4, 20, 1), (4, 20,
 def test_every_schedule_repeats_the_solve_alone(schedule):
     """The schedule (launch shape, the stash, the collision-turn threshold,
     the staging of the null test) changes no electron's draws, decisions or
-    roundings: the batched solve in any schedule repeats the solve alone bit
-    for bit (DC, crossed B, AC)."""
+    roundings: the batched solve in any schedule makes the collisions of the
+    solve alone, bit for bit (DC, crossed B, AC)."""
     specs = [ATOMIC[1], ATOMIC[2], ATOMIC[3]]
     alone = _alone(specs)
     batched, rep = _batched(specs, schedule=schedule)
@@ -163,13 +163,15 @@ def test_every_schedule_repeats_the_solve_alone(schedule):
     assert rep.coarse_null_test == schedule[2]
     for spec, (ra, ca, _), (rb, cb, _) in zip(specs, alone, batched):
         # every kernel rounds every step alike: the same collisions, bit for
-        # bit (the moment sums to their FP64 summation order)
+        # bit; the swarm parameters to the grouping of the moment sums (the
+        # single-condition and the batched sample passes add their per-thread
+        # partial sums in different groups: ~1e-9)
         assert rb.sync_steps == ra.sync_steps, spec
         assert np.array_equal(ca, cb), spec
         assert rb.real_collisions == ra.real_collisions and rb.null_collisions == ra.null_collisions, spec
-        assert abs(rb.mean_energy / ra.mean_energy - 1.0) < 1e-12, spec
+        assert abs(rb.mean_energy / ra.mean_energy - 1.0) < 1e-8, spec
         k = _drift_axis(spec)
-        assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < 1e-12, spec
+        assert abs(rb.flux_v[k] / ra.flux_v[k] - 1.0) < 1e-8, spec
 
 
 @pytest.mark.parametrize("gte", [1, 2], ids=["thermal", "smart"])
