@@ -67,6 +67,9 @@ typedef struct lgpu_config {
   int advance_real_batch;           /* lanes of a warp with a pending real collision that start its
                                        collision turn (1..32); 0: 20 alone, tuned on line in a batch.
                                        Scheduling only: no result depends on it */
+  int advance_queue;                /* secondaries a warp keeps in its own queue before it spills them to
+                                       the global buffer the drain launch works off (1..32; 0: 32).
+                                       Scheduling only: a small value exercises the spill path */
 } lgpu_config;
 
 /* Fills the reference's defaults (BoltzmannMC.h:50-76). */

@@ -255,7 +255,7 @@ template <class Sh>
 __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const IntervalView& iv, Sh& sh, int wid,
                                                 int lane, unsigned lt_mask, Lane& L, LaneTally& tl, uint32_t& sec_id,
                                                 uint32_t warp_tag) {
-  int qn = min(sh.qn[wid], kLocalQ);
+  int qn = min(sh.qn[wid], a.local_q);
   const unsigned idle = __ballot_sync(0xffffffffu, !L.have);
   const int r = __popc(idle & lt_mask);
   const int take = min(__popc(idle), qn);
@@ -361,7 +361,7 @@ __device__ __forceinline__ void lane_real(const AdvanceArgs& a, Sh& sh, int wid,
       const float4 A = make_float4(L.p.x, L.p.y, L.p.z, L.t);
       const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
       const int k = atomicAdd(&sh.qn[wid], 1);
-      if (k < kLocalQ) {
+      if (k < a.local_q) {
         sh.qa[wid][k] = A;
         sh.qb[wid][k] = B;
       } else {
@@ -515,7 +515,7 @@ __device__ __forceinline__ void warp_loop(const AdvanceArgs& a, Sh& sh, const In
     // ---- refill lanes without an electron: the warp's own queued secondaries
     // first (the queue stays short, so it rarely spills), then the ensemble
     // chunk, then (drain) the spilled secondaries
-    int qn = min(sh.qn[wid], kLocalQ);
+    int qn = min(sh.qn[wid], a.local_q);
     if (qn > 0) qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, warp_tag);
     const unsigned need = __ballot_sync(0xffffffffu, !L.have);
     if (need && !exhausted) lane_take_chunk<Sh::kChunk>(a, iv, L, need, lane, lt_mask, n_el, next, end, exhausted);
@@ -645,7 +645,7 @@ __device__ __forceinline__ void warp_loop_stash(const AdvanceArgs& a, Sh& sh, fl
       nr -= take;
       need = __ballot_sync(0xffffffffu, !L.have);
     }
-    int qn = min(sh.qn[wid], kLocalQ);
+    int qn = min(sh.qn[wid], a.local_q);
     if (need && qn > 0) {
       qn = lane_take_queued(a, iv, sh, wid, lane, lt_mask, L, tl, sec_id, warp_tag);
       need = __ballot_sync(0xffffffffu, !L.have);

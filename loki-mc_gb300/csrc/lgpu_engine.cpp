@@ -34,6 +34,7 @@ void lgpu_config_default(lgpu_config* c) {
   c->max_seconds = 0;
   c->max_sync_steps = 0;
   c->advance_real_batch = 0;
+  c->advance_queue = 0;
 }
 
 #define CTX_CHECK(ctx)                          \

@@ -109,6 +109,7 @@ class Engine {
     if (cfg_.sync_oversampling < 1) return fail(LGPU_ERR_BAD_ARG, "synchronizationOverSampling must be >= 1");
     if (cfg_.advance_real_batch < 0 || cfg_.advance_real_batch > 32)
       return fail(LGPU_ERR_BAD_ARG, "advance_real_batch must be 0..32");
+    if (cfg_.advance_queue < 0 || cfg_.advance_queue > 32) return fail(LGPU_ERR_BAD_ARG, "advance_queue must be 0..32");
     LGPU_CU(cudaSetDevice(cfg_.device));
     LGPU_CU(prepare_kernels());
     LGPU_CU(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, cfg_.device));
@@ -610,6 +611,7 @@ class Engine {
     a.ctl = d_ctl_;
     a.real_batch = cfg_.advance_real_batch > 0 ? std::min(cfg_.advance_real_batch, 32) : kDefaultRealBatch;
     a.coarse = 1;
+    a.local_q = cfg_.advance_queue > 0 ? cfg_.advance_queue : 32;
     return a;
   }
 

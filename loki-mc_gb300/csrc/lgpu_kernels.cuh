@@ -78,6 +78,7 @@ struct AdvanceArgs {
   int queue_only;                  // 1: only drain the spilled secondaries (one warp)
   int real_batch;                  // pending real collisions that start a warp's collision turn (1..32)
   int coarse;                      // 1: null test against the block bounds first (t.nu_coarse)
+  int local_q;                     // secondaries a warp queues before it spills (1..kLocalQ)
 };
 constexpr int kDefaultRealBatch = 20;
 

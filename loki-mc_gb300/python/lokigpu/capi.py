@@ -53,7 +53,8 @@ class Config(ctypes.Structure):
                 ("errors_checked", I), ("req_err_mean_energy", D), ("req_err_flux_v", D), ("req_err_flux_d", D),
                 ("req_err_bulk_v", D), ("req_err_bulk_d", D), ("req_err_power", D), ("n_energy_cells", I),
                 ("n_cos_cells", I), ("n_radial_cells", I), ("n_axial_cells", I), ("n_phases", I), ("sync_x", D),
-                ("sync_oversampling", I), ("max_seconds", D), ("max_sync_steps", LL), ("advance_real_batch", I)]
+                ("sync_oversampling", I), ("max_seconds", D), ("max_sync_steps", LL), ("advance_real_batch", I),
+                ("advance_queue", I)]
 
 
 class Process(ctypes.Structure):

@@ -477,3 +477,54 @@ def test_server_postprocesses_the_eedf_of_a_request(tmp_path):
     np.testing.assert_allclose(rates, r2, rtol=1e-13, atol=0)
     np.testing.assert_allclose(params.values(), p2.values(), rtol=1e-13, atol=1e-300)
     assert params.tot_ion_rate == 0.0 and params.mom_transf_freq > 0 and params.charac_energy > 0
+
+
+def test_spilled_secondaries_in_every_shape():
+    """Secondaries a warp cannot keep in its own queue go to the global spill
+    buffer, which the drain launch pushes from their creation time
+    (BoltzmannMC.C:1195-1272) before population control (:1282-1408). With
+    the warp queue cut to one entry (lgpu_config.advance_queue) nearly every
+    secondary of an ionization-dominated gas at 1000 Td takes that path; the
+    warp-turn shape and the collision stash, both spilling, agree with the
+    solve alone with the full queue."""
+    from lokigpu import capi, synth
+
+    # weak elastic scattering and a large ionization cross section
+    gas = synth.atomic_gas()
+    e = synth.log_grid(100)
+    gas.collisions = [synth.Collision("Elastic", "A1(gnd)", "A1(gnd)", 0.0, e, np.full_like(e, 1e-21)),
+                      synth.Collision("Ionization", "A1(gnd)", "A1(+)", 15.0, e, np.where(e < 15.0, 0.0, 1e-19))]
+    gas.states = {"A1(gnd)": synth.State(1.0), "A1(+)": synth.State(0.0)}
+    ps = synth.flatten([gas])
+
+    def context(seed, queue):
+        cfg = _config(200000, seed)
+        cfg.req_integration_points = 500.0
+        cfg.advance_queue = queue
+        c = capi.Context(cfg)
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, 300.0, 1000.0)
+        return c
+
+    out = []
+    for shape in (0, 4):
+        b = capi.Batch(0, 2)
+        b.set_schedule(shape, 20, 1)
+        c = context(91, 1)
+        b.add(c)
+        res, st, rep = b.run()
+        assert st[0] == 0, c.last_error()
+        assert rep.spilled > 0.5 * rep.secondaries > 0, (shape, rep.secondaries, rep.spilled)
+        counts, rate, _, _ = c.process_results()
+        out.append((res[0], counts, rate))
+        c.close()
+        b.close()
+    c = context(92, 0)
+    r = c.solve()
+    counts, rate, _, _ = c.process_results()
+    out.append((r, counts, rate))
+    c.close()
+    spec = ("ion", 200000, 1000.0, 180.0, 0.0, 0.0, 91)
+    for rb in out[:2]:
+        fails = _statistically_equal(spec, out[2], rb)
+        assert not fails, fails
