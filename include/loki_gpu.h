@@ -337,7 +337,7 @@ int lgpu_batch_step(lgpu_batch* batch, int n, int* running, lgpu_batch_report* r
 /* The cudaStream_t all of the batch's work runs on. */
 void* lgpu_batch_stream(lgpu_batch* batch);
 /* Pins the advance's schedule instead of tuning it on line: launch shape
- * 0..4 (lgpu_batch_report's advance_threads .. advance_stash name it), the
+ * 0..5 (lgpu_batch_report's advance_threads .. advance_stash name it), the
  * collision-turn threshold (12, 16, 20, 24 or 28; a stash shape always takes
  * 32) and the coarse null test (0 or 1). shape -1 returns to on-line tuning.
  * The schedule changes no result: what an electron draws and decides does

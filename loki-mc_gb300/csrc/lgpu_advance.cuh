@@ -68,7 +68,9 @@ template <>
 struct AdvShape<3> { static constexpr int kThreads = 256, kBlocksPerSM = 4, kChunk = 256, kStash = 0; };
 template <>
 struct AdvShape<4> { static constexpr int kThreads = 256, kBlocksPerSM = 4, kChunk = 128, kStash = 64; };
-static_assert(kAdvShapes == 5, "one AdvShape per tuner candidate");
+template <>
+struct AdvShape<5> { static constexpr int kThreads = 512, kBlocksPerSM = 2, kChunk = 128, kStash = 64; };
+static_assert(kAdvShapes == 6, "one AdvShape per tuner candidate");
 static_assert(AdvShape<kFirstStashShape>::kStash > 0 && AdvShape<kFirstStashShape - 1>::kStash == 0,
               "stash shapes come last");
 

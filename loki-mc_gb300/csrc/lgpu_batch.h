@@ -63,8 +63,8 @@ class Batch {
   // On-line autotuner of the advance's scheduling, which changes no result
   // (what an electron draws and decides does not depend on it), so tuning
   // intervals are ordinary intervals. Two stages, each candidate taking
-  // kTuneRounds intervals and the least advance time per electron-interval
-  // (median) winning:
+  // kTuneRounds intervals (in turn, every other round in reverse order) and
+  // the least advance time per trial event (median) winning:
   //  0. the launch shape (kAdvShapes: threads per block x blocks per SM, i.e.
   //     the register budget, and the electrons a warp takes at a time);
   //  1. for members whose config leaves the threshold at 0, the
@@ -406,8 +406,14 @@ class Batch {
         tune_stage_ = 2;
       }
     }
-    const int shape = tune_stage_ == 0 ? tune_next_ % kAdvShapes : shape_;
-    const int k1 = tune_stage_ == 1 ? tune_next_ % stage1_count() : 0;
+    // candidates in turn, every other round in reverse order, so that a drift
+    // of the ensemble during tuning (heating from the start) favours none
+    auto turn = [&](int n) {
+      const int k = tune_next_ % n;
+      return (tune_next_ / n) & 1 ? n - 1 - k : k;
+    };
+    const int shape = tune_stage_ == 0 ? turn(kAdvShapes) : shape_;
+    const int k1 = tune_stage_ == 1 ? turn(stage1_count()) : 0;
     const int cand = tune_stage_ == 0 ? kTuneDefault : (tune_stage_ == 1 ? stage1_cand(k1) : tuned_);
     for (int s = 0; s < n; ++s) {
       Engine* e = member(go[s]).e;
@@ -453,8 +459,16 @@ class Batch {
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     adv_ms_ += ms;
     if (tune_stage_ < 2 && electrons > 0) {
+      // cost per trial event (real + null collisions of the interval): the
+      // events per electron-interval change as the ensemble relaxes
+      double events = 0;
+      for (int s = 0; s < n; ++s) {
+        const Member& m = member(go[s]);
+        events += (double)(h_gather_[s].real_count - m.e->h_sc_->real_count) +
+                  (double)(h_gather_[s].null_count - m.e->h_sc_->null_count);
+      }
       const int nc = tune_stage_ == 0 ? kAdvShapes : stage1_count();
-      tune_cost_[tune_stage_ == 0 ? shape : k1].push_back(ms / electrons);
+      tune_cost_[tune_stage_ == 0 ? shape : k1].push_back(ms / std::max(events, electrons));
       if (++tune_next_ >= nc * kTuneRounds) {
         const int pick = tune_pick(nc);
         tune_next_ = 0;

@@ -266,10 +266,10 @@ int launch_batch_hist(const BatchArgs& b, int sm_count, unsigned parts, cudaStre
 // blocks per SM, electrons a warp takes at a time, records of a warp's
 // collision stash); advance_shape() names them. Shapes from 4 on are stash
 // shapes (lgpu_advance_stash.cu).
-constexpr int kAdvShapes = 5;
+constexpr int kAdvShapes = 6;
 constexpr int kFirstStashShape = 4;
 int launch_batch_advance(const BatchArgs& b, int sm_count, unsigned parts, int shape, cudaStream_t s);
-int launch_batch_advance_stash(const BatchArgs& b, int sm_count, unsigned parts, cudaStream_t s);
+int launch_batch_advance_stash(const BatchArgs& b, int sm_count, unsigned parts, int shape, cudaStream_t s);
 void advance_shape(int shape, int* threads, int* blocks_per_sm, int* chunk, int* stash);
 // dynamic shared memory of the stash shapes' kernels (part of prepare_kernels)
 cudaError_t prepare_advance_stash();

@@ -146,7 +146,7 @@ def test_batch_repeats_alone_without_ionization():
 
 # pinned schedules: (launch shape, collision-turn threshold, coarse null test);
 # shape 4 parks pending collisions in a per-warp stash
-SCHEDULES = [(0, 20, 1), (1, 12, 0), (2, 28, 1), (3, 16, 1), (4, 20, 1), (4, 20, 0)]
+SCHEDULES = [(0, 20, 1), (1, 12, 0), (2, 28, 1), (3, 16, 1), (4, 20, 1), (4, 20, 0), (5, 20, 1)]
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES, ids=[f"shape{s}_t{t}_c{c}" for s, t, c in SCHEDULES])
@@ -158,8 +158,8 @@ def test_every_schedule_repeats_the_solve_alone(schedule):
     specs = [ATOMIC[1], ATOMIC[2], ATOMIC[3]]
     alone = _alone(specs)
     batched, rep = _batched(specs, schedule=schedule)
-    assert rep.advance_stash == (64.0 if schedule[0] == 4 else 0.0)
-    assert rep.real_batch == (32.0 if schedule[0] == 4 else schedule[1])
+    assert rep.advance_stash == (64.0 if schedule[0] >= 4 else 0.0)
+    assert rep.real_batch == (32.0 if schedule[0] >= 4 else schedule[1])
     assert rep.coarse_null_test == schedule[2]
     for spec, (ra, ca, _), (rb, cb, _) in zip(specs, alone, batched):
         # every kernel rounds every step alike: the same collisions, bit for
@@ -184,7 +184,7 @@ def test_stash_repeats_the_warp_turn_shape_with_thermal_targets(gte):
     from lokigpu import capi
     spec = ("atomic", 30000, 20.0, 180.0, 0.0, 0.0, 71)
     out = []
-    for shape in (0, 4):
+    for shape in (0, 4, 5):
         b = capi.Batch(0, 4)
         b.set_schedule(shape, 20, 1)
         case, n_e, red_field, angle, freq, red_mag, seed = spec
@@ -196,21 +196,22 @@ def test_stash_repeats_the_warp_turn_shape_with_thermal_targets(gte):
         ctx.set_conditions(N_GAS, 300.0, red_field, angle, freq, red_mag)
         b.add(ctx)
         res, st, rep = b.run()
-        assert st[0] == 0 and rep.advance_stash == (64.0 if shape == 4 else 0.0)
+        assert st[0] == 0 and rep.advance_stash == (64.0 if shape >= 4 else 0.0)
         counts = ctx.process_results()[0]
         out.append((res[0], counts))
         ctx.close()
         b.close()
-    (ra, ca), (rb, cb) = out
-    assert np.array_equal(ca, cb)
-    assert ra.real_collisions == rb.real_collisions and ra.null_collisions == rb.null_collisions
-    assert ra.mean_energy == rb.mean_energy and ra.flux_v[2] == rb.flux_v[2]
+    ra, ca = out[0]
+    for rb, cb in out[1:]:
+        assert np.array_equal(ca, cb)
+        assert ra.real_collisions == rb.real_collisions and ra.null_collisions == rb.null_collisions
+        assert ra.mean_energy == rb.mean_energy and ra.flux_v[2] == rb.flux_v[2]
 
 
 def test_schedule_rejects_unknown_points():
     from lokigpu import capi
     b = capi.Batch(0, 4)
-    for bad in [(5, 20, 1), (0, 13, 1), (0, 20, 2)]:
+    for bad in [(6, 20, 1), (0, 13, 1), (0, 20, 2)]:
         with pytest.raises(capi.LokiGpuError):
             b.set_schedule(*bad)
     b.set_schedule(4, 0, 1)  # a stash shape ignores the threshold
@@ -378,7 +379,7 @@ def test_autotuner_picks_a_launch_shape_and_keeps_it_per_mixture():
         return b, ctxs
 
     b, ctxs = batch_of(100)
-    _, rep = b.step(60)  # 5 shapes x 3 rounds, then 10 (stash: 2) candidates x 3 rounds
+    _, rep = b.step(60)  # 6 shapes x 3 rounds, then 10 (stash: 2) candidates x 3 rounds
     assert rep.advance_threads in (256.0, 512.0) and rep.advance_chunk in (64.0, 128.0, 256.0)
     assert rep.advance_stash in (0.0, 64.0)
     assert rep.real_batch in ((32.0,) if rep.advance_stash else (12.0, 16.0, 20.0, 24.0, 28.0))
@@ -507,7 +508,7 @@ def test_spilled_secondaries_in_every_shape():
         return c
 
     out = []
-    for shape in (0, 4):
+    for shape in (0, 4, 5):
         b = capi.Batch(0, 2)
         b.set_schedule(shape, 20, 1)
         c = context(91, 1)
@@ -525,6 +526,6 @@ def test_spilled_secondaries_in_every_shape():
     out.append((r, counts, rate))
     c.close()
     spec = ("ion", 200000, 1000.0, 180.0, 0.0, 0.0, 91)
-    for rb in out[:2]:
-        fails = _statistically_equal(spec, out[2], rb)
+    for rb in out[:3]:
+        fails = _statistically_equal(spec, out[3], rb)
         assert not fails, fails
