@@ -70,10 +70,10 @@ N_ELECTRONS = 1_000_000
 DRAM_BYTES_PER_ELECTRON_STEP = (130.522112e6 + 73.842176e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch, the
-# collision-stash shape the tuner picks), from one ncu capture of the sweep
-# (profiles/k_advance_batch_sweep64.md): 853.7 MB read + 559.4 MB written for
-# 1.98e7 electrons
-SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (853.741568e6 + 559.394048e6) / 19795598
+# collision-stash shape the tuner picks, 512 x 2), from one ncu capture of the
+# sweep (profiles/k_advance_batch_sweep64.md): 822.5 MB read + 553.4 MB written
+# for 1.98e7 electrons
+SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (822.501120e6 + 553.399040e6) / 19795598
 
 # sweep workload
 SWEEP_POINTS = 64
@@ -702,9 +702,9 @@ def ops_real(n_processes):
 
 
 # ncu counters of one batched DC advance launch over the sweep (1.98e7
-# electrons, collision-stash shape, profiles/k_advance_batch_sweep64.md): warp
+# electrons, collision-stash shape 512 x 2, profiles/k_advance_batch_sweep64.md): warp
 # instructions per electron-interval issued to the FMA, ALU and XU (SFU) pipes
-NCU_PIPE_PER_ELECTRON = {"fma": 183899572 / 19795598, "alu": 240628723 / 19795598, "xu": 12146751 / 19795598}
+NCU_PIPE_PER_ELECTRON = {"fma": 180209971 / 19795598, "alu": 247472650 / 19795598, "xu": 12035468 / 19795598}
 
 
 def issue_roofline(real, null, electron_steps, kernel_ms, n_processes, flight_ops, sm_mhz):
