@@ -215,8 +215,8 @@ __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, Sh& sh) 
 
 // an ensemble electron (left alone when its slot is attached)
 __device__ __forceinline__ void lane_take_electron(const AdvanceArgs& a, const IntervalView& iv, Lane& L, int idx) {
-  const float4 A = a.state[2 * idx];
-  const float4 B = a.state[2 * idx + 1];
+  float4 A, B;
+  load_record(a.state + 2 * idx, A, B);
   // the stream's seeding needs no state: it runs while the loads are in flight
   L.rng.init((uint32_t)idx, iv.interval, a.seed, a.salt);
   if (B.w == 0.0f) {
@@ -279,8 +279,8 @@ __device__ __forceinline__ int lane_take_queued(const AdvanceArgs& a, const Inte
 // synchronisation time.
 __device__ __forceinline__ void lane_finish(const AdvanceArgs& a, Lane& L, LaneTally& tl, bool dead) {
   if (L.slot >= 0) {
-    a.state[2 * L.slot] = make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s);
-    a.state[2 * L.slot + 1] = make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f);
+    store_record(a.state + 2 * L.slot, make_float4(L.p.x, L.p.y, L.p.z, dead ? -1.0f : L.s),
+                 make_float4(L.v.x, L.v.y, L.v.z, dead ? 1.0f : 0.0f));
   } else if (!dead) {
     const int k = append_slot(a.sec_count);
     if (k < a.sec_cap) {

@@ -16,6 +16,23 @@
 
 namespace lgpu {
 
+// ------------------------------------------------------------ records
+// An electron record is two float4 in one 32-byte sector: (x, y, z, s) and
+// (vx, vy, vz, flag). Every record buffer (ensemble, secondaries, spill) comes
+// from cudaMalloc, so record i starts at a multiple of 32 bytes and moves with
+// one 256-bit access (sm_100 and later) instead of two 128-bit ones: half the
+// load/store instructions and L1 wavefronts of the passes over the ensemble.
+__device__ __forceinline__ void load_record(const float4* rec, float4& A, float4& B) {
+  asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(A.x), "=f"(A.y), "=f"(A.z), "=f"(A.w), "=f"(B.x), "=f"(B.y), "=f"(B.z), "=f"(B.w)
+               : "l"(rec));
+}
+__device__ __forceinline__ void store_record(float4* rec, float4 A, float4 B) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(rec), "f"(A.x), "f"(A.y),
+               "f"(A.z), "f"(A.w), "f"(B.x), "f"(B.y), "f"(B.z), "f"(B.w)
+               : "memory");
+}
+
 // Constant.h:6-8
 constexpr double kQe = 1.6021766208e-19;
 constexpr double kMe = 9.10938356e-31;

@@ -120,6 +120,8 @@ class Engine {
     N_ = (int)cfg_.n_electrons;
     sec_cap_ = std::max(N_, 4096);
     LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
+    // the kernels move a record with one 32-byte access
+    if (reinterpret_cast<uintptr_t>(d_state_) % 32 != 0) return fail(LGPU_ERR_CUDA, "ensemble not 32-byte aligned");
     LGPU_TRY(dalloc(&d_alive_, (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_spill_, 2 * (size_t)sec_cap_));
     LGPU_TRY(dalloc(&d_sec_, 2 * (size_t)sec_cap_));

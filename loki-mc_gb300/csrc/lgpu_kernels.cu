@@ -252,14 +252,15 @@ __device__ __forceinline__ void sample_range(const SampleArgs& a, int begin, int
   for (; i + 3 * step < end; i += 4 * step) {
     float4 A[4], B[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      A[u] = a.state[2 * (i + u * step)];
-      B[u] = a.state[2 * (i + u * step) + 1];
-    }
+    for (int u = 0; u < 4; ++u) load_record(a.state + 2 * (i + u * step), A[u], B[u]);
 #pragma unroll
     for (int u = 0; u < 4; ++u) add(A[u], B[u]);
   }
-  for (; i < end; i += step) add(a.state[2 * i], a.state[2 * i + 1]);
+  for (; i < end; i += step) {
+    float4 A, B;
+    load_record(a.state + 2 * i, A, B);
+    add(A, B);
+  }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // FP32 tree reduction inside the warp (32 partials), FP64 across warps and blocks
 #pragma unroll
