@@ -355,10 +355,19 @@ __device__ __forceinline__ void hist_chunk_a(const HistArgs& a, int first, int l
       }
     }
   };
-  // four electrons' loads in flight per thread before their counts
+  // four electrons' loads in flight per thread before their counts; each
+  // warp bulk-prefetches into L2 its 128 records of the block's pass two
+  // rounds ahead
   const int st = blockDim.x;
+  auto prefetch_round = [&](int base) {
+    const int e0 = base + (int)(threadIdx.x >> 5) * 128;
+    if ((threadIdx.x & 31) == 0 && e0 < last) prefetch_l2(a.state + 2 * e0, (uint32_t)min(128, last - e0) * 32u);
+  };
+  prefetch_round(first);
+  prefetch_round(first + 4 * st);
   int i = first + threadIdx.x;
   for (; i + 3 * st < last; i += 4 * st) {
+    prefetch_round(i - (int)threadIdx.x + 8 * st);
     const float4 B0 = a.state[2 * i + 1], B1 = a.state[2 * (i + st) + 1];
     const float4 B2 = a.state[2 * (i + 2 * st) + 1], B3 = a.state[2 * (i + 3 * st) + 1];
     bin(B0);
