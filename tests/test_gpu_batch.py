@@ -66,18 +66,18 @@ def _context(spec):
     return ctx
 
 
-def _alone(specs):
+def _alone(specs, dists=False):
     out = []
     for spec in specs:
         ctx = _context(spec)
         r = ctx.solve()
         counts, rate, _, _ = ctx.process_results()
-        out.append((r, counts, rate))
+        out.append((r, counts, rate, ctx.distributions()) if dists else (r, counts, rate))
         ctx.close()
     return out
 
 
-def _batched(specs, max_slots=64, schedule=None):
+def _batched(specs, max_slots=64, schedule=None, dists=False):
     from lokigpu import capi
     b = capi.Batch(0, max_slots)
     if schedule is not None:
@@ -90,7 +90,7 @@ def _batched(specs, max_slots=64, schedule=None):
     for c, r, s in zip(ctxs, res, st):
         assert s == 0, c.last_error()
         counts, rate, _, _ = c.process_results()
-        out.append((r, counts, rate))
+        out.append((r, counts, rate, c.distributions()) if dists else (r, counts, rate))
         c.close()
     b.close()
     return out, rep
@@ -154,19 +154,26 @@ def test_every_schedule_repeats_the_solve_alone(schedule):
     """The schedule (launch shape, the stash, the collision-turn threshold,
     the staging of the null test) changes no electron's draws, decisions or
     roundings: the batched solve in any schedule makes the collisions of the
-    solve alone, bit for bit (DC, crossed B, AC)."""
+    solve alone, bit for bit (DC, crossed B, AC). The distributions too: the
+    batch counts each sample's EEDF, EADF (and EVDF) as the next interval's
+    advance loads the electrons, the solve alone with its own passes over
+    the ensemble, and the counts agree exactly."""
     specs = [ATOMIC[1], ATOMIC[2], ATOMIC[3]]
-    alone = _alone(specs)
-    batched, rep = _batched(specs, schedule=schedule)
+    alone = _alone(specs, dists=True)
+    batched, rep = _batched(specs, schedule=schedule, dists=True)
     assert rep.advance_stash == (64.0 if schedule[0] >= 4 else 0.0)
     assert rep.real_batch == (32.0 if schedule[0] >= 4 else schedule[1])
     assert rep.coarse_null_test == schedule[2]
-    for spec, (ra, ca, _), (rb, cb, _) in zip(specs, alone, batched):
+    for spec, (ra, ca, _, da), (rb, cb, _, db) in zip(specs, alone, batched):
         # every kernel rounds every step alike: the same collisions, bit for
         # bit; the swarm parameters to the grouping of the moment sums (the
         # single-condition and the batched sample passes add their per-thread
         # partial sums in different groups: ~1e-9)
         assert rb.sync_steps == ra.sync_steps, spec
+        assert ra.integration_points > 0, spec
+        for key in ("eedf", "eadf", "evdf", "eedf_periodic"):
+            if key in da:
+                assert np.array_equal(da[key], db[key], equal_nan=True), (spec, key)
         assert np.array_equal(ca, cb), spec
         assert rb.real_collisions == ra.real_collisions and rb.null_collisions == ra.null_collisions, spec
         assert abs(rb.mean_energy / ra.mean_energy - 1.0) < 1e-8, spec
