@@ -118,7 +118,7 @@ class Engine {
     LGPU_CU(cudaEventCreate(&ev1_));
     LGPU_CU(cudaEventCreateWithFlags(&tables_ev_, cudaEventDisableTiming));
     N_ = (int)cfg_.n_electrons;
-    sec_cap_ = std::max(N_, 4096);
+    sec_cap_ = initial_sec_cap(cfg_);
     LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
     // the kernels move a record with one 32-byte access
     if (reinterpret_cast<uintptr_t>(d_state_) % 32 != 0) return fail(LGPU_ERR_CUDA, "ensemble not 32-byte aligned");
@@ -748,6 +748,12 @@ class Engine {
     LGPU_TRY(check_device_errors());
     if (h_sc_->sec_count > sec_cap_)
       return fail(LGPU_ERR_OVERFLOW, "secondary buffer overflow (%d > %d)", h_sc_->sec_count, sec_cap_);
+    // the reference's secondary list grows without bound; here the buffers
+    // grow ahead of need: an interval that filled a quarter of them makes
+    // them at least twice as large (and four times its own count) before
+    // the next one, so a slowly heating, ionizing swarm never overflows
+    if (h_sc_->sec_count > sec_cap_ / 4)
+      LGPU_TRY(grow_secondaries(std::max(2 * (long long)sec_cap_, 4 * (long long)h_sc_->sec_count)));
     {
       float f;
       std::memcpy(&f, &h_sc_->max_energy_bits, 4);
@@ -756,6 +762,62 @@ class Engine {
     time_ += pending_dt_;
     ++interval_;
     ++n_sync_;
+    return LGPU_OK;
+  }
+
+  // Secondary records the buffers first hold: the ensemble's size, times one
+  // per four trial collisions an electron makes in an interval (up to 8x);
+  // they grow from there when a run needs more.
+  static int initial_sec_cap(const lgpu_config& c) {
+    const double base = std::max(c.n_electrons, 4096.0);
+    const double per = std::min(8.0, std::max(1.0, std::ceil(c.sync_x / 4.0)));
+    return (int)std::max(base, std::min(base * per, (double)(INT32_MAX / 2)));
+  }
+
+  // The secondary, spill and population-control buffers at `cap` records
+  // (between intervals: nothing in flight uses them, and population control
+  // leaves every claim bit clear). The new buffers are allocated before the
+  // old ones go, so a failed allocation keeps the old capacity (an interval
+  // that then overflows fails cleanly). Launch arguments built from the old
+  // pointers (the interval graphs, a batch slot) are rebuilt.
+  int grow_secondaries(long long cap) {
+    const long long max_cap = std::min<long long>(INT32_MAX / 2, (long long)INT32_MAX - N_ - 32);
+    if (sec_cap_ >= max_cap) return LGPU_OK;
+    const int new_cap = (int)std::min<long long>(cap, max_cap);
+    const size_t words = ((size_t)N_ + new_cap + 31) / 32;
+    int *alive = nullptr, *removed = nullptr, *pair_slot = nullptr, *pair_sec = nullptr;
+    float4 *spill = nullptr, *sec = nullptr;
+    unsigned int* claim = nullptr;
+    const bool ok = cudaMalloc((void**)&alive, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
+                    cudaMalloc((void**)&spill, 2 * (size_t)new_cap * sizeof(float4)) == cudaSuccess &&
+                    cudaMalloc((void**)&sec, 2 * (size_t)new_cap * sizeof(float4)) == cudaSuccess &&
+                    cudaMalloc((void**)&claim, words * sizeof(unsigned int)) == cudaSuccess &&
+                    cudaMalloc((void**)&removed, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
+                    cudaMalloc((void**)&pair_slot, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
+                    cudaMalloc((void**)&pair_sec, (size_t)new_cap * sizeof(int)) == cudaSuccess;
+    if (!ok) {
+      void* part[] = {alive, spill, sec, claim, removed, pair_slot, pair_sec};
+      for (void* q : part)
+        if (q) cudaFree(q);
+      cudaGetLastError();  // the failed allocation is not the next call's error
+      return LGPU_OK;
+    }
+    LGPU_TRY(sync("grow"));
+    void* old[] = {d_alive_, d_spill_, d_sec_, d_claim_, d_removed_, d_pair_slot_, d_pair_sec_};
+    for (void* q : old) cudaFree(q);
+    d_alive_ = alive;
+    d_spill_ = spill;
+    d_sec_ = sec;
+    d_claim_ = claim;
+    d_removed_ = removed;
+    d_pair_slot_ = pair_slot;
+    d_pair_sec_ = pair_sec;
+    sec_cap_ = new_cap;
+    claim_words_ = words;
+    LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
+    drop_graphs();
+    slot_built_ = -1;
+    ++sec_grown_;
     return LGPU_OK;
   }
 
@@ -1245,7 +1307,7 @@ class Engine {
   // (bytes): ensemble and secondary buffers, population-control scratch,
   // tables, tallies and histograms, as init() and set_processes() allocate.
   static double footprint_bytes(const lgpu_config& c, int P, long long raw_points) {
-    const double N = c.n_electrons, cap = std::max(N, 4096.0), M = c.n_interp;
+    const double N = c.n_electrons, cap = initial_sec_cap(c), M = c.n_interp;
     const double stride = (double)((P + 1) & ~1);
     double b = N * 2 * sizeof(float4);                      // state
     b += cap * (sizeof(int) * 4 + 4 * sizeof(float4));      // alive, removed, pair_slot/sec; spill, sec
@@ -1757,6 +1819,7 @@ class Engine {
   bool batch_ = false, hist_pending_ = false, evdf_fused_ = false;
   BatchSlot slot_{};                            // cached argument blocks of this solve's batch slot
   long long solve_serial_ = 0, slot_built_ = -1;
+  int sec_grown_ = 0;  // times the secondary buffers grew
   cudaStream_t own_stream_ = nullptr;
   HistArgs pending_hist_{};
   // timing

@@ -536,3 +536,51 @@ def test_spilled_secondaries_in_every_shape():
     for rb in out[:3]:
         fails = _statistically_equal(spec, out[3], rb)
         assert not fails, fails
+
+
+def test_secondary_buffers_grow_with_long_intervals():
+    """With synchronisation intervals of 6 trial collisions per electron
+    (synchronizationTimeXMaxCollisionFrequency = 6, BoltzmannMC.C:622) an
+    ionizing gas at 1000 Td makes about as many secondaries in one interval as
+    the ensemble holds electrons, where the reference's list of secondaries
+    just grows (BoltzmannMC.C:1195-1272). The buffers start at twice the ensemble
+    and grow ahead of need between intervals (each time an interval fills a
+    quarter of them): the solve alone and the batched solve both finish, and
+    agree."""
+    from lokigpu import capi, synth
+
+    gas = synth.atomic_gas()
+    e = synth.log_grid(120, 1e-3, 1e5)
+    gas.collisions = [synth.Collision("Elastic", "A1(gnd)", "A1(gnd)", 0.0, e, np.full_like(e, 1e-21)),
+                      synth.Collision("Ionization", "A1(gnd)", "A1(+)", 15.0, e, np.where(e < 15.0, 0.0, 1e-20))]
+    gas.states = {"A1(gnd)": synth.State(1.0), "A1(+)": synth.State(0.0)}
+    ps = synth.flatten([gas])
+    n = 20000
+
+    def context(seed):
+        cfg = _config(n, seed)
+        cfg.sync_x = 6.0
+        cfg.req_integration_points = 100.0
+        c = capi.Context(cfg)
+        c.set_processes(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+        c.set_conditions(N_GAS, 300.0, 1000.0)
+        return c
+
+    c = context(93)
+    ra = c.solve()
+    counts_a, rate_a, _, _ = c.process_results()
+    c.close()
+    b = capi.Batch(0, 2)
+    c = context(94)
+    b.add(c)
+    res, st, rep = b.run()
+    assert st[0] == 0, c.last_error()
+    # on average past a quarter of the first buffers (2 n records) per
+    # interval, so they grew at least once
+    assert rep.secondaries / rep.intervals > n / 2, (rep.secondaries, rep.intervals)
+    counts_b, rate_b, _, _ = c.process_results()
+    c.close()
+    b.close()
+    spec = ("ion", n, 1000.0, 180.0, 0.0, 0.0, 93)
+    fails = _statistically_equal(spec, (ra, counts_a, rate_a), (res[0], counts_b, rate_b))
+    assert not fails, fails
