@@ -99,6 +99,65 @@ class Engine {
     return cuda(cudaMalloc((void**)p, n * sizeof(T)), "cudaMalloc");
   }
 
+  // Buffers carved from one allocation, each on a 256-byte boundary: a
+  // context makes a handful of allocations instead of dozens (creating the
+  // 64 contexts of a sweep took 0.36 ms each in allocation calls alone).
+  struct Carve {
+    size_t bytes = 0;
+    template <class T>
+    size_t take(size_t n) {
+      const size_t o = (bytes + 255) & ~(size_t)255;
+      bytes = o + std::max<size_t>(n, 1) * sizeof(T);
+      return o;
+    }
+  };
+  template <class T>
+  static T* at(char* base, size_t off) {
+    return reinterpret_cast<T*>(base + off);
+  }
+
+  // The secondary, spill and population-control buffers for `cap` records
+  // in one allocation.
+  struct SecondarySet {
+    char* base = nullptr;
+    int *alive = nullptr, *removed = nullptr, *pair_slot = nullptr, *pair_sec = nullptr;
+    float4 *spill = nullptr, *sec = nullptr;
+    unsigned int* claim = nullptr;
+    size_t claim_words = 0;
+  };
+  cudaError_t alloc_secondaries(int cap, SecondarySet* o) const {
+    Carve cv;
+    const size_t words = ((size_t)N_ + cap + 31) / 32;
+    const size_t a = cv.take<int>(cap), sp = cv.take<float4>(2 * (size_t)cap), se = cv.take<float4>(2 * (size_t)cap);
+    const size_t cl = cv.take<unsigned int>(words), rm = cv.take<int>(cap), ps = cv.take<int>(cap);
+    const size_t pc = cv.take<int>(cap);
+    const cudaError_t e = cudaMalloc((void**)&o->base, cv.bytes);
+    if (e != cudaSuccess) {
+      o->base = nullptr;
+      return e;
+    }
+    o->alive = at<int>(o->base, a);
+    o->spill = at<float4>(o->base, sp);
+    o->sec = at<float4>(o->base, se);
+    o->claim = at<unsigned int>(o->base, cl);
+    o->removed = at<int>(o->base, rm);
+    o->pair_slot = at<int>(o->base, ps);
+    o->pair_sec = at<int>(o->base, pc);
+    o->claim_words = words;
+    return cudaSuccess;
+  }
+  void use_secondaries(const SecondarySet& q) {
+    d_secbuf_ = q.base;
+    d_alive_ = q.alive;
+    d_spill_ = q.spill;
+    d_sec_ = q.sec;
+    d_claim_ = q.claim;
+    d_removed_ = q.removed;
+    d_pair_slot_ = q.pair_slot;
+    d_pair_sec_ = q.pair_sec;
+    claim_words_ = q.claim_words;
+  }
+
   int init() {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LGPU_ERR_NO_DEVICE, "no CUDA device");
@@ -118,41 +177,54 @@ class Engine {
     LGPU_CU(cudaEventCreate(&ev1_));
     LGPU_CU(cudaEventCreateWithFlags(&tables_ev_, cudaEventDisableTiming));
     N_ = (int)cfg_.n_electrons;
-    sec_cap_ = initial_sec_cap(cfg_);
-    LGPU_TRY(dalloc(&d_state_, 2 * (size_t)N_));
-    // the kernels move a record with one 32-byte access
-    if (reinterpret_cast<uintptr_t>(d_state_) % 32 != 0) return fail(LGPU_ERR_CUDA, "ensemble not 32-byte aligned");
-    LGPU_TRY(dalloc(&d_alive_, (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_spill_, 2 * (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_sec_, 2 * (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_att_, (size_t)N_));
-    claim_words_ = ((size_t)N_ + sec_cap_ + 31) / 32;
-    LGPU_TRY(dalloc(&d_claim_, claim_words_));
-    LGPU_TRY(dalloc(&d_removed_, (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_pair_slot_, (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_pair_sec_, (size_t)sec_cap_));
-    LGPU_TRY(dalloc(&d_sc_, 1));
-    LGPU_CU(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
-    LGPU_TRY(dalloc(&d_ctl_, 1));
-    LGPU_CU(cudaMallocHost((void**)&h_ctl_, sizeof(IntervalCtl)));
-    std::memset(h_ctl_, 0, sizeof(IntervalCtl));
-    LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
-    LGPU_CU(cudaMemsetAsync(d_sc_, 0, sizeof(DevScalars), stream_));
     M_ = cfg_.n_interp;
-    LGPU_TRY(dalloc(&d_nu_pair_, (size_t)M_));
-    LGPU_TRY(dalloc(&d_nu_tot_, (size_t)M_));
-    LGPU_TRY(dalloc(&d_nu_max_, (size_t)M_));
-    LGPU_TRY(dalloc(&d_nu_coarse_, (size_t)kMaxCoarse));
+    sec_cap_ = initial_sec_cap(cfg_);
     coarse_shift_ = 0;
     while (((M_ + (1 << coarse_shift_) - 1) >> coarse_shift_) > kMaxCoarse) ++coarse_shift_;
     n_coarse_ = (M_ + (1 << coarse_shift_) - 1) >> coarse_shift_;
-    LGPU_CU(cudaMallocHost((void**)&h_nu_max_, (size_t)M_ * sizeof(double)));
-    std::memset(h_nu_max_, 0, (size_t)M_ * sizeof(double));
     const int nEC = cfg_.n_energy_cells;
-    LGPU_TRY(dalloc(&d_eedf_, (size_t)nEC));
-    LGPU_TRY(dalloc(&d_eedf_per_, (size_t)std::max(cfg_.n_phases, 1) * nEC));
-    LGPU_TRY(dalloc(&d_eadf_, (size_t)nEC * std::max(cfg_.n_cos_cells, 1)));
-    LGPU_TRY(dalloc(&d_evdf_, (size_t)std::max(cfg_.n_radial_cells, 1) * std::max(cfg_.n_axial_cells, 1)));
+    // the fixed device buffers: ensemble, scalars, tables, tallies, constants
+    Carve cv;
+    const size_t o_state = cv.take<float4>(2 * (size_t)N_), o_att = cv.take<int>(N_);
+    const size_t o_sc = cv.take<DevScalars>(1), o_ctl = cv.take<IntervalCtl>(1);
+    const size_t o_nup = cv.take<float2>(M_), o_nut = cv.take<double>(M_), o_num = cv.take<double>(M_);
+    const size_t o_nuc = cv.take<float>(kMaxCoarse);
+    const size_t o_eedf = cv.take<double>(nEC);
+    const size_t o_eper = cv.take<double>((size_t)std::max(cfg_.n_phases, 1) * nEC);
+    const size_t o_eadf = cv.take<double>((size_t)nEC * std::max(cfg_.n_cos_cells, 1));
+    const size_t o_evdf = cv.take<double>((size_t)std::max(cfg_.n_radial_cells, 1) * std::max(cfg_.n_axial_cells, 1));
+    const size_t o_procf = cv.take<ProcF>(kMaxProcesses), o_gasf = cv.take<GasF>(kMaxGases);
+    LGPU_TRY(dalloc(&d_core_, cv.bytes));
+    d_state_ = at<float4>(d_core_, o_state);
+    // the kernels move a record with one 32-byte access
+    if (reinterpret_cast<uintptr_t>(d_state_) % 32 != 0) return fail(LGPU_ERR_CUDA, "ensemble not 32-byte aligned");
+    d_att_ = at<int>(d_core_, o_att);
+    d_sc_ = at<DevScalars>(d_core_, o_sc);
+    d_ctl_ = at<IntervalCtl>(d_core_, o_ctl);
+    d_nu_pair_ = at<float2>(d_core_, o_nup);
+    d_nu_tot_ = at<double>(d_core_, o_nut);
+    d_nu_max_ = at<double>(d_core_, o_num);
+    d_nu_coarse_ = at<float>(d_core_, o_nuc);
+    d_eedf_ = at<double>(d_core_, o_eedf);
+    d_eedf_per_ = at<double>(d_core_, o_eper);
+    d_eadf_ = at<double>(d_core_, o_eadf);
+    d_evdf_ = at<double>(d_core_, o_evdf);
+    d_procf_ = at<ProcF>(d_core_, o_procf);
+    d_gasf_ = at<GasF>(d_core_, o_gasf);
+    SecondarySet q;
+    LGPU_CU(alloc_secondaries(sec_cap_, &q));
+    use_secondaries(q);
+    // pinned host: the scalar read-back, the control block, the running maximum
+    Carve ch;
+    const size_t o_hsc = ch.take<DevScalars>(1), o_hctl = ch.take<IntervalCtl>(1), o_hnum = ch.take<double>(M_);
+    LGPU_CU(cudaMallocHost((void**)&h_pinned_, ch.bytes));
+    h_sc_ = at<DevScalars>(h_pinned_, o_hsc);
+    h_ctl_ = at<IntervalCtl>(h_pinned_, o_hctl);
+    h_nu_max_ = at<double>(h_pinned_, o_hnum);
+    std::memset(h_ctl_, 0, sizeof(IntervalCtl));
+    std::memset(h_nu_max_, 0, (size_t)M_ * sizeof(double));
+    LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
+    LGPU_CU(cudaMemsetAsync(d_sc_, 0, sizeof(DevScalars), stream_));
     return sync("init");
   }
 
@@ -161,19 +233,14 @@ class Engine {
     leave_batch();  // the batch's stream is not this context's to destroy
     if (stream_) cudaStreamSynchronize(stream_);
     drop_graphs();
-    if (d_ctl_) cudaFree(d_ctl_);
-    if (h_ctl_) cudaFreeHost(h_ctl_);
-    d_ctl_ = nullptr;
-    h_ctl_ = nullptr;
-    void* ptrs[] = {d_state_, d_alive_, d_spill_, d_sec_, d_att_, d_claim_, d_removed_, d_pair_slot_,
-                    d_pair_sec_, d_sc_, d_nu_pair_, d_nu_tot_, d_nu_max_, d_nu_coarse_, d_cum_pair_, d_sig_pair_, d_procf_,
-                    d_gasf_, d_is_super_, d_superw_, d_emin_, d_emax_, d_rel_dens_, d_raw_off_, d_raw_len_,
-                    d_raw_e_, d_raw_v_, d_proc_count_, d_proc_gain_, d_proc_loss_, d_eedf_, d_eedf_per_, d_eadf_,
-                    d_evdf_, d_rp_in_, d_rp_out_, d_tt_i_, d_tt_d_, d_tt_raw_, d_post_};
+    void* ptrs[] = {d_core_, d_secbuf_, d_procbuf_, d_rp_in_, d_rp_out_, d_tt_i_, d_tt_d_, d_tt_raw_, d_post_};
     for (void* p : ptrs)
       if (p) cudaFree(p);
-    if (h_sc_) cudaFreeHost(h_sc_);
-    if (h_nu_max_) cudaFreeHost(h_nu_max_);
+    d_core_ = d_secbuf_ = d_procbuf_ = nullptr;
+    if (h_pinned_) cudaFreeHost(h_pinned_);
+    h_pinned_ = nullptr;
+    h_sc_ = nullptr;
+    h_ctl_ = nullptr;
     h_nu_max_ = nullptr;
     if (tables_ev_) cudaEventDestroy(tables_ev_);
     if (ev0_) cudaEventDestroy(ev0_);
@@ -227,38 +294,51 @@ class Engine {
     gases_.assign(gs, gs + nG);
     P_ = nP;
     emax_elastic_ = emax_el;
-    // device copies
-    auto up = [&](auto** d, const auto& h) -> int {
-      using T = typename std::remove_reference<decltype(h)>::type::value_type;
-      if (*d) cudaFree(*d);
-      LGPU_TRY(dalloc(d, h.size()));
-      return cuda(copy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
-    };
-    LGPU_TRY(up(&d_is_super_, is_super));
-    LGPU_TRY(up(&d_superw_, superw));
-    LGPU_TRY(up(&d_emin_, emin));
-    LGPU_TRY(up(&d_emax_, emax));
-    LGPU_TRY(up(&d_rel_dens_, rel));
-    LGPU_TRY(up(&d_raw_off_, raw_off));
-    LGPU_TRY(up(&d_raw_len_, raw_len));
-    LGPU_TRY(up(&d_raw_e_, raw_e));
-    LGPU_TRY(up(&d_raw_v_, raw_v));
-    if (d_cum_pair_) cudaFree(d_cum_pair_);
-    if (d_sig_pair_) cudaFree(d_sig_pair_);
-    d_cum_pair_ = d_sig_pair_ = nullptr;
+    // device copies: the process arrays in one allocation, uploaded with one copy
     stride_ = (nP + 1) & ~1;
-    LGPU_TRY(dalloc(&d_cum_pair_, (size_t)M_ * stride_));
-    LGPU_TRY(dalloc(&d_sig_pair_, (size_t)M_ * stride_));
-    for (auto** d : {&d_proc_gain_, &d_proc_loss_}) {
-      if (*d) cudaFree(*d);
-      *d = nullptr;
-      LGPU_TRY(dalloc(d, (size_t)nP));
+    Carve cv;
+    const size_t o_sup = cv.take<int>(nP), o_sw = cv.take<double>(nP), o_emin = cv.take<double>(nP);
+    const size_t o_emax = cv.take<double>(nP), o_rel = cv.take<double>(nP), o_roff = cv.take<int>(nP);
+    const size_t o_rlen = cv.take<int>(nP), o_re = cv.take<double>(raw_e.size()), o_rv = cv.take<double>(raw_v.size());
+    const size_t uploaded = cv.bytes;
+    const size_t o_cum = cv.take<float2>((size_t)M_ * stride_), o_sig = cv.take<float2>((size_t)M_ * stride_);
+    const size_t o_gain = cv.take<double>(nP), o_loss = cv.take<double>(nP);
+    const size_t o_cnt = cv.take<unsigned long long>(nP);
+    std::vector<char> stage(uploaded, 0);
+    auto put = [&](size_t off, const auto& h) {
+      using T = typename std::remove_reference<decltype(h)>::type::value_type;
+      if (!h.empty()) std::memcpy(stage.data() + off, h.data(), h.size() * sizeof(T));
+    };
+    put(o_sup, is_super);
+    put(o_sw, superw);
+    put(o_emin, emin);
+    put(o_emax, emax);
+    put(o_rel, rel);
+    put(o_roff, raw_off);
+    put(o_rlen, raw_len);
+    put(o_re, raw_e);
+    put(o_rv, raw_v);
+    if (d_procbuf_) {
+      LGPU_TRY(sync("set_processes"));  // nothing in flight still reads the old arrays
+      cudaFree(d_procbuf_);
+      d_procbuf_ = nullptr;
     }
-    if (d_proc_count_) cudaFree(d_proc_count_);
-    d_proc_count_ = nullptr;
-    LGPU_TRY(dalloc(&d_proc_count_, (size_t)nP));
-    if (!d_procf_) LGPU_TRY(dalloc(&d_procf_, (size_t)kMaxProcesses));
-    if (!d_gasf_) LGPU_TRY(dalloc(&d_gasf_, (size_t)kMaxGases));
+    LGPU_TRY(dalloc(&d_procbuf_, cv.bytes));
+    d_is_super_ = at<int>(d_procbuf_, o_sup);
+    d_superw_ = at<double>(d_procbuf_, o_sw);
+    d_emin_ = at<double>(d_procbuf_, o_emin);
+    d_emax_ = at<double>(d_procbuf_, o_emax);
+    d_rel_dens_ = at<double>(d_procbuf_, o_rel);
+    d_raw_off_ = at<int>(d_procbuf_, o_roff);
+    d_raw_len_ = at<int>(d_procbuf_, o_rlen);
+    d_raw_e_ = at<double>(d_procbuf_, o_re);
+    d_raw_v_ = at<double>(d_procbuf_, o_rv);
+    d_cum_pair_ = at<float2>(d_procbuf_, o_cum);
+    d_sig_pair_ = at<float2>(d_procbuf_, o_sig);
+    d_proc_gain_ = at<double>(d_procbuf_, o_gain);
+    d_proc_loss_ = at<double>(d_procbuf_, o_loss);
+    d_proc_count_ = at<unsigned long long>(d_procbuf_, o_cnt);
+    LGPU_CU(copy(d_procbuf_, stage.data(), uploaded, cudaMemcpyHostToDevice));
     have_ion_att_ = false;
     for (int p = 0; p < nP; ++p) have_ion_att_ |= (pr[p].type != kConservative);
     have_procs_ = true;
@@ -784,36 +864,15 @@ class Engine {
     const long long max_cap = std::min<long long>(INT32_MAX / 2, (long long)INT32_MAX - N_ - 32);
     if (sec_cap_ >= max_cap) return LGPU_OK;
     const int new_cap = (int)std::min<long long>(cap, max_cap);
-    const size_t words = ((size_t)N_ + new_cap + 31) / 32;
-    int *alive = nullptr, *removed = nullptr, *pair_slot = nullptr, *pair_sec = nullptr;
-    float4 *spill = nullptr, *sec = nullptr;
-    unsigned int* claim = nullptr;
-    const bool ok = cudaMalloc((void**)&alive, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
-                    cudaMalloc((void**)&spill, 2 * (size_t)new_cap * sizeof(float4)) == cudaSuccess &&
-                    cudaMalloc((void**)&sec, 2 * (size_t)new_cap * sizeof(float4)) == cudaSuccess &&
-                    cudaMalloc((void**)&claim, words * sizeof(unsigned int)) == cudaSuccess &&
-                    cudaMalloc((void**)&removed, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
-                    cudaMalloc((void**)&pair_slot, (size_t)new_cap * sizeof(int)) == cudaSuccess &&
-                    cudaMalloc((void**)&pair_sec, (size_t)new_cap * sizeof(int)) == cudaSuccess;
-    if (!ok) {
-      void* part[] = {alive, spill, sec, claim, removed, pair_slot, pair_sec};
-      for (void* q : part)
-        if (q) cudaFree(q);
+    SecondarySet q;
+    if (alloc_secondaries(new_cap, &q) != cudaSuccess) {
       cudaGetLastError();  // the failed allocation is not the next call's error
       return LGPU_OK;
     }
     LGPU_TRY(sync("grow"));
-    void* old[] = {d_alive_, d_spill_, d_sec_, d_claim_, d_removed_, d_pair_slot_, d_pair_sec_};
-    for (void* q : old) cudaFree(q);
-    d_alive_ = alive;
-    d_spill_ = spill;
-    d_sec_ = sec;
-    d_claim_ = claim;
-    d_removed_ = removed;
-    d_pair_slot_ = pair_slot;
-    d_pair_sec_ = pair_sec;
+    cudaFree(d_secbuf_);
+    use_secondaries(q);
     sec_cap_ = new_cap;
-    claim_words_ = words;
     LGPU_CU(cudaMemsetAsync(d_claim_, 0, claim_words_ * sizeof(unsigned int), stream_));
     drop_graphs();
     slot_built_ = -1;
@@ -1825,7 +1884,8 @@ class Engine {
   // timing
   double adv_ms_ = 0, adv_electron_steps_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
   long long adv_launches_ = 0, launches_ = 0;
-  // device buffers
+  // device buffers (carved from d_core_, d_secbuf_ and d_procbuf_) and the pinned host block
+  char *d_core_ = nullptr, *d_secbuf_ = nullptr, *d_procbuf_ = nullptr, *h_pinned_ = nullptr;
   float4* d_state_ = nullptr;
   int* d_alive_ = nullptr;
   float4* d_spill_ = nullptr;

@@ -271,40 +271,58 @@ def replay_flights_noalloc(device, E, freq_hz, red_mag, cyclotron, t, dt, pos, v
     return po, vo, eo, go
 
 
+def _struct_dtype(st):
+    """A numpy record type with the layout of a ctypes structure of ints,
+    doubles and pointers (pointers as unsigned addresses)."""
+    names, formats, offsets = [], [], []
+    for name, ct in st._fields_:
+        names.append(name)
+        formats.append(np.int32 if ct is I else (np.float64 if ct is D else np.uintp))
+        offsets.append(getattr(st, name).offset)
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": ctypes.sizeof(st)})
+
+
+_PROCESS_DTYPE = None
+
+
 def process_arrays(ps, gas_first, gas_last, gas_fraction):
     """lgpu_process / lgpu_gas arrays of a ProcessSet-like object (see
-    synth.ProcessSet); the third value holds the raw arrays the structs point to."""
+    synth.ProcessSet); the third value holds the arrays the structs point to.
+    The records are filled column by column (a mixture of 65 processes in
+    tens of microseconds, where a per-field loop took about half a
+    millisecond per context)."""
+    global _PROCESS_DTYPE
+    if _PROCESS_DTYPE is None:
+        _PROCESS_DTYPE = _struct_dtype(Process)
     n = ps.n
-    arr = (Process * n)()
-    keep = []
-    for p in range(n):
-        q = arr[p]
-        q.type = int(ps.ptype[p])
-        q.is_super = int(ps.is_super[p])
-        q.is_elastic = int(ps.is_elastic[p])
-        q.sampler = int(ps.sampler[p])
-        q.sampler_p0 = float(ps.sampler_p0[p])
-        q.sampler_p1 = float(ps.sampler_p1[p])
-        q.superw = float(ps.superw[p])
-        q.emin = float(ps.emin[p])
-        q.emax = float(ps.emax[p])
-        q.rel_dens = float(ps.rel_dens[p])
-        q.mass = float(ps.mass[p])
-        q.eloss = float(ps.eloss[p])
-        q.wparam = float(ps.wparam[p])
-        e = np.ascontiguousarray(ps.raw_e[p], dtype=np.float64)
-        v = np.ascontiguousarray(ps.raw_v[p], dtype=np.float64)
-        keep += [e, v]
-        q.raw_len = len(e) if not ps.is_super[p] else 0
-        q.raw_e = dptr(e)
-        q.raw_v = dptr(v)
+    rec = np.zeros(n, dtype=_PROCESS_DTYPE)
+    for name, src, t in (("type", ps.ptype, np.int32), ("is_super", ps.is_super, np.int32),
+                         ("is_elastic", ps.is_elastic, np.int32), ("sampler", ps.sampler, np.int32),
+                         ("sampler_p0", ps.sampler_p0, np.float64), ("sampler_p1", ps.sampler_p1, np.float64),
+                         ("superw", ps.superw, np.float64), ("emin", ps.emin, np.float64),
+                         ("emax", ps.emax, np.float64), ("rel_dens", ps.rel_dens, np.float64),
+                         ("mass", ps.mass, np.float64), ("eloss", ps.eloss, np.float64),
+                         ("wparam", ps.wparam, np.float64)):
+        rec[name] = np.asarray(src, dtype=t)[:n]
+    raw_e = [np.ascontiguousarray(x, dtype=np.float64).ravel() for x in ps.raw_e[:n]]
+    raw_v = [np.ascontiguousarray(x, dtype=np.float64).ravel() for x in ps.raw_v[:n]]
+    len_e = np.array([len(x) for x in raw_e], dtype=np.int64)
+    len_v = np.array([len(x) for x in raw_v], dtype=np.int64)
+    e_all = np.concatenate(raw_e + [np.zeros(1)])
+    v_all = np.concatenate(raw_v + [np.zeros(1)])
+    off_e = np.concatenate([[0], np.cumsum(len_e)[:-1]]) if n else np.zeros(0, np.int64)
+    off_v = np.concatenate([[0], np.cumsum(len_v)[:-1]]) if n else np.zeros(0, np.int64)
+    rec["raw_len"] = np.where(np.asarray(ps.is_super[:n]) != 0, 0, len_e).astype(np.int32)
+    rec["raw_e"] = e_all.ctypes.data + 8 * off_e.astype(np.uint64)
+    rec["raw_v"] = v_all.ctypes.data + 8 * off_v.astype(np.uint64)
+    arr = rec.ctypes.data_as(P_(Process))
     G = len(gas_first)
     gs = (Gas * G)()
     for g in range(G):
         gs[g].first = int(gas_first[g])
         gs[g].last = int(gas_last[g])
         gs[g].fraction = float(gas_fraction[g])
-    return arr, gs, keep
+    return arr, gs, [rec, e_all, v_all]
 
 
 class Context:
