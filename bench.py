@@ -65,13 +65,13 @@ STATE_BYTES_PER_ELECTRON_STEP = 64  # 32 B state read + 32 B written per electro
 E_N = 200.0
 N_ELECTRONS = 1_000_000
 # DRAM bytes per electron and interval of k_advance, from one ncu capture of the
-# same kernel on 4e6 electrons (profiles/k_advance_n2_dc200.md): 130.5 MB read +
+# same kernel on 4e6 electrons (N2-like gas, DC 200 Td): 130.5 MB read +
 # 73.8 MB written; traffic grows in proportion to the electrons advanced
 DRAM_BYTES_PER_ELECTRON_STEP = (130.522112e6 + 73.842176e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch, the
 # collision-stash shape the tuner picks, 512 x 2), from one ncu capture of the
-# sweep (profiles/k_advance_batch_sweep64.md): 901.6 MB read + 561.8 MB written
+# sweep (the 41st interval, schedule 5,20,1): 901.6 MB read + 561.8 MB written
 # for 1.98e7 electrons
 SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (901.582848e6 + 561.755904e6) / 19795598
 
@@ -702,7 +702,7 @@ def ops_real(n_processes):
 
 
 # ncu counters of one batched DC advance launch over the sweep (1.98e7
-# electrons, collision-stash shape 512 x 2, profiles/k_advance_batch_sweep64.md): warp
+# electrons, collision-stash shape 512 x 2, the same launch as above): warp
 # instructions per electron-interval issued to the FMA, ALU and XU (SFU) pipes
 NCU_PIPE_PER_ELECTRON = {"fma": 182203341 / 19795598, "alu": 244065090 / 19795598, "xu": 12202573 / 19795598}
 
