@@ -57,3 +57,31 @@ def test_status_codes_without_device():
     lib.lgpu_destroy(h)
     assert lib.lgpu_create(None, ctypes.byref(h)) == 1  # LGPU_ERR_BAD_ARG
     assert lib.lgpu_solve(None, None) == 1
+
+
+def test_process_records_carry_every_field_and_table():
+    """The lgpu_process records the front end builds column by column hold
+    each process's fields, and their raw pointers read back each process's
+    own cross-section table (a superelastic copy has none)."""
+    import numpy as np
+
+    from lokigpu import synth
+
+    ps = synth.flatten([synth.n2_like_gas(fraction=0.8), synth.o2_like_gas(fraction=0.2)])
+    arr, gs, keep = capi.process_arrays(ps, ps.gas_first, ps.gas_last, ps.gas_fraction)
+    assert ctypes.sizeof(capi.Process) == capi._PROCESS_DTYPE.itemsize
+    for p in range(ps.n):
+        q = arr[p]
+        assert (q.type, q.is_super, q.is_elastic, q.sampler) == (int(ps.ptype[p]), int(ps.is_super[p]),
+                                                                 int(ps.is_elastic[p]), int(ps.sampler[p]))
+        for name, src in (("sampler_p0", ps.sampler_p0), ("sampler_p1", ps.sampler_p1), ("superw", ps.superw),
+                          ("emin", ps.emin), ("emax", ps.emax), ("rel_dens", ps.rel_dens), ("mass", ps.mass),
+                          ("eloss", ps.eloss), ("wparam", ps.wparam)):
+            assert getattr(q, name) == float(src[p]), (p, name)
+        e = np.asarray(ps.raw_e[p], dtype=np.float64)
+        v = np.asarray(ps.raw_v[p], dtype=np.float64)
+        assert q.raw_len == (0 if ps.is_super[p] else len(e))
+        assert [q.raw_e[k] for k in range(len(e))] == list(e)
+        assert [q.raw_v[k] for k in range(len(v))] == list(v)
+    assert [(g.first, g.last, g.fraction) for g in gs] == [
+        (int(a), int(b), float(c)) for a, b, c in zip(ps.gas_first, ps.gas_last, ps.gas_fraction)]
