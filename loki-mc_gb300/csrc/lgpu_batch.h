@@ -39,6 +39,10 @@ class Batch {
   int device_ = 0, max_slots_ = 0, sm_count_ = 1;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  // field branches after the first run their advance on side streams, forked
+  // from and joined to the batch stream inside the interval graph
+  cudaStream_t side_[kFieldModes - 1] = {};
+  cudaEvent_t fork_ = nullptr, join_[kFieldModes - 1] = {};
   char* h_stage_ = nullptr;
   char* d_stage_ = nullptr;
   char* h_hstage_ = nullptr;  // the distribution passes' staging (same layout)
@@ -205,6 +209,11 @@ class Batch {
     if ((rc = cuda(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device), "attribute"))) return rc;
     if ((rc = cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream"))) return rc;
     if ((rc = cuda(cudaEventCreate(&ev0_), "event")) || (rc = cuda(cudaEventCreate(&ev1_), "event"))) return rc;
+    if ((rc = cuda(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event"))) return rc;
+    for (int k = 0; k < kFieldModes - 1; ++k)
+      if ((rc = cuda(cudaStreamCreateWithFlags(&side_[k], cudaStreamNonBlocking), "stream")) ||
+          (rc = cuda(cudaEventCreateWithFlags(&join_[k], cudaEventDisableTiming), "event")))
+        return rc;
     const size_t sb = stage_bytes();
     if ((rc = cuda(cudaMallocHost((void**)&h_stage_, sb), "cudaMallocHost"))) return rc;
     if ((rc = cuda(cudaMalloc((void**)&d_stage_, sb), "cudaMalloc"))) return rc;
@@ -239,6 +248,14 @@ class Batch {
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     ev0_ = ev1_ = nullptr;
+    if (fork_) cudaEventDestroy(fork_);
+    fork_ = nullptr;
+    for (int k = 0; k < kFieldModes - 1; ++k) {
+      if (join_[k]) cudaEventDestroy(join_[k]);
+      if (side_[k]) cudaStreamDestroy(side_[k]);
+      join_[k] = nullptr;
+      side_[k] = nullptr;
+    }
     if (stream_) cudaStreamDestroy(stream_);
     stream_ = nullptr;
   }
@@ -276,7 +293,25 @@ class Batch {
         const BatchArgs b = args(d_stage_);
         n = launch_batch_pre(b, sm_count_, max_slots_, parts, stream_);
         cudaEventRecordWithFlags(ev0_, stream_, cudaEventRecordExternal);
-        n += launch_batch_advance(b, sm_count_, parts, (int)(parts >> kGraphShapeShift), stream_);
+        // one persistent launch per field branch; with several branches they
+        // run side by side, so the blocks of one fill the SMs another's tail
+        // leaves idle (each branch's slots are its own: nothing is shared)
+        const int shape = (int)(parts >> kGraphShapeShift);
+        const unsigned modes = parts & ((1u << kFieldModes) - 1u);
+        const unsigned rest = parts & ~((1u << kFieldModes) - 1u);
+        int first = 0;
+        while (first < kFieldModes && !(modes & (1u << first))) ++first;
+        int k = 0;
+        if (modes & ~(1u << first)) cudaEventRecord(fork_, stream_);
+        for (int m = first + 1; m < kFieldModes; ++m) {
+          if (!(modes & (1u << m))) continue;
+          cudaStreamWaitEvent(side_[k], fork_, 0);
+          n += launch_batch_advance(b, sm_count_, rest | (1u << m), shape, side_[k]);
+          cudaEventRecord(join_[k], side_[k]);
+          ++k;
+        }
+        if (first < kFieldModes) n += launch_batch_advance(b, sm_count_, rest | (1u << first), shape, stream_);
+        for (int j = 0; j < k; ++j) cudaStreamWaitEvent(stream_, join_[j], 0);
         cudaEventRecordWithFlags(ev1_, stream_, cudaEventRecordExternal);
         n += launch_batch_post(b, sm_count_, max_slots_, parts, stream_);
       }
