@@ -108,6 +108,14 @@ struct AdvSharedT {
   static constexpr bool kProcsInShared = STASH == 0;
   float nu_coarse[kMaxCoarse];  // block bounds of the total frequency of the current condition
   unsigned int count[kMaxProcesses];
+  // energy changes per process and sign: the count of collisions that lost
+  // energy, and the FP32 sums of dE - off, off the process's nominal change
+  // (-threshold; 0 for attachment). The flush adds the nominal part back as
+  // count x off in FP64, so FP32 only sums the small remainders (the recoil
+  // of inelastic collisions): a block adds thousands of nearly equal
+  // inelastic losses per process and interval, whose plain FP32 sum would
+  // round by up to ~1e-4 relative
+  unsigned int neg[kMaxProcesses];
   float gain[kMaxProcesses];
   float loss[kMaxProcesses];
   ProcF proc[kProcsInShared ? kMaxProcesses : 1];
@@ -203,6 +211,7 @@ template <class Sh>
 __device__ __forceinline__ void load_block_consts(const AdvanceArgs& a, Sh& sh) {
   for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
     sh.count[q] = 0u;
+    sh.neg[q] = 0u;
     sh.gain[q] = 0.0f;
     sh.loss[q] = 0.0f;
     if constexpr (Sh::kProcsInShared) sh.proc[q] = a.procs[q];
@@ -341,6 +350,11 @@ __device__ __forceinline__ const ProcF* procs_of(const AdvanceArgs& a, const Sh&
   else return a.procs;
 }
 
+// A process's nominal energy change per collision (eV): minus its threshold
+// (the gain of a superelastic process), none for attachment, whose loss is
+// the electron's whole energy.
+__device__ __forceinline__ float nominal_change(const ProcF& p) { return p.type == kAttachment ? 0.0f : -p.eloss; }
+
 // The collision turn: process choice, kinematics, tallies, secondaries and
 // attachment (BoltzmannMC.C:907-1280).
 template <class Sh>
@@ -356,9 +370,14 @@ __device__ __forceinline__ void lane_real(const AdvanceArgs& a, Sh& sh, int wid,
   } else {
     ++tl.real_n;
     atomicAdd(&sh.count[cr.chosen], 1u);
-    if (cr.dE >= 0.0f) atomicAdd(&sh.gain[cr.chosen], cr.dE);
-    else atomicAdd(&sh.loss[cr.chosen], cr.dE);
     const int ptype = procs[cr.chosen].type;
+    const float rest = cr.dE - nominal_change(procs[cr.chosen]);
+    if (cr.dE >= 0.0f) {
+      if (rest != 0.0f) atomicAdd(&sh.gain[cr.chosen], rest);
+    } else {
+      atomicAdd(&sh.neg[cr.chosen], 1u);
+      if (rest != 0.0f) atomicAdd(&sh.loss[cr.chosen], rest);
+    }
     if (ptype == kIonization) {
       const float4 A = make_float4(L.p.x, L.p.y, L.p.z, L.t);
       const float4 B = make_float4(cr.ej_v.x, cr.ej_v.y, cr.ej_v.z, 0.0f);
@@ -438,11 +457,14 @@ __device__ __forceinline__ void block_flush(const AdvanceArgs& a, Sh& sh, const 
     if (ns) atomicAdd(a.null_count, ns);
     if (rs) atomicAdd(a.real_count, rs);
   }
+  const ProcF* procs = procs_of(a, sh);
   for (int q = threadIdx.x; q < a.P; q += blockDim.x) {
     if (sh.count[q]) {
       atomicAdd(&a.proc_count[q], (unsigned long long)sh.count[q]);
-      if (sh.gain[q] != 0.0f) atomicAdd(&a.proc_gain[q], (double)sh.gain[q]);
-      if (sh.loss[q] != 0.0f) atomicAdd(&a.proc_loss[q], (double)sh.loss[q]);
+      const double off = (double)nominal_change(procs[q]);
+      const unsigned int n_loss = sh.neg[q], n_gain = sh.count[q] - n_loss;
+      if (n_gain) atomicAdd(&a.proc_gain[q], (double)n_gain * off + (double)sh.gain[q]);
+      if (n_loss) atomicAdd(&a.proc_loss[q], (double)n_loss * off + (double)sh.loss[q]);
     }
   }
 }
