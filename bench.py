@@ -71,9 +71,9 @@ DRAM_BYTES_PER_ELECTRON_STEP = (130.522112e6 + 73.842176e6) / 4.0e6
 
 # DRAM bytes per electron and interval of the batched advance (DC launch, the
 # collision-stash shape the tuner picks, 512 x 2), from one ncu capture of the
-# sweep (the 41st interval, schedule 5,20,1): 901.6 MB read + 561.8 MB written
+# sweep (the 41st interval, schedule 5,20,1): 888.3 MB read + 560.6 MB written
 # for 1.98e7 electrons
-SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (901.582848e6 + 561.755904e6) / 19795598
+SWEEP_DRAM_BYTES_PER_ELECTRON_STEP = (888.269312e6 + 560.615424e6) / 19795598
 
 # sweep workload
 SWEEP_POINTS = 64
@@ -704,7 +704,7 @@ def ops_real(n_processes):
 # ncu counters of one batched DC advance launch over the sweep (1.98e7
 # electrons, collision-stash shape 512 x 2, the same launch as above): warp
 # instructions per electron-interval issued to the FMA, ALU and XU (SFU) pipes
-NCU_PIPE_PER_ELECTRON = {"fma": 182203341 / 19795598, "alu": 244065090 / 19795598, "xu": 12202573 / 19795598}
+NCU_PIPE_PER_ELECTRON = {"fma": 181978916 / 19795598, "alu": 244863326 / 19795598, "xu": 12198627 / 19795598}
 
 
 def issue_roofline(real, null, electron_steps, kernel_ms, n_processes, flight_ops, sm_mhz):
